@@ -1,0 +1,391 @@
+#!/usr/bin/env python
+"""Benchmark of the beamforming hot path: pixel x tx x rx samples per second.
+
+Workload (the plain Tabbed DAS, FP32, cubic configuration): 128-element linear
+array at 0.3 mm pitch, 11 plane waves over -10..+10 deg, fs 25 MHz, Nt 2048,
+c 1540 m/s, seeded channel data (20 points + 5000 speckle, 5 MHz pulse at 60 %
+bandwidth, -40 dB noise), 256 x 512 pixel grid; tautx/taurx from the
+plane-wave geometry, apodtx ones, apodrx Hann inside an F#1.5 mask.
+One step = one frame: spline prefilter + delay-and-sum (two kernel launches).
+
+  value     device-resident throughput (inputs already in HBM), L2 flushed
+            (256 MiB write) before every step, CUDA events on the launch stream
+  e2e       the same through the public API (TabbedBeamformer.__call__) from
+            pinned host memory: H2D of the frame, kernels, D2H of the image
+  roofline  the delay-and-sum kernel: algorithmic bytes (0.855 B/tap: tables,
+            channel data and image) over its event-timed duration, against the
+            measured HBM copy bandwidth; an FP32 roofline beside it
+  cpu_baseline  the CPU oracle (a float32 restatement of the reference's C
+            path) or the reference's own compiled C, all host cores, ~10 s
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun (N > 1) each rank beamforms its own frames on its own GPU (the
+path shards by frame with no exchange); the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as ct
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DAS pixel×tx×rx samples/s at ≤1e-3 rel-L2; batched/fp16 & fwd+adj vs plain"
+UNIT = "samples/s"
+BYTES_PER_TAP_NOTE = "tables 145.8 MB + channel data 11.5 MB + image 0.5 MB per frame"
+WORKLOAD = "tabbed_das_fp32_cubic_128el_11pw_2048s_256x512"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--pixel-order", default="auto", choices=["auto", "natural"])
+    return ap.parse_args()
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def c1_workload(device):
+    from pycbf_gb300 import phantom
+    return phantom.linear_pw_tabbed(device=device)
+
+
+def taps_of(w):
+    return w.tautx.shape[0] * w.taurx.shape[0] * w.tautx.shape[1]
+
+
+def algorithmic_bytes(w):
+    ntx, np_ = w.tautx.shape
+    nrx = w.taurx.shape[0]
+    return 4 * (2 * (ntx + nrx) * np_ + ntx * nrx * w.nt + np_)
+
+
+# ---------------------------------------------------------------------------
+# CPU side
+# ---------------------------------------------------------------------------
+def cpu_baseline(w, seconds):
+    from oracle import oracle
+    threads = max(1, len(os.sched_getaffinity(0)))
+    kind = "port"
+    use_ref = False
+    if oracle.ref_lib() is not None:
+        kind, use_ref = "reference", True
+    taps = taps_of(w)
+    args = (w.rf, w.tautx, w.apodtx, w.taurx, w.apodrx, w.t0, w.dt, w.nt)
+    n = 0
+    t = time.perf_counter()
+    while True:
+        oracle.das_tabbed(*args, interp="cubic", threads=1 if use_ref else threads, use_ref=use_ref)
+        n += 1
+        el = time.perf_counter() - t
+        if el >= seconds:
+            break
+    cores = 1 if use_ref else threads
+    return {"value": taps * n / el, "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": f"{n} full frames of the workload ({taps} taps each) in {el:.1f} s, "
+                      f"{'reference pycbf.c per channel, 1 thread' if use_ref else f'oracle, {threads} threads over transmits'}"}
+
+
+def run_reference_arm(a):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    w = c1_workload("cpu")
+    from oracle import oracle
+    threads = max(1, len(os.sched_getaffinity(0)))
+    use_ref = oracle.ref_lib() is not None
+    kind = "reference" if use_ref else "port"
+    args = (w.rf, w.tautx, w.apodtx, w.taurx, w.apodrx, w.t0, w.dt, w.nt)
+    run = lambda: oracle.das_tabbed(*args, interp="cubic", threads=1 if use_ref else threads,
+                                    use_ref=use_ref)
+    for _ in range(a.warmup):
+        run()
+    times = []
+    for _ in range(a.steps):
+        t = time.perf_counter()
+        run()
+        times.append(time.perf_counter() - t)
+    total = sum(times)
+    taps = taps_of(w)
+    value = taps * a.steps / total
+    cores = 1 if use_ref else threads
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * total / a.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded phantom)",
+        "config": {"workload": WORKLOAD, "global_batch": 1, "frames_per_step": 1},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": f"one full frame per step ({taps} taps), "
+                                   f"{'reference pycbf.c, 1 thread' if use_ref else f'CPU oracle restating pycbf.c, {threads} threads'}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as fp:
+            for line in fp:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def main_ours(a):
+    import torch
+    import torch.distributed as dist
+
+    import pycbf_gb300 as pg
+    from pycbf_gb300 import _lib
+
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    L = _lib.load()
+
+    w = c1_workload(dev)
+    taps = taps_of(w)
+    bf = pg.TabbedBeamformer(tautx=w.tautx, taurx=w.taurx, apodtx=w.apodtx, apodrx=w.apodrx,
+                             t0=w.t0, dt=w.dt, nt=w.nt, interp={"kind": "cubic"},
+                             pixel_order=a.pixel_order)
+    cnt, _ = bf.tap_census()
+    n_contrib = int(cnt.sum().item())
+    rf = torch.as_tensor(w.rf, device=dev).contiguous()
+    info = bf._rfinfo(None)
+    ws, nws = bf._workspace_for(info)
+    out = torch.empty(bf.nop, device=dev)
+    tautx, apodtx, taurx, apodrx = bf._tables
+    pidx = ct.c_void_p(bf._pixel_index.data_ptr()) if bf._pixel_index is not None else None
+    P = lambda t: ct.c_void_p(t.data_ptr())
+    args_spline = (ct.byref(info), P(rf), P(ws), nws)
+    args_das = (ct.byref(info), P(ws), P(tautx), P(apodtx), P(taurx), P(apodrx), bf.nop, pidx,
+                ct.c_float(0.01), 3, P(out))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > L2
+    stream = torch.cuda.current_stream()
+    sp = ct.c_void_p(stream.cuda_stream)
+
+    def step(ev):
+        flush.zero_()
+        ev[0].record(stream)
+        _lib.check(L.pycbf_gb_spline_coefficients(*args_spline, sp), "spline")
+        ev[1].record(stream)
+        _lib.check(L.pycbf_gb_das_tabbed_prefiltered(*args_das, sp), "das")
+        ev[2].record(stream)
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(a.steps)]
+    for _ in range(a.warmup):
+        step(evs[0])
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter()
+    for k in range(a.steps):
+        step(evs[k])
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    spline_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    das_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    total_ms = sum(s + d for s, d in zip(spline_ms, das_ms))
+    if world > 1:
+        tt = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    value = world * taps * a.steps / (total_ms * 1e-3)
+
+    # end to end through the public API, pinned host input, numpy output
+    rf_host = torch.from_numpy(w.rf).pin_memory()
+    for _ in range(max(1, a.warmup)):
+        bf(rf_host)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    t = time.perf_counter()
+    for _ in range(a.steps):
+        img = bf(rf_host)
+    e2e_s = time.perf_counter() - t
+    if world > 1:
+        tt = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = {"value": world * taps * a.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(rf_host.numel() * rf_host.element_size()),
+           "d2h_bytes_per_step": int(img.size * img.itemsize),
+           "ms_per_step": 1e3 * e2e_s / a.steps}
+
+    # roofline of the delay-and-sum kernel
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fp:
+            peaks = json.load(fp)
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs") or 6800.0
+    das_s = statistics.mean(das_ms) * 1e-3
+    alg_bytes = algorithmic_bytes(w)
+    achieved = alg_bytes / das_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": None,
+                "kernel": "das_kernel<tabbed, cubic, tx_and_rx, f32>",
+                "kernel_ms": 1e3 * das_s, "spline_ms": statistics.mean(spline_ms),
+                "peak_source": "measured" if peaks.get("hbm_gbs") else "fallback",
+                "algorithmic_bytes": alg_bytes}
+    traffic_file = os.path.join(ROOT, "profiles", "das_tabbed_cubic_c1.traffic.json")
+    if os.path.exists(traffic_file):
+        with open(traffic_file) as fp:
+            roofline["traffic"] = json.load(fp).get("dram_bytes_per_launch")
+    # FP32 roofline: algorithmic FLOPs (20 per contributing cubic tap, 2 per tap for the
+    # weight product and threshold) over the kernel time, against the FMA probe
+    probe_out = torch.empty(152 * 8 * 256, device=dev)
+    iters = 4096
+    L.pycbf_gb_fp32_probe(P(probe_out), 152 * 8, iters, sp)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    L.pycbf_gb_fp32_probe(P(probe_out), 152 * 8, iters, sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fp32_peak = 152 * 8 * 256 * iters * 16 / (e0.elapsed_time(e1) * 1e-3) / 1e12
+    flops = 20 * n_contrib + 2 * taps
+    fp32 = {"achieved": flops / das_s / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": flops / das_s / 1e12 / fp32_peak, "flops_per_launch": flops,
+            "contributing_taps": n_contrib, "peak_source": "measured (FMA probe)"}
+
+    variants = {}
+    if not a.no_variants:
+        variants = run_variants(a, w, dev, taps)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": total_ms / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded phantom, 20 points + 5000 speckle)",
+        "config": {"workload": WORKLOAD, "global_batch": world, "frames_per_step": 1,
+                   "interp": "cubic", "pixel_order": a.pixel_order,
+                   "l2": "flushed (256 MiB write) before each step",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": e2e, "roofline": roofline, "fp32_roofline": fp32,
+        "gpu_launches": 2 * a.steps, "clocks": clk,
+        "wall_s_timed": t_wall, "variants": variants,
+    }
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, a.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_variants(a, w, dev, taps):
+    """Secondary lines: batched frames with FP16/BF16 storage, and nearest."""
+    import numpy as np
+    import torch
+
+    import pycbf_gb300 as pg
+    res = {}
+    nfr = 8
+    rng = np.random.default_rng(0)
+    frames = np.stack([w.rf] + [w.rf * np.float32(rng.uniform(0.5, 1.5)) for _ in range(nfr - 1)])
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    for name, storage, kind, nf in (("fp32_batch8", "float32", "cubic", nfr),
+                                    ("fp16_batch8", "float16", "cubic", nfr),
+                                    ("bf16_batch8", "bfloat16", "cubic", nfr),
+                                    ("nearest_fp32", "float32", "nearest", 1)):
+        bf = pg.TabbedBeamformer(tautx=w.tautx, taurx=w.taurx, apodtx=w.apodtx, apodrx=w.apodrx,
+                                 t0=w.t0, dt=w.dt, nt=w.nt, interp={"kind": kind}, storage=storage)
+        x = torch.as_tensor(frames[:nf] if nf > 1 else w.rf, device=dev).to(
+            {"float32": torch.float32, "float16": torch.float16, "bfloat16": torch.bfloat16}[storage])
+        out = torch.empty(bf._out_shape(nf if nf > 1 else None), device=dev)
+        for _ in range(3):
+            bf(x, out_as_numpy=False, buffer=out)
+        times = []
+        for _ in range(max(3, a.steps // 2)):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            bf(x, out_as_numpy=False, buffer=out)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) * 1e-3)
+        res[name] = {"value": taps * nf / statistics.mean(times), "unit": UNIT,
+                     "ms_per_call": 1e3 * statistics.mean(times), "frames_per_call": nf,
+                     "storage": storage, "interp": kind}
+    return res
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference_arm(a)
+    else:
+        main_ours(a)
+
+
+if __name__ == "__main__":
+    main()

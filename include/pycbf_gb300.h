@@ -1,0 +1,226 @@
+/*
+ * pycbf_gb300.h -- C ABI of the GB300 (sm_103a) beamforming kernels.
+ *
+ * Plain C types only: device pointers are `void *` / `float *`, sizes are
+ * integers, streams are passed as `void *` (a cudaStream_t; NULL = the legacy
+ * default stream).  Every entry point:
+ *   - validates its arguments on the host first and returns a status code
+ *     (never aborts, never prints);
+ *   - allocates no device memory: scratch comes from the caller's workspace
+ *     (size from pycbf_gb_workspace_bytes);
+ *   - is stream-ordered and does not synchronise;
+ *   - keeps no mutable global state, so it is safe to call from several
+ *     host threads on distinct outputs.
+ *
+ * All arithmetic is float32.  Channel data may be stored as float32, float16
+ * or bfloat16; delays, weights and sums stay float32.
+ */
+#ifndef PYCBF_GB300_H
+#define PYCBF_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PYCBF_GB_ABI_VERSION 1
+
+/* status codes */
+enum {
+    PYCBF_GB_OK = 0,
+    PYCBF_GB_EINVAL = 1,       /* null pointer, negative size or unknown code       */
+    PYCBF_GB_ERANGE = 2,       /* sizes beyond what the kernels index                */
+    PYCBF_GB_EWORKSPACE = 3,   /* workspace missing or smaller than required         */
+    PYCBF_GB_EUNSUPPORTED = 4, /* combination this path does not implement           */
+    PYCBF_GB_ECUDA = 5         /* a CUDA call failed: see pycbf_gb_last_cuda_error() */
+};
+
+/* storage type of channel data */
+enum { PYCBF_GB_F32 = 0, PYCBF_GB_F16 = 1, PYCBF_GB_BF16 = 2 };
+
+/* interpolation kinds */
+enum {
+    PYCBF_GB_INTERP_NEAREST = 0,      /* pycbf.c:264-267 (usf = 1)                          */
+    PYCBF_GB_INTERP_LINEAR = 1,       /* two-point part of the cubic formula, cubic's range */
+    PYCBF_GB_INTERP_CUBIC = 2,        /* natural cubic spline, pycbf.c:68-166               */
+    PYCBF_GB_INTERP_LINEAR_FLOOR = 3  /* __engines__.cu:36-53 as written (floor sample)     */
+};
+
+/* how taps are summed; 0..3 are the reference's flag values (__engines__.cu:500-504) */
+enum {
+    PYCBF_GB_SUM_NONE = 0,        /* out (nframes, ntx, nrx, np)                         */
+    PYCBF_GB_SUM_TX_ONLY = 1,     /* out (nframes, nrx, np): summed over transmits       */
+    PYCBF_GB_SUM_RX_ONLY = 2,     /* out (nframes, ntx, np): summed over receives        */
+    PYCBF_GB_SUM_TX_AND_RX = 3,   /* out (nframes, np)                                   */
+    PYCBF_GB_SUM_DMAS_SSR = 4,    /* out (nframes, np): sum over all receive pairs i<j of
+                                     sign(a_i a_j) sqrt|a_i a_j|, a = transmit sums       */
+    PYCBF_GB_SUM_DMAS_POWER = 5   /* out (nframes, np): sum over all pairs i<j of a_i a_j */
+};
+
+/* Channel-data description; mirrors RFInfo of pycbf/gpu/__engines__.cu:369-374
+ * plus the frame count and the storage type.  rfdata is (nframes, ntx, nrx, nt),
+ * C-contiguous. */
+typedef struct pycbf_gb_rfinfo {
+    long long ntx;
+    long long nrx;
+    int ndim;            /* 0 for Tabbed; 2 or 3 for Synthetic                   */
+    float t0;            /* time of sample 0 (tInfo.x0)                            */
+    float dt;            /* sample period (tInfo.dx)                               */
+    int nt;              /* samples per channel (tInfo.nx)                         */
+    long long nframes;
+    int dtype;           /* PYCBF_GB_F32 / _F16 / _BF16                            */
+} pycbf_gb_rfinfo;
+
+/* Synthetic-point geometry, all device pointers (float32).  The fields follow
+ * the Synthetic dataclass (pycbf/__bf_base_classes__.py:166-178).  The acos
+ * tests of __engines__.cu:412,427,468 are evaluated as cosine compares, so
+ * the caller passes cos(ala) per element, and per transmit sec(ala) =
+ * sqrt(1 + tan^2 ala) and dof*sin(ala)/2 (each computed in double, rounded to
+ * float). */
+typedef struct pycbf_gb_synthetic {
+    const float *ovectx;       /* (ntx, ndim) */
+    const float *nvectx;       /* (ntx, ndim) */
+    const float *t0tx;         /* (ntx)       */
+    const float *alatx;        /* (ntx)       */
+    const float *doftx;        /* (ntx)       */
+    const float *cosalatx;     /* (ntx)       */
+    const float *secalatx;     /* (ntx)       */
+    const float *halfdofsintx; /* (ntx)       */
+    const float *ovecrx;       /* (nrx, ndim) */
+    const float *nvecrx;       /* (nrx, ndim) */
+    const float *cosalarx;     /* (nrx)       */
+    const float *pnts;         /* (np, ndim)  */
+    long long np;
+    float c0;
+} pycbf_gb_synthetic;
+
+/* ---------------------------------------------------------------------- */
+/* housekeeping                                                            */
+/* ---------------------------------------------------------------------- */
+int pycbf_gb_abi_version(void);
+const char *pycbf_gb_status_string(int status);
+/* cudaError_t of the last failed CUDA call made by this thread (0 if none) */
+int pycbf_gb_last_cuda_error(void);
+
+/* Bytes of workspace a Tabbed or Synthetic call with this channel data and
+ * interpolation kind needs (0 for nearest/linear; the spline coefficients for
+ * cubic). */
+size_t pycbf_gb_workspace_bytes(const pycbf_gb_rfinfo *rf, int interp);
+
+/* ---------------------------------------------------------------------- */
+/* Natural cubic spline coefficients of every channel.                     */
+/* Replaces tie_knots1D_fixed (pycbf/cpu/pycbf.c:114-166), which the      */
+/* reference runs per channel inside beamform_cubic (pycbf.c:194).        */
+/* coef receives, per channel and sample j, (y_j, y_j+1, z_j, z_j+1) with  */
+/* z = y'' dt^2 / 6 and y_nt = z_nt = 0; float32 x4 for F32 channel data,  */
+/* the storage type x4 otherwise.  coef must hold                          */
+/* pycbf_gb_workspace_bytes(rf, PYCBF_GB_INTERP_CUBIC) bytes.              */
+/* ---------------------------------------------------------------------- */
+int pycbf_gb_spline_coefficients(const pycbf_gb_rfinfo *rf, const void *rfdata, void *coef,
+                                 size_t coef_bytes, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Tabbed delay-and-sum.                                                   */
+/* Replaces the per-channel C call beamform_cubic / beamform_nearest       */
+/* (pycbf/cpu/pycbf.h:27-54, driven by cpu/__core_bf_classes__.py:149-192) */
+/* and the CuPy kernels das_bmode_tabbed_korder_cubic /                    */
+/* das_bmode_tabbed_multi_interp (pycbf/gpu/__engines__.cu:726-864,        */
+/* launched by gpu/__core_bf_classes__.py:291-354).                        */
+/*                                                                          */
+/* tautx, apodtx: (ntx, np); taurx, apodrx: (nrx, np), float32, device.    */
+/* A tap (pixel, tx, rx) contributes when |apodtx*apodrx| >= thresh and    */
+/* the delay tautx+taurx is in range (pycbf.c:200-203, 84-87, 264-267).    */
+/* pixel_index: NULL, or int32[np]: table column i is written to output    */
+/* pixel pixel_index[i] (lets callers store the tables in a                */
+/* locality-friendly order).  out is written, not accumulated.             */
+/* ---------------------------------------------------------------------- */
+int pycbf_gb_das_tabbed(const pycbf_gb_rfinfo *rf, const void *rfdata, const float *tautx,
+                        const float *apodtx, const float *taurx, const float *apodrx,
+                        long long np, const int *pixel_index, int interp, float thresh,
+                        int sumtype, float *out, void *workspace, size_t workspace_bytes,
+                        void *stream);
+
+/* The cubic Tabbed delay-and-sum on coefficients already produced by      */
+/* pycbf_gb_spline_coefficients (prefilter once, beamform with several     */
+/* table sets or sum types).  Same arguments as pycbf_gb_das_tabbed with   */
+/* interp = cubic; coef must be 16-byte aligned.                           */
+int pycbf_gb_das_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef,
+                                    const float *tautx, const float *apodtx, const float *taurx,
+                                    const float *apodrx, long long np, const int *pixel_index,
+                                    float thresh, int sumtype, float *out, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Synthetic-point delay-and-sum: delays and masks computed per pixel on   */
+/* the fly.  Replaces das_bmode_synthetic_korder_cubic /                   */
+/* das_bmode_synthetic_multi_interp (pycbf/gpu/__engines__.cu:506-694,     */
+/* launched by gpu/__core_bf_classes__.py:167-243) and their delay         */
+/* functions calc_tautx_apodtx / calc_taurx_apodrx (:382-470).  A tap      */
+/* contributes when both masks are on (|apodtx*apodrx| > 0.01, :564) and   */
+/* the delay is in range.                                                  */
+/* ---------------------------------------------------------------------- */
+int pycbf_gb_das_synthetic(const pycbf_gb_rfinfo *rf, const void *rfdata,
+                           const pycbf_gb_synthetic *geo, const int *pixel_index, int interp,
+                           int sumtype, float *out, void *workspace, size_t workspace_bytes,
+                           void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Tap census (test and debug aid): per table column, the number of        */
+/* contributing (tx, rx) taps and the sum of their sample indices (knot j  */
+/* for cubic/linear, nearest sample for nearest).  Frame 0 only.           */
+/* count: int32[np], index_sum: int64[np], both overwritten.               */
+/* ---------------------------------------------------------------------- */
+int pycbf_gb_tap_census_tabbed(const pycbf_gb_rfinfo *rf, const float *tautx,
+                               const float *apodtx, const float *taurx, const float *apodrx,
+                               long long np, int interp, float thresh, int *count,
+                               long long *index_sum, void *stream);
+int pycbf_gb_tap_census_synthetic(const pycbf_gb_rfinfo *rf, const pycbf_gb_synthetic *geo,
+                                  int interp, int *count, long long *index_sum, void *stream);
+
+/* Receive masks of a synthetic geometry, the apodrx of calc_taurx_apodrx  */
+/* (pycbf/gpu/__engines__.cu:444-470): mask (nrx, np) uint8, 1 = accepted. */
+/* Used to select SLSC elements for Synthetic beamformers.                 */
+int pycbf_gb_synthetic_rx_mask(const pycbf_gb_rfinfo *rf, const pycbf_gb_synthetic *geo,
+                               unsigned char *mask, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* DMAS over separated images.  Replaces calc_dmas                         */
+/* (pycbf/gpu/__advanced_engines__.cu:17-61, launched by                   */
+/* gpu/__advanced_bf_classes__.py:30-67).  imsep: (nframes, nsep, np);     */
+/* lags: device int32[nlag], the lag values (the reference kernel uses the */
+/* lag's position 0..nlag-1 instead; both agree when lags = 0..nlag-1).    */
+/* dmastype 0 = signed square root, 1 = power.  out: (nframes, np) if      */
+/* sumlags else (nframes, nlag, np); written, not accumulated.             */
+/* ---------------------------------------------------------------------- */
+int pycbf_gb_dmas(const float *imsep, long long nframes, long long nsep, long long np,
+                  const int *lags, int nlag, int dmastype, int sumlags, float *out,
+                  void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Short-lag spatial coherence.  The reference has it only as notebook     */
+/* NumPy (examples/advanced_beamforming.ipynb, calc_lagn_coherence in      */
+/* cell 2, pixel loop in cell 6).  im: (nframes, nrx, nx, nz) tx-summed    */
+/* per-element images (z fastest); mask: (nrx, nx, nz) uint8 receive mask. */
+/* For pixel (ix, iz) the axial kernel is rows [iz-nkern, iz+nkern]        */
+/* clipped to the grid; elements whose mask is on for all of it are kept;  */
+/* fewer than nlag+1 kept gives 0; otherwise the mean over lags 1..nlag of */
+/* the nan-mean over kept element pairs of the normalised axial            */
+/* correlation (NaN when a lag has no pair with both deviations >= 1e-10). */
+/* out: (nframes, nx, nz) float32, written.                                */
+/* ---------------------------------------------------------------------- */
+int pycbf_gb_slsc(const float *im, const unsigned char *mask, long long nframes, int nrx, int nx,
+                  int nz, int nlag, int nkern, float *out, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Measurement utility (no counterpart in the reference): blocks x 256    */
+/* threads each run iters rounds of 8 independent float32 FMAs and store  */
+/* one float to out[blocks*256].  FLOPs = blocks*256*iters*16.  Gives the */
+/* FP32 peak that the benchmark's FP32 roofline fraction divides by.      */
+/* ---------------------------------------------------------------------- */
+int pycbf_gb_fp32_probe(float *out, int blocks, int iters, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYCBF_GB300_H */

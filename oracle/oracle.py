@@ -1,0 +1,345 @@
+"""CPU oracle for the pycbf beamforming hot path -- TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module, and only as the checker (or as the timed CPU
+baseline).  The product package ``pycbf_gb300`` never imports it.
+
+Three layers:
+
+* ``liboracle.so`` built from ``oracle/pycbf_oracle.c`` -- a float32
+  restatement of the reference's C path (pycbf/cpu/pycbf.c) and of the
+  formulas of its CUDA kernels and notebooks (see the C file's header).
+* ``oracle/_ref/libpycbf_ref.so`` -- the reference's own ``pycbf.c`` compiled
+  from its sources by ``oracle/Makefile`` (only where the reference checkout
+  exists).  Used to pin the restatement and, when present, as the CPU baseline.
+* float64 NumPy/SciPy restatements (``*_fp64``) -- the accuracy yardstick.
+
+Pinning: tests/test_oracle.py checks the restatement against the golden
+vectors in tests/golden/ (generated by importing the reference's own Python
+package, tests/golden/make_golden.py) and against the compiled reference.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+import subprocess
+import threading
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_REF = None
+_LOCK = threading.Lock()
+
+INTERP_CODES = {"cubic": 0, "nearest": 1, "linear": 2, "linear_floor": 3}
+SUMTYPE_CODES = {"none": 0, "tx_only": 1, "rx_only": 2, "tx_and_rx": 3}
+
+_f = ct.c_float
+_i = ct.c_int
+_ll = ct.c_longlong
+_p = ct.c_void_p
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so with oracle/Makefile; returns its path."""
+    path = os.path.join(HERE, "_build", "liboracle.so")
+    src = os.path.join(HERE, "pycbf_oracle.c")
+    if force or not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return path
+
+
+def build_ref(ref_root: str = "/root/reference") -> str | None:
+    """Compile the reference's own pycbf.c into oracle/_ref when its checkout exists."""
+    src = os.path.join(ref_root, "pycbf", "cpu", "pycbf.c")
+    if not os.path.exists(src):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
+    return os.path.join(HERE, "_ref", "libpycbf_ref.so")
+
+
+def lib() -> ct.CDLL:
+    global _LIB
+    with _LOCK:
+        if _LIB is None:
+            L = ct.CDLL(build())
+            L.orc_spline_y2.argtypes = [_p, _i, _f, _p, _p]
+            L.orc_cubic_point.argtypes = [_f, _p, _p, _i, _f, _f, _f]
+            L.orc_cubic_point.restype = _f
+            L.orc_xmax.argtypes = [_f, _f, _i]
+            L.orc_xmax.restype = _f
+            chan = [_f, _f, _i, _p, _i, _f, _p, _p, _p, _p, _p]
+            L.orc_beamform_cubic.argtypes = chan
+            L.orc_beamform_nearest.argtypes = chan + [_i]
+            L.orc_beamform_linear.argtypes = chan + [_i]
+            L.orc_das_tabbed.argtypes = [_i, _i, _f, _f, _i, _p, _i, _i, _ll, _f,
+                                         _p, _p, _p, _p, _i, _p, _i, _i]
+            L.orc_tap_census.argtypes = [_i, _i, _f, _f, _i, _i, _i, _ll, _f,
+                                         _p, _p, _p, _p, _p, _p]
+            L.orc_synth_tx.argtypes = [_i, _p, _p, _f, _f, _f, _f, _f, _f, _f, _p, _p, _p]
+            L.orc_synth_rx.argtypes = [_i, _p, _p, _f, _f, _p, _p, _p]
+            L.orc_synth_tables.argtypes = [_i, _ll, _p, _f, _i, _p, _p, _p, _p, _p, _p, _p, _p,
+                                           _i, _p, _p, _p, _p, _p, _p, _p]
+            L.orc_dmas.argtypes = [_p, _ll, _ll, _p, _i, _i, _i, _p]
+            L.orc_slsc.argtypes = [_p, _p, _i, _i, _i, _i, _i, _p]
+            _LIB = L
+        return _LIB
+
+
+def ref_lib() -> ct.CDLL | None:
+    """The reference's compiled pycbf.c, or None where it was not built."""
+    global _REF
+    with _LOCK:
+        if _REF is None:
+            path = os.path.join(HERE, "_ref", "libpycbf_ref.so")
+            if not os.path.exists(path):
+                return None
+            try:
+                R = ct.CDLL(path)
+            except OSError:  # e.g. a binary built for another machine
+                return None
+            chan = [_f, _f, _i, _p, _i, _f, _p, _p, _p, _p, _p]
+            R.beamform_cubic.argtypes = chan
+            R.beamform_cubic.restype = None
+            R.beamform_nearest.argtypes = chan + [_i]
+            R.beamform_nearest.restype = None
+            _REF = R
+        return _REF
+
+
+def _c32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_p)
+
+
+def out_size(sumtype: str, ntx: int, nrx: int, np_: int) -> int:
+    return {"none": ntx * nrx * np_, "tx_only": nrx * np_, "rx_only": ntx * np_,
+            "tx_and_rx": np_}[sumtype]
+
+
+# ---------------------------------------------------------------------------
+# Tabbed DAS, float32, the reference's loop order
+# ---------------------------------------------------------------------------
+def das_tabbed(rf, tautx, apodtx, taurx, apodrx, t0, dt, nt, interp="cubic", usf=1,
+               thresh=1e-2, sumtype="tx_and_rx", threads=1, use_ref=False):
+    """Float32 image of a Tabbed beamformer.
+
+    With threads == 1 the accumulation order is the reference's
+    (pycbf/cpu/__core_bf_classes__.py:240-245, tx-major, rx-minor, in place).
+    With threads > 1 the transmits are split across threads, each with a
+    private buffer, summed at the end (the same taps, another rounding order).
+    use_ref=True calls the reference's own compiled beamform_cubic /
+    beamform_nearest per channel instead of the restatement.
+    """
+    rf = _c32(rf)
+    tautx, apodtx, taurx, apodrx = map(_c32, (tautx, apodtx, taurx, apodrx))
+    ntx, nrx = tautx.shape[0], taurx.shape[0]
+    np_ = tautx.shape[1]
+    assert rf.shape == (ntx, nrx, nt)
+    size = out_size(sumtype, ntx, nrx, np_)
+    if use_ref:
+        return _das_tabbed_ref(rf, tautx, apodtx, taurx, apodrx, t0, dt, nt, interp, usf,
+                               thresh, sumtype, size)
+    L = lib()
+    code = INTERP_CODES[interp]
+    st = SUMTYPE_CODES[sumtype]
+
+    def run(tx0, tx1):
+        out = np.zeros(size, dtype=np.float32)
+        L.orc_das_tabbed(code, int(usf), float(t0), float(dt), int(nt), _ptr(rf), ntx, nrx, np_,
+                         float(thresh), _ptr(tautx), _ptr(apodtx), _ptr(taurx), _ptr(apodrx),
+                         st, _ptr(out), tx0, tx1)
+        return out
+
+    if threads <= 1 or ntx == 1:
+        return run(0, ntx)
+    if sumtype in ("none", "rx_only"):
+        # outputs are disjoint per transmit: one shared buffer, no reduction
+        out = np.zeros(size, dtype=np.float32)
+
+        def run_into(tx0, tx1):
+            L.orc_das_tabbed(code, int(usf), float(t0), float(dt), int(nt), _ptr(rf), ntx, nrx,
+                             np_, float(thresh), _ptr(tautx), _ptr(apodtx), _ptr(taurx),
+                             _ptr(apodrx), st, _ptr(out), tx0, tx1)
+
+        with ThreadPoolExecutor(threads) as ex:
+            list(ex.map(lambda t: run_into(t, t + 1), range(ntx)))
+        return out
+    with ThreadPoolExecutor(min(threads, ntx)) as ex:
+        parts = list(ex.map(lambda t: run(t, t + 1), range(ntx)))
+    return np.sum(parts, axis=0, dtype=np.float32)
+
+
+def _das_tabbed_ref(rf, tautx, apodtx, taurx, apodrx, t0, dt, nt, interp, usf, thresh,
+                    sumtype, size):
+    R = ref_lib()
+    if R is None:
+        raise RuntimeError("the reference C library was not built (oracle/Makefile ref)")
+    ntx, nrx, np_ = tautx.shape[0], taurx.shape[0], tautx.shape[1]
+    out = np.zeros(size, dtype=np.float32)
+    for itx in range(ntx):
+        for irx in range(nrx):
+            if sumtype == "none":
+                off = np_ * (irx + itx * nrx)
+            elif sumtype == "tx_only":
+                off = np_ * irx
+            elif sumtype == "rx_only":
+                off = np_ * itx
+            else:
+                off = 0
+            args = [_f(t0), _f(dt), _i(nt), _ptr(rf[itx, irx]), _i(np_), _f(thresh),
+                    _ptr(tautx[itx]), _ptr(apodtx[itx]), _ptr(taurx[irx]), _ptr(apodrx[irx]),
+                    ct.c_void_p(out.ctypes.data + 4 * off)]
+            if interp == "cubic":
+                R.beamform_cubic(*args)
+            elif interp == "nearest":
+                R.beamform_nearest(*args, _i(usf))
+            else:
+                raise ValueError("the reference C path has cubic and nearest only")
+    return out
+
+
+def tap_census(tautx, apodtx, taurx, apodrx, t0, dt, nt, interp="cubic", usf=1, thresh=1e-2):
+    """Per pixel: (number of contributing taps, sum of their sample indices)."""
+    tautx, apodtx, taurx, apodrx = map(_c32, (tautx, apodtx, taurx, apodrx))
+    ntx, nrx, np_ = tautx.shape[0], taurx.shape[0], tautx.shape[1]
+    count = np.zeros(np_, dtype=np.int32)
+    isum = np.zeros(np_, dtype=np.int64)
+    code = 1 if interp == "nearest" else 0
+    lib().orc_tap_census(code, int(usf), float(t0), float(dt), int(nt), ntx, nrx, np_,
+                         float(thresh), _ptr(tautx), _ptr(apodtx), _ptr(taurx), _ptr(apodrx),
+                         _ptr(count), _ptr(isum))
+    return count, isum
+
+
+def spline_y2(y, dt):
+    y = _c32(y)
+    n = y.shape[-1]
+    y2 = np.empty(n, np.float32)
+    u = np.empty(n, np.float32)
+    lib().orc_spline_y2(_ptr(y), n, float(dt), _ptr(y2), _ptr(u))
+    return y2
+
+
+# ---------------------------------------------------------------------------
+# synthetic-point geometry -> float32 tables (restated delay/mask formulas)
+# ---------------------------------------------------------------------------
+def synth_constants(alatx, doftx, alarx):
+    """Per-element constants shared by the product and the oracle (float32)."""
+    alatx = np.asarray(alatx, np.float32).astype(np.float64)
+    doftx = np.asarray(doftx, np.float32).astype(np.float64)
+    alarx = np.asarray(alarx, np.float32).astype(np.float64)
+    cos_tx = np.cos(alatx).astype(np.float32)
+    sec_tx = np.sqrt(1.0 + np.tan(alatx) ** 2).astype(np.float32)
+    hds_tx = (doftx * np.sin(alatx) / 2.0).astype(np.float32)
+    cos_rx = np.cos(alarx).astype(np.float32)
+    return cos_tx, sec_tx, hds_tx, cos_rx
+
+
+def synth_tables(ovectx, nvectx, doftx, alatx, t0tx, ovecrx, nvecrx, alarx, c0, pnts):
+    pnts = _c32(pnts)
+    ndim = pnts.shape[1]
+    np_ = pnts.shape[0]
+    ovectx, nvectx, ovecrx, nvecrx = map(_c32, (ovectx, nvectx, ovecrx, nvecrx))
+    t0tx, alatx, doftx = map(_c32, (t0tx, alatx, doftx))
+    cos_tx, sec_tx, hds_tx, cos_rx = synth_constants(alatx, doftx, alarx)
+    ntx, nrx = ovectx.shape[0], ovecrx.shape[0]
+    tautx = np.empty((ntx, np_), np.float32)
+    apodtx = np.empty((ntx, np_), np.float32)
+    taurx = np.empty((nrx, np_), np.float32)
+    apodrx = np.empty((nrx, np_), np.float32)
+    lib().orc_synth_tables(ndim, np_, _ptr(pnts), float(np.float32(c0)), ntx, _ptr(ovectx),
+                           _ptr(nvectx), _ptr(t0tx), _ptr(alatx), _ptr(cos_tx), _ptr(sec_tx),
+                           _ptr(hds_tx), _ptr(doftx), nrx, _ptr(ovecrx), _ptr(nvecrx),
+                           _ptr(cos_rx), _ptr(tautx), _ptr(apodtx), _ptr(taurx), _ptr(apodrx))
+    return tautx, apodtx, taurx, apodrx
+
+
+# ---------------------------------------------------------------------------
+# DMAS and SLSC
+# ---------------------------------------------------------------------------
+def dmas(im, lags, power=False, sumlags=True):
+    im = _c32(im)
+    nsep, np_ = im.shape
+    lags = np.ascontiguousarray(lags, dtype=np.int32)
+    out = np.zeros(np_ if sumlags else len(lags) * np_, np.float32)
+    lib().orc_dmas(_ptr(im), nsep, np_, _ptr(lags), len(lags), int(power), int(sumlags),
+                   _ptr(out))
+    return out if sumlags else out.reshape(len(lags), np_)
+
+
+def slsc(im, mask, nlag, nkern):
+    """im, mask: (nrx, nx, nz).  Returns (nx, nz) float64."""
+    im = _c32(im)
+    nrx, nx, nz = im.shape
+    m = np.ascontiguousarray(np.asarray(mask) != 0, dtype=np.uint8)
+    out = np.zeros((nx, nz), np.float64)
+    lib().orc_slsc(_ptr(im), _ptr(m), nrx, nx, nz, int(nlag), int(nkern), _ptr(out))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# float64 yardsticks
+# ---------------------------------------------------------------------------
+def das_tabbed_fp64(rf, tautx, apodtx, taurx, apodrx, t0, dt, nt, interp="cubic",
+                    thresh=1e-2, sumtype="tx_and_rx", mask32=True):
+    """Float64 DAS: SciPy natural cubic spline (or nearest) evaluated in double.
+
+    The set of contributing taps is decided exactly as in float32 (mask32=True)
+    so that the float64 image differs from the float32 one by arithmetic only.
+    """
+    from scipy.interpolate import CubicSpline
+
+    rf = np.asarray(rf, np.float64)
+    ntx, nrx, np_ = tautx.shape[0], taurx.shape[0], tautx.shape[1]
+    t = t0 + dt * np.arange(nt, dtype=np.float64)
+    t32 = np.float32(t0)
+    xmax32 = lib().orc_xmax(float(t0), float(dt), int(nt))
+    out = np.zeros(out_size(sumtype, ntx, nrx, np_), np.float64)
+    ttx32, atx32, trx32, arx32 = map(_c32, (tautx, apodtx, taurx, apodrx))
+    for itx in range(ntx):
+        for irx in range(nrx):
+            apod32 = atx32[itx] * arx32[irx]
+            x32 = ttx32[itx] + trx32[irx]
+            if interp == "cubic":
+                ok = (np.abs(apod32) >= np.float32(thresh)) & (x32 >= t32) & (x32 <= xmax32)
+                cs = CubicSpline(t, rf[itx, irx], bc_type="natural")
+                x = np.asarray(tautx[itx], np.float64) + np.asarray(taurx[irx], np.float64)
+                v = np.where(ok, cs(np.clip(x, t[0], t[-1])), 0.0)
+            elif interp == "nearest":
+                q = ((x32 - t32) / np.float32(dt)).astype(np.float64) + 0.5
+                it = np.where((q > -2**31) & (q < 2**31 - 1), q, -1).astype(np.int64)
+                ok = (np.abs(apod32) >= np.float32(thresh)) & (it >= 0) & (it < nt)
+                v = np.where(ok, rf[itx, irx][np.clip(it, 0, nt - 1)], 0.0)
+            else:
+                raise ValueError(interp)
+            apod = np.asarray(apodtx[itx], np.float64) * np.asarray(apodrx[irx], np.float64)
+            contrib = np.where(ok, apod * v, 0.0)
+            if sumtype == "none":
+                out[np_ * (irx + itx * nrx):np_ * (irx + itx * nrx + 1)] += contrib
+            elif sumtype == "tx_only":
+                out[np_ * irx:np_ * (irx + 1)] += contrib
+            elif sumtype == "rx_only":
+                out[np_ * itx:np_ * (itx + 1)] += contrib
+            else:
+                out += contrib
+    return out
+
+
+def rel_l2(a, b) -> float:
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    den = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / den) if den > 0 else float(np.linalg.norm(a - b))
+
+
+def max_abs_rel_peak(a, b) -> float:
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    peak = np.max(np.abs(b))
+    return float(np.max(np.abs(a - b)) / peak) if peak > 0 else float(np.max(np.abs(a - b)))

@@ -1,0 +1,101 @@
+"""ctypes binding of libpycbf_gb300.so (the C ABI of include/pycbf_gb300.h).
+
+The library is loaded from this package's directory.  There is no fallback:
+if it is missing or fails to load, every beamformer call raises.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpycbf_gb300.so")
+
+# status codes
+OK, EINVAL, ERANGE, EWORKSPACE, EUNSUPPORTED, ECUDA = range(6)
+# storage types
+F32, F16, BF16 = 0, 1, 2
+# interpolation kinds
+INTERP = {"nearest": 0, "linear": 1, "cubic": 2, "linear_floor": 3}
+# sum types (0..3 are the reference's flag values)
+SUMTYPE = {"none": 0, "tx_only": 1, "rx_only": 2, "tx_and_rx": 3, "dmas_ssr": 4, "dmas_power": 5}
+
+EXPORTS = (
+    "pycbf_gb_abi_version", "pycbf_gb_status_string", "pycbf_gb_last_cuda_error",
+    "pycbf_gb_workspace_bytes", "pycbf_gb_spline_coefficients", "pycbf_gb_das_tabbed",
+    "pycbf_gb_das_tabbed_prefiltered",
+    "pycbf_gb_das_synthetic", "pycbf_gb_tap_census_tabbed", "pycbf_gb_tap_census_synthetic",
+    "pycbf_gb_synthetic_rx_mask", "pycbf_gb_dmas", "pycbf_gb_slsc", "pycbf_gb_fp32_probe",
+)
+
+
+class RFInfo(ct.Structure):
+    """pycbf_gb_rfinfo: mirrors RFInfo of pycbf/gpu/__engines__.cu:369-374."""
+    _fields_ = [("ntx", ct.c_longlong), ("nrx", ct.c_longlong), ("ndim", ct.c_int),
+                ("t0", ct.c_float), ("dt", ct.c_float), ("nt", ct.c_int),
+                ("nframes", ct.c_longlong), ("dtype", ct.c_int)]
+
+
+class SyntheticGeom(ct.Structure):
+    """pycbf_gb_synthetic: device pointers of the synthetic-point geometry."""
+    _fields_ = [(n, ct.c_void_p) for n in (
+        "ovectx", "nvectx", "t0tx", "alatx", "doftx", "cosalatx", "secalatx", "halfdofsintx",
+        "ovecrx", "nvecrx", "cosalarx", "pnts")] + [("np", ct.c_longlong), ("c0", ct.c_float)]
+
+
+class GPUError(RuntimeError):
+    pass
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load() -> ct.CDLL:
+    """Load the library (building it first when it is absent and nvcc exists)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            from . import build
+            build.build()
+        L = ct.CDLL(LIB_PATH)
+        vp, ll, i, f, sz = ct.c_void_p, ct.c_longlong, ct.c_int, ct.c_float, ct.c_size_t
+        P = ct.POINTER
+        L.pycbf_gb_abi_version.restype = i
+        L.pycbf_gb_status_string.argtypes = [i]
+        L.pycbf_gb_status_string.restype = ct.c_char_p
+        L.pycbf_gb_last_cuda_error.restype = i
+        L.pycbf_gb_workspace_bytes.argtypes = [P(RFInfo), i]
+        L.pycbf_gb_workspace_bytes.restype = sz
+        L.pycbf_gb_spline_coefficients.argtypes = [P(RFInfo), vp, vp, sz, vp]
+        L.pycbf_gb_das_tabbed.argtypes = [P(RFInfo), vp, vp, vp, vp, vp, ll, vp, i, f, i, vp, vp,
+                                          sz, vp]
+        L.pycbf_gb_das_tabbed_prefiltered.argtypes = [P(RFInfo), vp, vp, vp, vp, vp, ll, vp, f, i,
+                                                      vp, vp]
+        L.pycbf_gb_das_synthetic.argtypes = [P(RFInfo), vp, P(SyntheticGeom), vp, i, i, vp, vp,
+                                             sz, vp]
+        L.pycbf_gb_tap_census_tabbed.argtypes = [P(RFInfo), vp, vp, vp, vp, ll, i, f, vp, vp, vp]
+        L.pycbf_gb_tap_census_synthetic.argtypes = [P(RFInfo), P(SyntheticGeom), i, vp, vp, vp]
+        L.pycbf_gb_synthetic_rx_mask.argtypes = [P(RFInfo), P(SyntheticGeom), vp, vp]
+        L.pycbf_gb_dmas.argtypes = [vp, ll, ll, ll, vp, i, i, i, vp, vp]
+        L.pycbf_gb_slsc.argtypes = [vp, vp, ll, i, i, i, i, i, vp, vp]
+        L.pycbf_gb_fp32_probe.argtypes = [vp, i, i, vp]
+        for name in EXPORTS:
+            if name not in ("pycbf_gb_abi_version", "pycbf_gb_status_string",
+                            "pycbf_gb_last_cuda_error", "pycbf_gb_workspace_bytes"):
+                getattr(L, name).restype = i
+        _lib = L
+        return L
+
+
+def check(status: int, what: str) -> None:
+    if status == OK:
+        return
+    L = load()
+    msg = L.pycbf_gb_status_string(status).decode()
+    if status == ECUDA:
+        msg += f" (cudaError {L.pycbf_gb_last_cuda_error()})"
+    raise GPUError(f"{what}: {msg}")

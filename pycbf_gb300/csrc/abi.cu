@@ -1,0 +1,301 @@
+// The C ABI (include/pycbf_gb300.h): host-side validation, then stream-ordered
+// launches.  No allocation, no synchronisation, no mutable shared state.
+#include <cmath>
+#include <cstdint>
+#include <limits>
+
+#include "common.cuh"
+
+using namespace pgb;
+
+namespace {
+
+thread_local int g_last_cuda_error = 0;
+
+int cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return PYCBF_GB_OK;
+    g_last_cuda_error = (int)e;
+    return PYCBF_GB_ECUDA;
+}
+
+size_t dtype_bytes(int dtype) {
+    switch (dtype) {
+        case PYCBF_GB_F32: return 4;
+        case PYCBF_GB_F16:
+        case PYCBF_GB_BF16: return 2;
+        default: return 0;
+    }
+}
+
+// Largest sample count the nearest-neighbour rounding handles exactly in float.
+constexpr int kMaxNt = 1 << 22;
+constexpr int kMaxNtSpline = 18000;  // three shared-memory copies of a channel per warp
+
+int check_rf(const pycbf_gb_rfinfo *rf, bool synthetic) {
+    if (!rf) return PYCBF_GB_EINVAL;
+    if (rf->ntx <= 0 || rf->nrx <= 0 || rf->nt <= 0 || rf->nframes <= 0) return PYCBF_GB_EINVAL;
+    if (!dtype_bytes(rf->dtype)) return PYCBF_GB_EINVAL;
+    if (!std::isfinite(rf->t0) || !std::isfinite(rf->dt) || !(rf->dt > 0.f)) return PYCBF_GB_EINVAL;
+    if (synthetic && rf->ndim != 2 && rf->ndim != 3) return PYCBF_GB_EINVAL;
+    if (rf->ntx > (1 << 20) || rf->nrx > (1 << 20) || rf->nt >= kMaxNt || rf->nframes > 65535)
+        return PYCBF_GB_ERANGE;
+    return PYCBF_GB_OK;
+}
+
+// 4 ulp of the largest quotient magnitude that can still be in range: the
+// fast reciprocal quotient is within 1.5 ulp of the correctly rounded one.
+float boundary_eps(int nt) {
+    int k = 0;
+    while ((1LL << k) < (long long)nt + 2) ++k;
+    return std::ldexp(1.0f, k - 22);
+}
+
+void fill_time_axis(DasArgs &a, const pycbf_gb_rfinfo *rf) {
+    a.ntx = (int)rf->ntx;
+    a.nrx = (int)rf->nrx;
+    a.nt = rf->nt;
+    a.nframes = (int)rf->nframes;
+    a.t0 = rf->t0;
+    a.dt = rf->dt;
+    a.inv_dt = 1.0f / rf->dt;
+    // xmax = t0 + dt*(nt-1), two roundings as in pycbf.c:77
+    volatile float span = rf->dt * (float)(rf->nt - 1);
+    a.xmax = rf->t0 + span;
+    // x0 + dx*nx of the reference linear_interp (__engines__.cu:47), two roundings
+    volatile float span2 = rf->dt * (float)rf->nt;
+    a.xend = rf->t0 + span2;
+    a.eps = boundary_eps(rf->nt);
+}
+
+bool das_shape_ok(int geom, int sumtype, long long ntx) {
+    if (ntx <= 16) return true;
+    const size_t per = (geom == GEOM_TABBED ? 2 : 1) + (sumtype == PYCBF_GB_SUM_RX_ONLY ? 1 : 0);
+    return per * (size_t)ntx * 128 * sizeof(float) <= 227 * 1024;
+}
+
+int prepare_data(const pycbf_gb_rfinfo *rf, const void *rfdata, int interp, void *workspace,
+                 size_t workspace_bytes, cudaStream_t s, const void **data) {
+    if (interp != PYCBF_GB_INTERP_CUBIC) {
+        *data = rfdata;
+        return PYCBF_GB_OK;
+    }
+    const size_t need = pycbf_gb_workspace_bytes(rf, interp);
+    if (!workspace || workspace_bytes < need) return PYCBF_GB_EWORKSPACE;
+    if (reinterpret_cast<uintptr_t>(workspace) % 16) return PYCBF_GB_EINVAL;
+    if (rf->nt > kMaxNtSpline) return PYCBF_GB_ERANGE;
+    SplineArgs sa;
+    sa.rf = rfdata;
+    sa.coef = workspace;
+    sa.nch = rf->nframes * rf->ntx * rf->nrx;
+    sa.nt = rf->nt;
+    sa.dt = rf->dt;
+    int st = cuda_status(launch_spline(sa, rf->dtype, s));
+    if (st) return st;
+    *data = workspace;
+    return PYCBF_GB_OK;
+}
+
+bool geo_ok(const pycbf_gb_synthetic *g) {
+    return g && g->ovectx && g->nvectx && g->t0tx && g->alatx && g->doftx && g->cosalatx &&
+           g->secalatx && g->halfdofsintx && g->ovecrx && g->nvecrx && g->cosalarx && g->pnts &&
+           g->np > 0 && g->np < (1LL << 31) && std::isfinite(g->c0) && g->c0 != 0.f;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pycbf_gb_abi_version(void) { return PYCBF_GB_ABI_VERSION; }
+
+const char *pycbf_gb_status_string(int status) {
+    switch (status) {
+        case PYCBF_GB_OK: return "ok";
+        case PYCBF_GB_EINVAL: return "invalid argument";
+        case PYCBF_GB_ERANGE: return "size out of supported range";
+        case PYCBF_GB_EWORKSPACE: return "workspace missing, misaligned or too small";
+        case PYCBF_GB_EUNSUPPORTED: return "unsupported combination";
+        case PYCBF_GB_ECUDA: return "CUDA error";
+        default: return "unknown status";
+    }
+}
+
+int pycbf_gb_last_cuda_error(void) { return g_last_cuda_error; }
+
+size_t pycbf_gb_workspace_bytes(const pycbf_gb_rfinfo *rf, int interp) {
+    if (!rf || interp != PYCBF_GB_INTERP_CUBIC) return 0;
+    if (rf->ntx <= 0 || rf->nrx <= 0 || rf->nt <= 0 || rf->nframes <= 0) return 0;
+    const size_t rec = rf->dtype == PYCBF_GB_F32 ? 16 : 8;
+    return (size_t)rf->nframes * (size_t)rf->ntx * (size_t)rf->nrx * (size_t)rf->nt * rec;
+}
+
+int pycbf_gb_spline_coefficients(const pycbf_gb_rfinfo *rf, const void *rfdata, void *coef,
+                                 size_t coef_bytes, void *stream) {
+    int st = check_rf(rf, false);
+    if (st) return st;
+    if (!rfdata) return PYCBF_GB_EINVAL;
+    const void *data = nullptr;
+    return prepare_data(rf, rfdata, PYCBF_GB_INTERP_CUBIC, coef, coef_bytes,
+                        static_cast<cudaStream_t>(stream), &data);
+}
+
+int pycbf_gb_das_tabbed(const pycbf_gb_rfinfo *rf, const void *rfdata, const float *tautx,
+                        const float *apodtx, const float *taurx, const float *apodrx,
+                        long long np, const int *pixel_index, int interp, float thresh,
+                        int sumtype, float *out, void *workspace, size_t workspace_bytes,
+                        void *stream) {
+    int st = check_rf(rf, false);
+    if (st) return st;
+    if (!rfdata || !tautx || !apodtx || !taurx || !apodrx || !out) return PYCBF_GB_EINVAL;
+    if (np <= 0 || np >= (1LL << 31)) return np == 0 ? PYCBF_GB_OK : PYCBF_GB_ERANGE;
+    if (interp < 0 || interp > 3 || sumtype < 0 || sumtype > 5) return PYCBF_GB_EINVAL;
+    if (std::isnan(thresh)) return PYCBF_GB_EINVAL;
+    if (!das_shape_ok(GEOM_TABBED, sumtype, rf->ntx)) return PYCBF_GB_ERANGE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const void *data = nullptr;
+    st = prepare_data(rf, rfdata, interp, workspace, workspace_bytes, s, &data);
+    if (st) return st;
+    DasArgs a = {};
+    fill_time_axis(a, rf);
+    a.data = data;
+    a.tautx = tautx;
+    a.apodtx = apodtx;
+    a.taurx = taurx;
+    a.apodrx = apodrx;
+    a.pixel_index = pixel_index;
+    a.out = out;
+    a.np = np;
+    a.thresh = thresh;
+    return cuda_status(launch_das(a, GEOM_TABBED, interp, sumtype, rf->dtype, false, s));
+}
+
+int pycbf_gb_das_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef,
+                                    const float *tautx, const float *apodtx, const float *taurx,
+                                    const float *apodrx, long long np, const int *pixel_index,
+                                    float thresh, int sumtype, float *out, void *stream) {
+    int st = check_rf(rf, false);
+    if (st) return st;
+    if (!coef || !tautx || !apodtx || !taurx || !apodrx || !out) return PYCBF_GB_EINVAL;
+    if (reinterpret_cast<uintptr_t>(coef) % 16) return PYCBF_GB_EINVAL;
+    if (np <= 0 || np >= (1LL << 31)) return np == 0 ? PYCBF_GB_OK : PYCBF_GB_ERANGE;
+    if (sumtype < 0 || sumtype > 5 || std::isnan(thresh)) return PYCBF_GB_EINVAL;
+    if (!das_shape_ok(GEOM_TABBED, sumtype, rf->ntx)) return PYCBF_GB_ERANGE;
+    DasArgs a = {};
+    fill_time_axis(a, rf);
+    a.data = coef;
+    a.tautx = tautx;
+    a.apodtx = apodtx;
+    a.taurx = taurx;
+    a.apodrx = apodrx;
+    a.pixel_index = pixel_index;
+    a.out = out;
+    a.np = np;
+    a.thresh = thresh;
+    return cuda_status(launch_das(a, GEOM_TABBED, PYCBF_GB_INTERP_CUBIC, sumtype, rf->dtype, false,
+                                  static_cast<cudaStream_t>(stream)));
+}
+
+int pycbf_gb_das_synthetic(const pycbf_gb_rfinfo *rf, const void *rfdata,
+                           const pycbf_gb_synthetic *geo, const int *pixel_index, int interp,
+                           int sumtype, float *out, void *workspace, size_t workspace_bytes,
+                           void *stream) {
+    int st = check_rf(rf, true);
+    if (st) return st;
+    if (!rfdata || !out || !geo_ok(geo)) return PYCBF_GB_EINVAL;
+    if (interp < 0 || interp > 3 || sumtype < 0 || sumtype > 5) return PYCBF_GB_EINVAL;
+    if (!das_shape_ok(GEOM_SYNTH, sumtype, rf->ntx)) return PYCBF_GB_ERANGE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const void *data = nullptr;
+    st = prepare_data(rf, rfdata, interp, workspace, workspace_bytes, s, &data);
+    if (st) return st;
+    DasArgs a = {};
+    fill_time_axis(a, rf);
+    a.data = data;
+    a.geo = *geo;
+    a.ndim = rf->ndim;
+    a.pixel_index = pixel_index;
+    a.out = out;
+    a.np = geo->np;
+    a.thresh = 0.01f;
+    return cuda_status(launch_das(a, GEOM_SYNTH, interp, sumtype, rf->dtype, false, s));
+}
+
+int pycbf_gb_tap_census_tabbed(const pycbf_gb_rfinfo *rf, const float *tautx,
+                               const float *apodtx, const float *taurx, const float *apodrx,
+                               long long np, int interp, float thresh, int *count,
+                               long long *index_sum, void *stream) {
+    int st = check_rf(rf, false);
+    if (st) return st;
+    if (!tautx || !apodtx || !taurx || !apodrx || !count || !index_sum) return PYCBF_GB_EINVAL;
+    if (np <= 0 || np >= (1LL << 31)) return np == 0 ? PYCBF_GB_OK : PYCBF_GB_ERANGE;
+    if (interp < 0 || interp > 3 || std::isnan(thresh)) return PYCBF_GB_EINVAL;
+    if (!das_shape_ok(GEOM_TABBED, PYCBF_GB_SUM_TX_AND_RX, rf->ntx)) return PYCBF_GB_ERANGE;
+    DasArgs a = {};
+    fill_time_axis(a, rf);
+    a.nframes = 1;
+    a.tautx = tautx;
+    a.apodtx = apodtx;
+    a.taurx = taurx;
+    a.apodrx = apodrx;
+    a.np = np;
+    a.thresh = thresh;
+    a.census_count = count;
+    a.census_isum = index_sum;
+    return cuda_status(launch_das(a, GEOM_TABBED, interp, PYCBF_GB_SUM_TX_AND_RX, PYCBF_GB_F32,
+                                  true, static_cast<cudaStream_t>(stream)));
+}
+
+int pycbf_gb_tap_census_synthetic(const pycbf_gb_rfinfo *rf, const pycbf_gb_synthetic *geo,
+                                  int interp, int *count, long long *index_sum, void *stream) {
+    int st = check_rf(rf, true);
+    if (st) return st;
+    if (!geo_ok(geo) || !count || !index_sum) return PYCBF_GB_EINVAL;
+    if (interp < 0 || interp > 3) return PYCBF_GB_EINVAL;
+    if (!das_shape_ok(GEOM_SYNTH, PYCBF_GB_SUM_TX_AND_RX, rf->ntx)) return PYCBF_GB_ERANGE;
+    DasArgs a = {};
+    fill_time_axis(a, rf);
+    a.nframes = 1;
+    a.geo = *geo;
+    a.ndim = rf->ndim;
+    a.np = geo->np;
+    a.thresh = 0.01f;
+    a.census_count = count;
+    a.census_isum = index_sum;
+    return cuda_status(launch_das(a, GEOM_SYNTH, interp, PYCBF_GB_SUM_TX_AND_RX, PYCBF_GB_F32,
+                                  true, static_cast<cudaStream_t>(stream)));
+}
+
+int pycbf_gb_synthetic_rx_mask(const pycbf_gb_rfinfo *rf, const pycbf_gb_synthetic *geo,
+                               unsigned char *mask, void *stream) {
+    int st = check_rf(rf, true);
+    if (st) return st;
+    if (!geo_ok(geo) || !mask) return PYCBF_GB_EINVAL;
+    DasArgs a = {};
+    fill_time_axis(a, rf);
+    a.geo = *geo;
+    a.ndim = rf->ndim;
+    a.np = geo->np;
+    return cuda_status(launch_synth_rx_mask(a, mask, static_cast<cudaStream_t>(stream)));
+}
+
+int pycbf_gb_dmas(const float *imsep, long long nframes, long long nsep, long long np,
+                  const int *lags, int nlag, int dmastype, int sumlags, float *out,
+                  void *stream) {
+    if (!imsep || !lags || !out) return PYCBF_GB_EINVAL;
+    if (nframes <= 0 || nsep <= 0 || np <= 0 || nlag <= 0) return PYCBF_GB_EINVAL;
+    if (dmastype != 0 && dmastype != 1) return PYCBF_GB_EINVAL;
+    if (nframes > 65535 || np >= (1LL << 40)) return PYCBF_GB_ERANGE;
+    return cuda_status(launch_dmas(imsep, nframes, nsep, np, lags, nlag, dmastype, sumlags ? 1 : 0,
+                                   out, static_cast<cudaStream_t>(stream)));
+}
+
+int pycbf_gb_slsc(const float *im, const unsigned char *mask, long long nframes, int nrx, int nx,
+                  int nz, int nlag, int nkern, float *out, void *stream) {
+    if (!im || !mask || !out) return PYCBF_GB_EINVAL;
+    if (nframes <= 0 || nrx <= 0 || nx <= 0 || nz <= 0 || nlag <= 0 || nkern < 0)
+        return PYCBF_GB_EINVAL;
+    if (nlag > 32 || 2 * nkern + 1 > 64 || nframes > 65535) return PYCBF_GB_ERANGE;
+    return cuda_status(launch_slsc(im, mask, nframes, nrx, nx, nz, nlag, nkern, out,
+                                   static_cast<cudaStream_t>(stream)));
+}
+
+}  // extern "C"

@@ -1,0 +1,126 @@
+// Shared device helpers and the launch interface between the kernel files and
+// the C ABI (abi.cu).  Internal to libpycbf_gb300.so.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "pycbf_gb300.h"
+
+namespace pgb {
+
+// ---------------------------------------------------------------------------
+// storage types
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float load_sample(const float *p) { return __ldg(p); }
+__device__ __forceinline__ float load_sample(const __half *p) { return __half2float(__ldg(p)); }
+__device__ __forceinline__ float load_sample(const __nv_bfloat16 *p) {
+    return __bfloat162float(__ldg(p));
+}
+
+// A spline coefficient record (y_j, y_j+1, z_j, z_j+1): float4 for float32
+// channel data, four 16-bit values packed in a uint2 otherwise.
+template <typename T> struct CoefRec;
+template <> struct CoefRec<float> {
+    using raw = float4;
+    static __device__ __forceinline__ float4 load(const raw *p) { return __ldg(p); }
+    static __device__ __forceinline__ raw pack(float a, float b, float c, float d) {
+        return make_float4(a, b, c, d);
+    }
+};
+template <> struct CoefRec<__half> {
+    using raw = uint2;
+    static __device__ __forceinline__ float4 load(const raw *p) {
+        uint2 r = __ldg(p);
+        __half2 h0 = *reinterpret_cast<__half2 *>(&r.x);
+        __half2 h1 = *reinterpret_cast<__half2 *>(&r.y);
+        float2 a = __half22float2(h0), b = __half22float2(h1);
+        return make_float4(a.x, a.y, b.x, b.y);
+    }
+    static __device__ __forceinline__ raw pack(float a, float b, float c, float d) {
+        __half2 h0 = __floats2half2_rn(a, b), h1 = __floats2half2_rn(c, d);
+        uint2 r;
+        r.x = *reinterpret_cast<unsigned *>(&h0);
+        r.y = *reinterpret_cast<unsigned *>(&h1);
+        return r;
+    }
+};
+template <> struct CoefRec<__nv_bfloat16> {
+    using raw = uint2;
+    static __device__ __forceinline__ float4 load(const raw *p) {
+        uint2 r = __ldg(p);
+        __nv_bfloat162 h0 = *reinterpret_cast<__nv_bfloat162 *>(&r.x);
+        __nv_bfloat162 h1 = *reinterpret_cast<__nv_bfloat162 *>(&r.y);
+        float2 a = __bfloat1622float2(h0), b = __bfloat1622float2(h1);
+        return make_float4(a.x, a.y, b.x, b.y);
+    }
+    static __device__ __forceinline__ raw pack(float a, float b, float c, float d) {
+        __nv_bfloat162 h0 = __floats2bfloat162_rn(a, b), h1 = __floats2bfloat162_rn(c, d);
+        uint2 r;
+        r.x = *reinterpret_cast<unsigned *>(&h0);
+        r.y = *reinterpret_cast<unsigned *>(&h1);
+        return r;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// spline prefilter
+// ---------------------------------------------------------------------------
+// The forward sweep of the natural-spline tridiagonal solve (pycbf.c:126-133)
+// has data-independent pivots p_i = 0.5*y2f_{i-1} + 2; they converge to
+// 2 - (2 - sqrt 3)/2 within ~10 steps.  The host tabulates 1/p_i and the
+// back-substitution factors c_i = y2f_i = -0.5/p_i for i < kSplineTab; larger
+// i use the last entry.
+constexpr int kSplineTab = 64;
+struct SplineTable {
+    float invp[kSplineTab];
+    float c[kSplineTab];
+};
+void make_spline_table(SplineTable *t);
+
+struct SplineArgs {
+    const void *rf;          // (nch, nt) storage type
+    void *coef;              // (nch, nt) coefficient records
+    long long nch;
+    int nt;
+    float dt;
+};
+cudaError_t launch_spline(const SplineArgs &a, int dtype, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// delay-and-sum
+// ---------------------------------------------------------------------------
+enum Geom { GEOM_TABBED = 0, GEOM_SYNTH = 1 };
+
+struct DasArgs {
+    // channel data (or spline coefficients for cubic), (nframes, ntx, nrx, nt)
+    const void *data;
+    // Tabbed tables (device, float32)
+    const float *tautx, *apodtx, *taurx, *apodrx;
+    // Synthetic geometry (device, float32)
+    pycbf_gb_synthetic geo;
+    const int *pixel_index;
+    float *out;
+    int *census_count;
+    long long *census_isum;
+    long long np;
+    int ntx, nrx, nt, ndim, nframes;
+    float t0, dt, inv_dt, xmax, xend, thresh, eps;
+};
+cudaError_t launch_das(const DasArgs &a, int geom, int interp, int sumtype, int dtype, bool census,
+                       cudaStream_t s);
+cudaError_t launch_synth_rx_mask(const DasArgs &a, unsigned char *mask, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// coherence
+// ---------------------------------------------------------------------------
+cudaError_t launch_dmas(const float *im, long long nframes, long long nsep, long long np,
+                        const int *lags, int nlag, int power, int sumlags, float *out,
+                        cudaStream_t s);
+cudaError_t launch_slsc(const float *im, const unsigned char *mask, long long nframes, int nrx,
+                        int nx, int nz, int nlag, int nkern, float *out, cudaStream_t s);
+
+}  // namespace pgb

@@ -1,0 +1,131 @@
+// Natural cubic spline coefficients for every channel, one warp per channel.
+//
+// The reference builds the knots of each channel with a serial Thomas solve
+// (tie_knots1D_fixed, pycbf/cpu/pycbf.c:114-166): a forward sweep
+//   u_i = (6 (y_{i+1} - 2 y_i + y_{i-1}) / (2 dx^2) - 0.5 u_{i-1}) / p_i
+// and a back-substitution y2_k = c_k y2_{k+1} + u_k.  Both recurrences
+// contract by |0.5/p| -> 2 - sqrt(3) = 0.268 per step, so a lane can start
+// either sweep 32 samples before its chunk from zero: the start error has
+// shrunk by 0.268^32 ~ 5e-19 when the chunk begins.  Each of the 32 lanes
+// owns a contiguous chunk of the channel; the channel, u and y2 sit in shared
+// memory.  Output per sample j: (y_j, y_j+1, z_j, z_j+1), z = y2 dx^2 / 6,
+// with y_nt = z_nt = 0, so the forward kernel does one 16-byte (or 8-byte)
+// load per tap.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace pgb {
+
+constexpr int kWarm = 32;
+
+void make_spline_table(SplineTable *t) {
+    float y2f = 0.0f;
+    t->invp[0] = 0.5f;
+    t->c[0] = 0.0f;
+    for (int i = 1; i < kSplineTab; ++i) {
+        float p = 0.5f * y2f + 2.0f;
+        float y2 = (0.5f - 1.0f) / p;
+        t->invp[i] = 1.0f / p;
+        t->c[i] = y2;
+        y2f = y2;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+spline_coef_kernel(const T *__restrict__ rf, typename CoefRec<T>::raw *__restrict__ coef,
+                   long long nch, int nt, float dt, const __grid_constant__ SplineTable tab) {
+    extern __shared__ float smem[];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    const long long ch = (long long)blockIdx.x * wpb + w;
+    if (ch >= nch) return;
+    const int stride = nt + 1;
+    float *y = smem + (size_t)w * 3 * stride;
+    float *u = y + stride;
+    float *z = u + stride;
+
+    const T *src = rf + ch * (long long)nt;
+    for (int k = lane; k < nt; k += 32) y[k] = load_sample(src + k);
+    if (lane == 0) {
+        y[nt] = 0.f;
+        u[0] = 0.f;
+        z[nt] = 0.f;
+        z[nt - 1] = 0.f;
+    }
+    __syncwarp();
+
+    const float inv_dt = 1.0f / dt;
+    const float cscale = 6.0f / (2.0f * dt);
+    const float zscale = dt * dt / 6.0f;
+    const int C = (nt + 31) >> 5;
+    const int s = lane * C;
+    const int e = min(s + C, nt);
+
+    // forward sweep: u_i for i in [max(s,1), min(e, nt-1))
+    {
+        const int ib = max(s, 1), ie = min(e, nt - 1);
+        if (ib < ie) {
+            float up = 0.f;
+            for (int i = max(1, ib - kWarm); i < ie; ++i) {
+                const float d1 = (y[i + 1] - y[i]) * inv_dt;
+                const float d0 = (y[i] - y[i - 1]) * inv_dt;
+                const float ui = fmaf(d1 - d0, cscale, -0.5f * up) * tab.invp[min(i, kSplineTab - 1)];
+                if (i >= ib) u[i] = ui;
+                up = ui;
+            }
+        }
+    }
+    __syncwarp();
+    // back-substitution: y2_k for k in [s, min(e, nt-1)), y2_{nt-1} = 0
+    {
+        const int kb = s, ke = min(e, nt - 1);
+        if (kb < ke) {
+            float yn = 0.f;
+            for (int k = min(nt - 2, ke - 1 + kWarm); k >= kb; --k) {
+                const float uk = (k == 0) ? 0.f : u[k];
+                const float y2k = fmaf(tab.c[min(k, kSplineTab - 1)], yn, uk);
+                if (k < ke) z[k] = y2k * zscale;
+                yn = y2k;
+            }
+        }
+    }
+    __syncwarp();
+    typename CoefRec<T>::raw *dst = coef + ch * (long long)nt;
+    for (int k = lane; k < nt; k += 32) dst[k] = CoefRec<T>::pack(y[k], y[k + 1], z[k], z[k + 1]);
+}
+
+template <typename T>
+static cudaError_t launch_spline_t(const SplineArgs &a, cudaStream_t s) {
+    const size_t per_warp = sizeof(float) * 3 * (size_t)(a.nt + 1);
+    int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (96 * 1024) / per_warp));
+    const size_t smem = per_warp * wpb;
+    if (smem > 227 * 1024) return cudaErrorInvalidValue;
+    static SplineTable tab = [] {
+        SplineTable t;
+        make_spline_table(&t);
+        return t;
+    }();
+    cudaError_t err = cudaFuncSetAttribute(spline_coef_kernel<T>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    const long long blocks = (a.nch + wpb - 1) / wpb;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    spline_coef_kernel<T><<<(unsigned)blocks, 32 * wpb, smem, s>>>(
+        static_cast<const T *>(a.rf), static_cast<typename CoefRec<T>::raw *>(a.coef), a.nch, a.nt,
+        a.dt, tab);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spline(const SplineArgs &a, int dtype, cudaStream_t s) {
+    switch (dtype) {
+        case PYCBF_GB_F32: return launch_spline_t<float>(a, s);
+        case PYCBF_GB_F16: return launch_spline_t<__half>(a, s);
+        case PYCBF_GB_BF16: return launch_spline_t<__nv_bfloat16>(a, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace pgb

@@ -1,0 +1,179 @@
+"""Seeded synthetic channel data and the named workloads.
+
+Channel data are sums of Gaussian-modulated pulses (the pulse of
+scipy.signal.gausspulse: exp(-a t^2) cos(2 pi fc t), a set by the fractional
+bandwidth at -6 dB) at the two-way delays of point scatterers, plus white
+noise at a fixed level below the signal RMS.  Each echo is evaluated only on
+the samples where its envelope exceeds 1e-9, with torch on the given device.
+
+Workloads (sizes as named by the benchmark configurations):
+
+* ``tabbed_c1``: 128-element linear array, 0.3 mm pitch, 11 plane waves over
+  -10..+10 deg, fs 25 MHz, 5 MHz pulse at 60 % bandwidth, Nt 2048, c 1540 m/s,
+  20 bright points + 5000 N(0,1) speckle in x in [-19, 19] mm, z in [5, 45] mm,
+  -40 dB noise; grid 256 x 512; tautx/taurx from the plane-wave geometry,
+  apodtx all ones, apodrx a Hann window inside an F#1.5 mask.
+* ``synthetic_c2``: 192 elements, 0.2 mm pitch, 75 plane waves over -18..+18
+  deg, fs 31.25 MHz, f0 6.25 MHz, Nt 4096, 40 000 speckle + 30 points, grid
+  512 x 1024 over x in [-19.2, 19.2] mm, z in [5, 45] mm, synthetic-point
+  geometry (virtual sources 10 m behind the array), F#1.5 receive.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import helpers
+
+
+def gauss_pulse_a(fc: float, bw: float, bwr_db: float = -6.0) -> float:
+    ref = 10.0 ** (bwr_db / 20.0)
+    return -((math.pi * fc * bw) ** 2) / (4.0 * math.log(ref))
+
+
+def simulate_channels(tau_tx: torch.Tensor, tau_rx: torch.Tensor, amp: torch.Tensor,
+                      t0: float, dt: float, nt: int, fc: float, bw: float,
+                      noise_db: float | None, seed: int) -> torch.Tensor:
+    """rf[tx, rx, t] = sum_s amp[s] * pulse(t - tau_tx[tx, s] - tau_rx[rx, s]).
+
+    tau_tx: (ntx, ns), tau_rx: (nrx, ns), amp: (ns,) on one device (float64).
+    Returns float32 (ntx, nrx, nt) on that device.
+    """
+    dev = tau_tx.device
+    ntx, ns = tau_tx.shape
+    nrx = tau_rx.shape[0]
+    a = gauss_pulse_a(fc, bw)
+    half = int(math.ceil(math.sqrt(math.log(1e9) / a) / dt)) + 1
+    offs = torch.arange(-half, half + 1, device=dev, dtype=torch.float64)
+    chunk = max(1, int(2e7 // (ntx * nrx * offs.numel())))
+    rf = torch.zeros(ntx * nrx * nt, dtype=torch.float64, device=dev)
+    for s0 in range(0, ns, chunk):
+        s1 = min(ns, s0 + chunk)
+        tt = tau_tx[:, None, s0:s1] + tau_rx[None, :, s0:s1]            # (ntx, nrx, S)
+        centre = torch.round((tt - t0) / dt)                            # nearest sample
+        idx = centre[..., None] + offs                                  # (ntx, nrx, S, K)
+        tloc = t0 + idx * dt - tt[..., None]
+        val = amp[None, None, s0:s1, None] * torch.exp(-a * tloc * tloc) * torch.cos(
+            2 * math.pi * fc * tloc)
+        ok = (idx >= 0) & (idx < nt)
+        base = (torch.arange(ntx * nrx, device=dev, dtype=torch.float64).view(ntx, nrx, 1, 1)
+                * nt)
+        flat = (base + idx.clamp(0, nt - 1)).long()
+        rf.index_add_(0, flat[ok], val[ok])
+    rf = rf.view(ntx, nrx, nt)
+    if noise_db is not None:
+        g = torch.Generator(device="cpu").manual_seed(seed + 1)
+        rms = torch.sqrt(torch.mean(rf * rf)).item()
+        noise = torch.randn(rf.shape, generator=g, dtype=torch.float64) * (
+            rms * 10 ** (noise_db / 20.0))
+        rf = rf + noise.to(dev)
+    return rf.to(torch.float32)
+
+
+def scatterers(seed: int, n_speckle: int, n_points: int, xlim, zlim, bright: float = 10.0,
+               ndim: int = 2, ylim=None):
+    """(positions (ns, ndim), amplitudes (ns,)) -- speckle N(0,1), points `bright`."""
+    rng = np.random.default_rng(seed)
+    ns = n_speckle + n_points
+    pos = np.empty((ns, ndim))
+    pos[:, 0] = rng.uniform(xlim[0], xlim[1], ns)
+    if ndim == 3:
+        pos[:, 1] = rng.uniform(ylim[0], ylim[1], ns)
+    pos[:, -1] = rng.uniform(zlim[0], zlim[1], ns)
+    amp = np.concatenate([rng.normal(0.0, 1.0, n_speckle), np.full(n_points, bright)])
+    return pos, amp
+
+
+@dataclass
+class TabbedWorkload:
+    name: str
+    rf: np.ndarray            # (ntx, nrx, nt) float32
+    tautx: np.ndarray         # (ntx, np) float32
+    apodtx: np.ndarray
+    taurx: np.ndarray         # (nrx, np) float32
+    apodrx: np.ndarray
+    t0: float
+    dt: float
+    nt: int
+    grid: tuple = ()
+    meta: dict = field(default_factory=dict)
+
+
+@dataclass
+class SyntheticWorkload:
+    name: str
+    rf: np.ndarray
+    geometry: dict            # ovectx, nvectx, t0tx, doftx, alatx, ovecrx, nvecrx, alarx, c0, pnts
+    t0: float
+    dt: float
+    nt: int
+    grid: tuple = ()
+    meta: dict = field(default_factory=dict)
+
+
+def _device(device):
+    if device is None:
+        return torch.device("cuda" if torch.cuda.is_available() else "cpu")
+    return torch.device(device)
+
+
+def linear_pw_tabbed(nele=128, pitch=0.3e-3, nsteer=11, max_deg=10.0, fs=25e6, fc=5e6, bw=0.6,
+                     nt=2048, c=1540.0, nx=256, nz=512, xlim=(-19e-3, 19e-3),
+                     zlim=(5e-3, 45e-3), n_speckle=5000, n_points=20, fnum=1.5,
+                     noise_db=-40.0, seed=1234, device=None, name="tabbed") -> TabbedWorkload:
+    """Plane-wave Tabbed workload (defaults: the 128-element, 11-angle case)."""
+    dev = _device(device)
+    xele = helpers.element_positions(nele, pitch)
+    steers = np.radians(np.linspace(-max_deg, max_deg, nsteer))
+    xout = np.linspace(xlim[0], xlim[1], nx)
+    zout = np.linspace(zlim[0], zlim[1], nz)
+    tautx, _ = helpers.pw_tx_tables(steers, c, c, xele, xout, zout, ones=True)
+    taurx, apodrx = helpers.rx_tables(c, xele, xout, zout, fnum, hann=True)
+    pos, amp = scatterers(seed, n_speckle, n_points, xlim, zlim)
+    # scatterer delays with the same formulas as the tables
+    sx = pos[:, 0]
+    sz = pos[:, 1]
+    O = np.where(steers <= 0, xele[-1], xele[0])
+    tt = ((sx[None] - O[:, None]) * np.sin(steers)[:, None] + sz[None] * np.cos(steers)[:, None]) / c
+    tr = np.hypot(sx[None] - xele[:, None], sz[None]) / c
+    t0, dt = 0.0, 1.0 / fs
+    rf = simulate_channels(torch.tensor(tt, device=dev), torch.tensor(tr, device=dev),
+                           torch.tensor(amp, device=dev), t0, dt, nt, fc, bw, noise_db, seed)
+    f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    return TabbedWorkload(name, rf.cpu().numpy(), f32(tautx), np.ones_like(f32(tautx)), f32(taurx),
+                          f32(apodrx), t0, dt, nt, (nx, nz),
+                          dict(nele=nele, pitch=pitch, nsteer=nsteer, fs=fs, fc=fc, bw=bw, c=c,
+                               fnum=fnum, seed=seed, xout=xout, zout=zout))
+
+
+def linear_pw_synthetic(nele=192, pitch=0.2e-3, nsteer=75, max_deg=18.0, fs=31.25e6, fc=6.25e6,
+                        bw=0.6, nt=4096, c=1540.0, nx=512, nz=1024, xlim=(-19.2e-3, 19.2e-3),
+                        zlim=(5e-3, 45e-3), n_speckle=40000, n_points=30, fnum=1.5,
+                        noise_db=-40.0, seed=4321, device=None,
+                        name="synthetic") -> SyntheticWorkload:
+    """Plane waves as far virtual sources (defaults: the 192-element, 75-angle case)."""
+    dev = _device(device)
+    xele = helpers.element_positions(nele, pitch)
+    steers = np.radians(np.linspace(-max_deg, max_deg, nsteer))
+    xout = np.linspace(xlim[0], xlim[1], nx)
+    zout = np.linspace(zlim[0], zlim[1], nz)
+    geo = helpers.pw_synthetic_points(steers, c, c, xele, fnum)
+    pnts = helpers.pixel_grid(xout, zout)
+    pos, amp = scatterers(seed, n_speckle, n_points, xlim, zlim)
+    # echo delays from the same virtual-source model: sign(proj)|s-o|/c + t0tx
+    d = pos[None, :, :] - geo["ovectx"][:, None, :]
+    proj = np.sum(d * geo["nvectx"][:, None, :], axis=-1)
+    tt = np.sign(proj) * np.linalg.norm(d, axis=-1) / c + geo["t0tx"][:, None]
+    tr = np.linalg.norm(pos[None, :, :] - geo["ovecrx"][:, None, :], axis=-1) / c
+    t0, dt = 0.0, 1.0 / fs
+    rf = simulate_channels(torch.tensor(tt, device=dev), torch.tensor(tr, device=dev),
+                           torch.tensor(amp, device=dev), t0, dt, nt, fc, bw, noise_db, seed)
+    geo = dict(geo)
+    geo["c0"] = c
+    geo["pnts"] = pnts
+    return SyntheticWorkload(name, rf.cpu().numpy(), geo, t0, dt, nt, (nx, nz),
+                             dict(nele=nele, pitch=pitch, nsteer=nsteer, fs=fs, fc=fc, c=c,
+                                  fnum=fnum, seed=seed, xout=xout, zout=zout))

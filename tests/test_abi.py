@@ -1,0 +1,106 @@
+"""The C-ABI library builds, loads and exports every symbol its header declares;
+host-side validation returns status codes before any CUDA call (CPU only)."""
+import ctypes as ct
+import os
+import re
+import subprocess
+
+import pytest
+
+from pycbf_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            text = open(os.path.join(inc, f)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names |= set(re.findall(r"\b(pycbf_gb_\w+)\s*\(", text))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.load()
+    syms = declared_symbols()
+    assert len(syms) >= 12
+    for s in syms:
+        assert hasattr(L, s), s
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True,
+                         text=True).stdout
+    exported = set(re.findall(r"\bT (pycbf_gb_\w+)", out))
+    assert syms <= exported
+    assert set(_lib.EXPORTS) <= syms
+
+
+def test_abi_version_and_status_strings():
+    L = _lib.load()
+    assert L.pycbf_gb_abi_version() == 1
+    assert L.pycbf_gb_status_string(0) == b"ok"
+    assert b"workspace" in L.pycbf_gb_status_string(_lib.EWORKSPACE)
+
+
+def _info(**kw):
+    base = dict(ntx=2, nrx=3, ndim=0, t0=0.0, dt=1.0, nt=16, nframes=1, dtype=_lib.F32)
+    base.update(kw)
+    return _lib.RFInfo(**base)
+
+
+def test_workspace_bytes():
+    L = _lib.load()
+    info = _info()
+    assert L.pycbf_gb_workspace_bytes(ct.byref(info), _lib.INTERP["cubic"]) == 2 * 3 * 16 * 16
+    assert L.pycbf_gb_workspace_bytes(ct.byref(info), _lib.INTERP["nearest"]) == 0
+    half = _info(dtype=_lib.F16, nframes=4)
+    assert L.pycbf_gb_workspace_bytes(ct.byref(half), _lib.INTERP["cubic"]) == 4 * 2 * 3 * 16 * 8
+
+
+@pytest.mark.parametrize("bad,code", [
+    (dict(ntx=0), _lib.EINVAL), (dict(nt=0), _lib.EINVAL), (dict(dt=0.0), _lib.EINVAL),
+    (dict(dt=float("nan")), _lib.EINVAL), (dict(dtype=7), _lib.EINVAL),
+    (dict(nframes=70000), _lib.ERANGE), (dict(nt=1 << 22), _lib.ERANGE),
+])
+def test_tabbed_rejects_bad_rfinfo(bad, code):
+    L = _lib.load()
+    info = _info(**bad)
+    p = ct.c_void_p(16)  # never dereferenced: validation fails first
+    st = L.pycbf_gb_das_tabbed(ct.byref(info), p, p, p, p, p, 10, None, 2, 0.01, 3, p, p, 1 << 20,
+                               None)
+    assert st == code
+
+
+def test_tabbed_rejects_null_and_codes():
+    L = _lib.load()
+    info = _info()
+    p = ct.c_void_p(16)
+    call = lambda **kw: L.pycbf_gb_das_tabbed(
+        ct.byref(info), kw.get("rf", p), p, p, p, p, kw.get("np", 10), None, kw.get("interp", 2),
+        kw.get("thresh", 0.01), kw.get("sum", 3), kw.get("out", p), kw.get("ws", p),
+        kw.get("wsb", 1 << 20), None)
+    assert call(rf=None) == _lib.EINVAL
+    assert call(out=None) == _lib.EINVAL
+    assert call(interp=9) == _lib.EINVAL
+    assert call(sum=6) == _lib.EINVAL
+    assert call(thresh=float("nan")) == _lib.EINVAL
+    assert call(np=-1) == _lib.ERANGE
+    assert call(np=0) == _lib.OK          # nothing to do
+    assert call(ws=None) == _lib.EWORKSPACE
+    assert call(wsb=100) == _lib.EWORKSPACE
+    assert call(ws=ct.c_void_p(8)) == _lib.EINVAL  # misaligned workspace
+
+
+def test_synthetic_and_coherence_validation():
+    L = _lib.load()
+    info = _info(ndim=1)
+    geo = _lib.SyntheticGeom()
+    p = ct.c_void_p(16)
+    assert L.pycbf_gb_das_synthetic(ct.byref(info), p, ct.byref(geo), None, 2, 3, p, p, 1 << 20,
+                                    None) == _lib.EINVAL
+    assert L.pycbf_gb_dmas(None, 1, 4, 10, p, 2, 0, 1, p, None) == _lib.EINVAL
+    assert L.pycbf_gb_dmas(p, 1, 4, 10, p, 2, 3, 1, p, None) == _lib.EINVAL
+    assert L.pycbf_gb_slsc(p, p, 1, 8, 4, 4, 40, 2, p, None) == _lib.ERANGE
+    assert L.pycbf_gb_slsc(p, p, 1, 8, 4, 4, 4, 40, p, None) == _lib.ERANGE
+    assert L.pycbf_gb_slsc(p, None, 1, 8, 4, 4, 4, 2, p, None) == _lib.EINVAL

@@ -1,0 +1,210 @@
+"""GPU parity of the Tabbed path against the pinned oracle and the reference's
+golden outputs.  The tap set (in-range and apodization decisions, and each
+tap's sample index) must match bit-exactly; images within rel-L2 1e-5 and
+max-abs 1e-4 of the peak; the float64 error is checked and reported."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import pycbf_gb300 as pg
+from gpu_util import assert_image_close, report
+from oracle import oracle
+from pycbf_gb300 import phantom
+
+pytestmark = pytest.mark.gpu
+CASES = ["pw_small", "edge", "short2", "short3"]
+NCPU = max(1, len(os.sched_getaffinity(0)))
+
+
+def bf_for(case, kind="cubic", sumtype="tx_and_rx", **kw):
+    interp = dict(kind=kind) if isinstance(kind, str) else kind
+    return pg.TabbedBeamformer(tautx=case["tautx"], taurx=case["taurx"], apodtx=case["apodtx"],
+                               apodrx=case["apodrx"], t0=float(case["t0"]), dt=float(case["dt"]),
+                               nt=int(case["nt"]), interp=interp, sumtype=sumtype, **kw)
+
+
+def oracle_for(case, kind="cubic", sumtype="tx_and_rx", threads=1):
+    return oracle.das_tabbed(case["rf"], case["tautx"], case["apodtx"], case["taurx"], case["apodrx"],
+                             float(case["t0"]), float(case["dt"]), int(case["nt"]), interp=kind,
+                             sumtype=sumtype, threads=threads)
+
+
+@pytest.fixture(scope="module")
+def c1_small():
+    w = phantom.linear_pw_tabbed(nx=64, nz=128, n_speckle=1500, device="cuda")
+    return dict(rf=w.rf, tautx=w.tautx, apodtx=w.apodtx, taurx=w.taurx, apodrx=w.apodrx,
+                t0=w.t0, dt=w.dt, nt=w.nt)
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("sumtype", ["tx_and_rx", "tx_only", "rx_only", "none"])
+def test_cubic_vs_reference_golden(golden, name, sumtype):
+    case = golden(f"tabbed_{name}.npz")
+    out = bf_for(case, "cubic", sumtype)(case["rf"])
+    assert_image_close(out, case[f"ref_cubic_{sumtype}"], what=f"{name}/{sumtype}")
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_nearest_vs_reference_golden(golden, name):
+    case = golden(f"tabbed_{name}.npz")
+    out = bf_for(case, "nearest")(case["rf"])
+    # nearest picks samples: exact up to the summation order
+    assert_image_close(out, case["ref_nearest_tx_and_rx"], rel=1e-6, peak=1e-6, what=name)
+    out = bf_for(case, "nearest", "rx_only")(case["rf"])
+    assert_image_close(out, case["ref_nearest_rx_only"], rel=1e-6, peak=1e-6, what=name)
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("kind", ["cubic", "nearest", "linear"])
+def test_tap_census_bit_exact_golden_cases(golden, name, kind):
+    case = golden(f"tabbed_{name}.npz")
+    cnt, isum = bf_for(case, kind).tap_census()
+    ok_cnt, ok_isum = oracle.tap_census(case["tautx"], case["apodtx"], case["taurx"], case["apodrx"],
+                                        float(case["t0"]), float(case["dt"]), int(case["nt"]),
+                                        interp="nearest" if kind == "nearest" else "cubic")
+    np.testing.assert_array_equal(cnt.cpu().numpy(), ok_cnt)
+    np.testing.assert_array_equal(isum.cpu().numpy(), ok_isum)
+
+
+def test_tap_census_near_boundaries():
+    """Delays placed within a few ulp of every knot and half-knot boundary."""
+    rng = np.random.default_rng(42)
+    nt, dt, t0 = 512, np.float32(1 / 31.25e6), np.float32(1.3e-6)
+    npx = 4096
+    k = rng.integers(-3, nt + 3, size=npx).astype(np.float32)
+    frac = rng.choice(np.array([0.0, 0.5], np.float32), size=npx)
+    base = (t0 + dt * (k + frac)).astype(np.float32)
+    ulps = rng.integers(-4, 5, size=npx)
+    tau = np.array([np.float32(b) for b in base], np.float32)
+    for i in range(npx):
+        for _ in range(abs(int(ulps[i]))):
+            tau[i] = np.nextafter(tau[i], np.float32(np.inf if ulps[i] > 0 else -np.inf))
+    case = dict(tautx=tau[None, :].copy(), taurx=np.zeros((2, npx), np.float32),
+                apodtx=np.ones((1, npx), np.float32),
+                apodrx=rng.choice(np.array([1, 0.01, 0.0099999, -0.02], np.float32), size=(2, npx)),
+                t0=t0, dt=dt, nt=nt)
+    for kind in ("cubic", "nearest"):
+        cnt, isum = bf_for(case, kind).tap_census()
+        ok_cnt, ok_isum = oracle.tap_census(case["tautx"], case["apodtx"], case["taurx"],
+                                            case["apodrx"], float(t0), float(dt), nt, interp=kind)
+        np.testing.assert_array_equal(cnt.cpu().numpy(), ok_cnt)
+        np.testing.assert_array_equal(isum.cpu().numpy(), ok_isum)
+
+
+@pytest.mark.parametrize("sumtype", ["tx_and_rx", "tx_only", "rx_only", "none"])
+def test_c1_geometry_small_grid(c1_small, sumtype):
+    case = c1_small
+    out = bf_for(case, "cubic", sumtype)(case["rf"])
+    ref = oracle_for(case, "cubic", sumtype, threads=NCPU)
+    r, m = assert_image_close(out, ref, what=sumtype)
+    report(f"tabbed_c1_64x128_cubic_{sumtype}", rel_l2=r, max_abs_peak=m)
+
+
+def test_c1_small_fp64_error_and_census(c1_small):
+    case = c1_small
+    out = bf_for(case, "cubic")(case["rf"])
+    ref64 = oracle.das_tabbed_fp64(case["rf"], case["tautx"], case["apodtx"], case["taurx"],
+                                   case["apodrx"], case["t0"], case["dt"], case["nt"])
+    r64 = oracle.rel_l2(out, ref64)
+    assert r64 < 1e-5
+    report("tabbed_c1_64x128_cubic_vs_fp64", rel_l2=r64,
+           max_abs_peak=oracle.max_abs_rel_peak(out, ref64))
+    cnt, isum = bf_for(case, "cubic").tap_census()
+    ok_cnt, ok_isum = oracle.tap_census(case["tautx"], case["apodtx"], case["taurx"], case["apodrx"],
+                                        case["t0"], case["dt"], case["nt"])
+    np.testing.assert_array_equal(cnt.cpu().numpy(), ok_cnt)
+    np.testing.assert_array_equal(isum.cpu().numpy(), ok_isum)
+
+
+@pytest.mark.parametrize("kind", ["nearest", "linear"])
+def test_other_kinds_vs_oracle(c1_small, kind):
+    out = bf_for(c1_small, kind)(c1_small["rf"])
+    ref = oracle_for(c1_small, kind, threads=NCPU)
+    assert_image_close(out, ref, what=kind)
+
+
+def test_linear_reference_floor_vs_oracle(c1_small):
+    out = bf_for(c1_small, dict(kind="linear", reference_floor=True))(c1_small["rf"])
+    ref = oracle_for(c1_small, "linear_floor", threads=NCPU)
+    assert_image_close(out, ref, rel=1e-6, peak=1e-6, what="linear_floor")
+
+
+def test_pixel_order_does_not_change_results(c1_small):
+    a = bf_for(c1_small, "cubic", pixel_order="auto")(c1_small["rf"])
+    b = bf_for(c1_small, "cubic", pixel_order="natural")(c1_small["rf"])
+    np.testing.assert_array_equal(a, b)
+
+
+def test_frames_batch_equals_single_frames(c1_small):
+    rng = np.random.default_rng(1)
+    frames = np.stack([c1_small["rf"], rng.normal(size=c1_small["rf"].shape).astype(np.float32),
+                       -c1_small["rf"]])
+    for sumtype in ("tx_and_rx", "tx_only"):
+        bf = bf_for(c1_small, "cubic", sumtype)
+        batch = bf(frames)
+        for f in range(3):
+            np.testing.assert_array_equal(batch[f], bf(frames[f]))
+
+
+@pytest.mark.parametrize("storage,tol", [("float16", 1e-3), ("bfloat16", 1e-2)])
+def test_reduced_precision_storage(c1_small, storage, tol):
+    case = c1_small
+    out = bf_for(case, "cubic", storage=storage)(case["rf"])
+    ref64 = oracle.das_tabbed_fp64(case["rf"], case["tautx"], case["apodtx"], case["taurx"],
+                                   case["apodrx"], case["t0"], case["dt"], case["nt"])
+    r = oracle.rel_l2(out, ref64)
+    report(f"tabbed_c1_64x128_cubic_{storage}_vs_fp64", rel_l2=r)
+    assert r < tol
+
+
+def test_torch_io_and_buffer(c1_small):
+    bf = bf_for(c1_small, "cubic")
+    rf = torch.as_tensor(c1_small["rf"], device="cuda")
+    buf = torch.empty(bf.nop, device="cuda")
+    out = bf(rf, out_as_numpy=False, buffer=buf)
+    assert out.data_ptr() == buf.data_ptr() and out.is_cuda
+    np.testing.assert_array_equal(out.cpu().numpy(), bf(c1_small["rf"]))
+    with pytest.raises(pg.BeamformerException):
+        bf(rf, buffer=torch.empty(3, device="cuda"))
+    with pytest.raises(pg.BeamformerException):
+        bf(rf[:, :5])
+
+
+def test_full_c1_vs_threaded_oracle():
+    """The full 11 x 128 x 2048, 256 x 512 workload against the oracle."""
+    w = phantom.linear_pw_tabbed(device="cuda")
+    case = dict(rf=w.rf, tautx=w.tautx, apodtx=w.apodtx, taurx=w.taurx, apodrx=w.apodrx,
+                t0=w.t0, dt=w.dt, nt=w.nt)
+    bf = bf_for(case, "cubic")
+    out = bf(case["rf"])
+    ref = oracle_for(case, "cubic", threads=NCPU)
+    r, m = assert_image_close(out, ref, what="full c1")
+    report("tabbed_c1_full_cubic_vs_oracle", rel_l2=r, max_abs_peak=m)
+    cnt, isum = bf.tap_census()
+    ok_cnt, ok_isum = oracle.tap_census(case["tautx"], case["apodtx"], case["taurx"], case["apodrx"],
+                                        case["t0"], case["dt"], case["nt"])
+    np.testing.assert_array_equal(cnt.cpu().numpy(), ok_cnt)
+    np.testing.assert_array_equal(isum.cpu().numpy(), ok_isum)
+    # size-independent property: the image is linear in the channel data
+    two = bf(2 * case["rf"] - case["rf"][:, ::-1, :])
+    lin = 2 * out - bf(np.ascontiguousarray(case["rf"][:, ::-1, :]))
+    assert oracle.rel_l2(two, lin) < 1e-5
+
+
+def test_interp_known_answer_gpu():
+    import kat_interp
+    d = kat_interp.make_data()
+    t0, dt, nt = d["t"][0], d["t"][1] - d["t"][0], len(d["t"])
+    tab = dict(tautx=d["tautxrx"], taurx=d["tautxrx"], apodtx=d["apod"], apodrx=d["apod"])
+    mk = lambda kind: pg.TabbedBeamformer(**tab, t0=t0, dt=dt, nt=nt, interp={"kind": kind})
+    g_near = mk("nearest")(d["rf"])
+    g_cubic = mk("cubic")(d["rf"])
+    o_cubic = oracle.das_tabbed(d["rf"], d["tautxrx"], d["apod"], d["tautxrx"], d["apod"], t0, dt, nt,
+                                interp="cubic", threads=NCPU)
+    rmse = kat_interp.rmse_roi(g_near, o_cubic, d)
+    assert abs(rmse - kat_interp.NOTEBOOK_RMSE) <= 1e-6 * kat_interp.NOTEBOOK_RMSE, rmse
+    err = kat_interp.rmse_roi(g_cubic, o_cubic, d)
+    report("kat_gpu", rmse_nearest_vs_cubic=rmse, rmse_gpu_cubic_vs_cpu_cubic=err)
+    assert err < 1e-5 * kat_interp.rms_roi(o_cubic, d)
