@@ -43,6 +43,24 @@ __device__ __forceinline__ float quotient_near_half(float d, const DasArgs &a) {
     return q;
 }
 
+// knot j = (int)((x - t0)/dt) for an in-range x (pycbf.c:81)
+__device__ __forceinline__ int knot_index(float x, const DasArgs &a) {
+    const float q = quotient_near_int(__fsub_rn(x, a.t0), a);
+    return min((int)floorf(q), a.nt - 1);
+}
+
+// The interpolation fractions as the reference rounds them (pycbf.c:93-98):
+// xhi = t0 + dt*(j+1), xlo = t0 + dt*j, a = (xhi - x)/dt, b = (x - xlo)/dt.
+// x carries ~q*2^-24 of rounding relative to dt, so deriving b from the
+// quotient instead would differ from the reference by that much.
+__device__ __forceinline__ void knot_fractions(float x, int j, const DasArgs &a, float &am,
+                                               float &b) {
+    const float xlo = __fadd_rn(a.t0, __fmul_rn(a.dt, (float)j));
+    const float xhi = __fadd_rn(a.t0, __fmul_rn(a.dt, (float)(j + 1)));
+    am = __fmul_rn(__fsub_rn(xhi, x), a.inv_dt);
+    b = __fmul_rn(__fsub_rn(x, xlo), a.inv_dt);
+}
+
 // ---------------------------------------------------------------------------
 // interpolation of one channel at delay x; sets idx (census) and inr
 // ---------------------------------------------------------------------------
@@ -54,16 +72,13 @@ template <typename T> struct Interp<PYCBF_GB_INTERP_CUBIC, T> {
                                                  const DasArgs &a, int &idx, bool &inr) {
         inr = (x >= a.t0) && (x <= a.xmax);
         if (!inr) return 0.f;
-        const float d = __fsub_rn(x, a.t0);
-        const float q = quotient_near_int(d, a);
-        const float fq = floorf(q);
-        const float b = q - fq;
-        const int j = min((int)fq, a.nt - 1);
+        const int j = knot_index(x, a);
         idx = j;
         if (!LOAD) return 0.f;
         using rec = typename CoefRec<T>::raw;
         const float4 c = CoefRec<T>::load(static_cast<const rec *>(data) + ch + j);
-        const float am = 1.f - b;
+        float am, b;
+        knot_fractions(x, j, a, am, b);
         const float wa = fmaf(am * am, am, -am);
         const float wb = fmaf(b * b, b, -b);
         return fmaf(am, c.x, fmaf(b, c.y, fmaf(wa, c.z, wb * c.w)));
@@ -76,17 +91,15 @@ template <typename T> struct Interp<PYCBF_GB_INTERP_LINEAR, T> {
                                                  const DasArgs &a, int &idx, bool &inr) {
         inr = (x >= a.t0) && (x <= a.xmax);
         if (!inr) return 0.f;
-        const float d = __fsub_rn(x, a.t0);
-        const float q = quotient_near_int(d, a);
-        const float fq = floorf(q);
-        const float b = q - fq;
-        const int j = min((int)fq, a.nt - 1);
+        const int j = knot_index(x, a);
         idx = j;
         if (!LOAD) return 0.f;
         const T *y = static_cast<const T *>(data) + ch;
         const float y0 = load_sample(y + j);
         const float y1 = (j + 1 < a.nt) ? load_sample(y + j + 1) : 0.f;
-        return fmaf(1.f - b, y0, b * y1);
+        float am, b;
+        knot_fractions(x, j, a, am, b);
+        return fmaf(am, y0, b * y1);
     }
 };
 
@@ -271,7 +284,7 @@ __global__ void __launch_bounds__(kBlock) das_kernel(const __grid_constant__ Das
                     }
                 }
             }
-            if (SUM == PYCBF_GB_SUM_NONE)
+            if (!CENSUS && SUM == PYCBF_GB_SUM_NONE)
                 a.out[((long long)(f * ntx + t) * nrx + r) * np + op] = contrib;
             return contrib;
         };
@@ -294,7 +307,7 @@ __global__ void __launch_bounds__(kBlock) das_kernel(const __grid_constant__ Das
             }
         }
         if (SUM == PYCBF_GB_SUM_TX_AND_RX) acc += accr;
-        if (SUM == PYCBF_GB_SUM_TX_ONLY) a.out[((long long)f * nrx + r) * np + op] = accr;
+        if (!CENSUS && SUM == PYCBF_GB_SUM_TX_ONLY) a.out[((long long)f * nrx + r) * np + op] = accr;
         if (SUM == PYCBF_GB_SUM_DMAS_SSR || SUM == PYCBF_GB_SUM_DMAS_POWER) {
             // pairwise sum over receives i<j of s_i s_j as sum_j s_j * (sum_{i<j} s_i):
             // no cancellation, two FMAs per receive
@@ -304,10 +317,11 @@ __global__ void __launch_bounds__(kBlock) das_kernel(const __grid_constant__ Das
         }
     }
 
-    if (SUM == PYCBF_GB_SUM_TX_AND_RX || SUM == PYCBF_GB_SUM_DMAS_SSR ||
-        SUM == PYCBF_GB_SUM_DMAS_POWER)
+    // census launches carry no image buffer (out is NULL): they store counts only
+    if (!CENSUS && (SUM == PYCBF_GB_SUM_TX_AND_RX || SUM == PYCBF_GB_SUM_DMAS_SSR ||
+                    SUM == PYCBF_GB_SUM_DMAS_POWER))
         a.out[(long long)f * np + op] = acc;
-    if (SUM == PYCBF_GB_SUM_RX_ONLY) {
+    if (!CENSUS && SUM == PYCBF_GB_SUM_RX_ONLY) {
         for (int k = 0; k < ntx; ++k) {
             float v;
             if (in_regs) {
