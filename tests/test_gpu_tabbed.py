@@ -108,9 +108,14 @@ def test_c1_small_fp64_error_and_census(c1_small):
     ref64 = oracle.das_tabbed_fp64(case["rf"], case["tautx"], case["apodtx"], case["taurx"],
                                    case["apodrx"], case["t0"], case["dt"], case["nt"])
     r64 = oracle.rel_l2(out, ref64)
-    assert r64 < 1e-5
+    # float32 delays carry ~q*2^-24 of rounding relative to dt, so any float32
+    # implementation of the reference algorithm sits ~2e-5 from float64; the GPU
+    # must be no further from float64 than the reference's own float32 path
+    ref32 = oracle_for(case, "cubic", threads=NCPU)
+    r32 = oracle.rel_l2(ref32, ref64)
+    assert r64 <= 1e-3 and r64 <= 1.25 * r32, (r64, r32)
     report("tabbed_c1_64x128_cubic_vs_fp64", rel_l2=r64,
-           max_abs_peak=oracle.max_abs_rel_peak(out, ref64))
+           max_abs_peak=oracle.max_abs_rel_peak(out, ref64), oracle_f32_rel_l2_vs_fp64=r32)
     cnt, isum = bf_for(case, "cubic").tap_census()
     ok_cnt, ok_isum = oracle.tap_census(case["tautx"], case["apodtx"], case["taurx"], case["apodrx"],
                                         case["t0"], case["dt"], case["nt"])
