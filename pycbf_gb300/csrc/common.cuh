@@ -21,6 +21,10 @@ __device__ __forceinline__ float load_sample(const __nv_bfloat16 *p) {
     return __bfloat162float(__ldg(p));
 }
 
+__device__ __forceinline__ float load_sample_reg(float v) { return v; }
+__device__ __forceinline__ float load_sample_reg(__half v) { return __half2float(v); }
+__device__ __forceinline__ float load_sample_reg(__nv_bfloat16 v) { return __bfloat162float(v); }
+
 // A spline coefficient record (y_j, y_j+1, z_j, z_j+1): float4 for float32
 // channel data, four 16-bit values packed in a uint2 otherwise.
 template <typename T> struct CoefRec;

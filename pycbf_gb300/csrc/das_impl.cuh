@@ -26,27 +26,12 @@
 namespace pgb {
 
 constexpr int kBlock = 128;
-constexpr int kTxReg = 16;
+constexpr int kTxReg = 12;
 constexpr float kDxMin = 1e-12f;
 
-__device__ __forceinline__ float quotient_near_int(float d, const DasArgs &a) {
-    float q = __fmul_rn(d, a.inv_dt);
-    const float f = q - floorf(q);
-    if (f < a.eps || f > 1.f - a.eps) q = __fdiv_rn(d, a.dt);
-    return q;
-}
-
-__device__ __forceinline__ float quotient_near_half(float d, const DasArgs &a) {
-    float q = __fmul_rn(d, a.inv_dt);
-    const float f = q - floorf(q);
-    if (fabsf(f - 0.5f) < a.eps) q = __fdiv_rn(d, a.dt);
-    return q;
-}
-
-// knot j = (int)((x - t0)/dt) for an in-range x (pycbf.c:81)
-__device__ __forceinline__ int knot_index(float x, const DasArgs &a) {
-    const float q = quotient_near_int(__fsub_rn(x, a.t0), a);
-    return min((int)floorf(q), a.nt - 1);
+// (int)fl for an integral float 0 <= fl < 2^23 without a conversion instruction
+__device__ __forceinline__ int small_int(float fl) {
+    return __float_as_int(__fadd_rn(fl, 8388608.0f)) - 0x4B000000;
 }
 
 // The interpolation fractions as the reference rounds them (pycbf.c:93-98):
@@ -55,28 +40,45 @@ __device__ __forceinline__ int knot_index(float x, const DasArgs &a) {
 // quotient instead would differ from the reference by that much.
 __device__ __forceinline__ void knot_fractions(float x, int j, const DasArgs &a, float &am,
                                                float &b) {
-    const float xlo = __fadd_rn(a.t0, __fmul_rn(a.dt, (float)j));
-    const float xhi = __fadd_rn(a.t0, __fmul_rn(a.dt, (float)(j + 1)));
+    const float fj = (float)j;
+    const float xlo = __fadd_rn(a.t0, __fmul_rn(a.dt, fj));
+    const float xhi = __fadd_rn(a.t0, __fmul_rn(a.dt, __fadd_rn(fj, 1.0f)));
     am = __fmul_rn(__fsub_rn(xhi, x), a.inv_dt);
     b = __fmul_rn(__fsub_rn(x, xlo), a.inv_dt);
 }
 
 // ---------------------------------------------------------------------------
-// interpolation of one channel at delay x; sets idx (census) and inr
+// Interpolation kinds.  Each tap goes through
+//   index(x)        fast: in-range flag, sample index, and whether the
+//                   reciprocal quotient sits within eps of a decision boundary
+//   index_exact(x)  the same with the IEEE quotient (taken only when flagged)
+//   load(idx)       the channel payload (one 16/8-byte record or 1-2 samples)
+//   value(payload)  the interpolated sample
+// so that a thread can put the gathers of several taps in flight at once.
 // ---------------------------------------------------------------------------
-template <int KIND, typename T> struct Interp;
+template <int KIND, typename T> struct Kind;
 
-template <typename T> struct Interp<PYCBF_GB_INTERP_CUBIC, T> {
-    template <bool LOAD>
-    static __device__ __forceinline__ float eval(const void *data, long long ch, float x,
-                                                 const DasArgs &a, int &idx, bool &inr) {
-        inr = (x >= a.t0) && (x <= a.xmax);
-        if (!inr) return 0.f;
-        const int j = knot_index(x, a);
-        idx = j;
-        if (!LOAD) return 0.f;
+template <typename T> struct Kind<PYCBF_GB_INTERP_CUBIC, T> {
+    using P = float4;
+    static __device__ __forceinline__ bool index(float x, const DasArgs &a, int &idx, bool &fix) {
+        const bool inr = (x >= a.t0) && (x <= a.xmax);
+        const float q = __fmul_rn(__fsub_rn(x, a.t0), a.inv_dt);
+        const float fl = floorf(q);
+        const float f = q - fl;
+        fix = (f < a.eps) || (f > 1.f - a.eps);
+        idx = min(small_int(fl), a.nt - 1);
+        return inr;
+    }
+    static __device__ __forceinline__ bool index_exact(float x, const DasArgs &a, int &idx) {
+        idx = min((int)floorf(__fdiv_rn(__fsub_rn(x, a.t0), a.dt)), a.nt - 1);
+        return (x >= a.t0) && (x <= a.xmax);
+    }
+    static __device__ __forceinline__ P load(const void *data, long long ch, int idx,
+                                            const DasArgs &a) {
         using rec = typename CoefRec<T>::raw;
-        const float4 c = CoefRec<T>::load(static_cast<const rec *>(data) + ch + j);
+        return CoefRec<T>::load(static_cast<const rec *>(data) + ch + idx);
+    }
+    static __device__ __forceinline__ float value(const P &c, float x, int j, const DasArgs &a) {
         float am, b;
         knot_fractions(x, j, a, am, b);
         const float wa = fmaf(am * am, am, -am);
@@ -85,61 +87,80 @@ template <typename T> struct Interp<PYCBF_GB_INTERP_CUBIC, T> {
     }
 };
 
-template <typename T> struct Interp<PYCBF_GB_INTERP_LINEAR, T> {
-    template <bool LOAD>
-    static __device__ __forceinline__ float eval(const void *data, long long ch, float x,
-                                                 const DasArgs &a, int &idx, bool &inr) {
-        inr = (x >= a.t0) && (x <= a.xmax);
-        if (!inr) return 0.f;
-        const int j = knot_index(x, a);
-        idx = j;
-        if (!LOAD) return 0.f;
+template <typename T> struct Kind<PYCBF_GB_INTERP_LINEAR, T> {
+    using P = float2;
+    static __device__ __forceinline__ bool index(float x, const DasArgs &a, int &idx, bool &fix) {
+        return Kind<PYCBF_GB_INTERP_CUBIC, T>::index(x, a, idx, fix);
+    }
+    static __device__ __forceinline__ bool index_exact(float x, const DasArgs &a, int &idx) {
+        return Kind<PYCBF_GB_INTERP_CUBIC, T>::index_exact(x, a, idx);
+    }
+    static __device__ __forceinline__ P load(const void *data, long long ch, int idx,
+                                            const DasArgs &a) {
         const T *y = static_cast<const T *>(data) + ch;
-        const float y0 = load_sample(y + j);
-        const float y1 = (j + 1 < a.nt) ? load_sample(y + j + 1) : 0.f;
+        return make_float2(load_sample(y + idx), idx + 1 < a.nt ? load_sample(y + idx + 1) : 0.f);
+    }
+    static __device__ __forceinline__ float value(const P &c, float x, int j, const DasArgs &a) {
         float am, b;
         knot_fractions(x, j, a, am, b);
-        return fmaf(am, y0, b * y1);
+        return fmaf(am, c.x, b * c.y);
     }
 };
 
-template <typename T> struct Interp<PYCBF_GB_INTERP_NEAREST, T> {
-    template <bool LOAD>
-    static __device__ __forceinline__ float eval(const void *data, long long ch, float x,
-                                                 const DasArgs &a, int &idx, bool &inr) {
-        const float d = __fsub_rn(x, a.t0);
-        const float q = quotient_near_half(d, a);
+template <typename T> struct Kind<PYCBF_GB_INTERP_NEAREST, T> {
+    using P = float;
+    static __device__ __forceinline__ bool index(float x, const DasArgs &a, int &idx, bool &fix) {
+        const float q = __fmul_rn(__fsub_rn(x, a.t0), a.inv_dt);
+        const float f = q - floorf(q);
+        fix = fabsf(f - 0.5f) < a.eps;
         const int it = __float2int_rz(q + 0.5f);
-        inr = (x == x) && (it >= 0) && (it < a.nt);
-        if (!inr) return 0.f;
         idx = it;
-        if (!LOAD) return 0.f;
-        return load_sample(static_cast<const T *>(data) + ch + it);
+        return (x == x) && (it >= 0) && (it < a.nt);
+    }
+    static __device__ __forceinline__ bool index_exact(float x, const DasArgs &a, int &idx) {
+        const int it = __float2int_rz(__fdiv_rn(__fsub_rn(x, a.t0), a.dt) + 0.5f);
+        idx = it;
+        return (x == x) && (it >= 0) && (it < a.nt);
+    }
+    static __device__ __forceinline__ P load(const void *data, long long ch, int idx,
+                                            const DasArgs &a) {
+        return load_sample(static_cast<const T *>(data) + ch + idx);
+    }
+    static __device__ __forceinline__ float value(const P &c, float, int, const DasArgs &) {
+        return c;
     }
 };
 
 // The reference CUDA linear_interp as written (__engines__.cu:36-53): the two
 // weights multiply the same sample, so it returns (nearly) the floor sample.
-template <typename T> struct Interp<PYCBF_GB_INTERP_LINEAR_FLOOR, T> {
-    template <bool LOAD>
-    static __device__ __forceinline__ float eval(const void *data, long long ch, float x,
-                                                 const DasArgs &a, int &idx, bool &inr) {
-        const T *y = static_cast<const T *>(data) + ch;
+template <typename T> struct Kind<PYCBF_GB_INTERP_LINEAR_FLOOR, T> {
+    using P = float;
+    static __device__ __forceinline__ bool index(float x, const DasArgs &a, int &idx, bool &fix) {
+        const float q = __fmul_rn(__fsub_rn(x, a.t0), a.inv_dt);
+        const float f = q - floorf(q);
+        fix = (f < a.eps) || (f > 1.f - a.eps);
+        return floor_in_range(x, __float2int_rz(q), a, idx);
+    }
+    static __device__ __forceinline__ bool index_exact(float x, const DasArgs &a, int &idx) {
+        return floor_in_range(x, __float2int_rz(__fdiv_rn(__fsub_rn(x, a.t0), a.dt)), a, idx);
+    }
+    static __device__ __forceinline__ bool floor_in_range(float x, int ixo, const DasArgs &a,
+                                                          int &idx) {
         if (x == a.xend) {
-            inr = true;
             idx = a.nt - 1;
-            return LOAD ? load_sample(y + a.nt - 1) : 0.f;
+            return true;
         }
-        const float d = __fsub_rn(x, a.t0);
-        const float q = quotient_near_int(d, a);
-        const int ixo = __float2int_rz(q);
-        inr = (x == x) && (ixo >= 0) && (ixo < a.nt);
-        if (!inr) return 0.f;
         idx = ixo;
-        if (!LOAD) return 0.f;
+        return (x == x) && (ixo >= 0) && (ixo < a.nt);
+    }
+    static __device__ __forceinline__ P load(const void *data, long long ch, int idx,
+                                            const DasArgs &a) {
+        return load_sample(static_cast<const T *>(data) + ch + idx);
+    }
+    static __device__ __forceinline__ float value(const P &v, float x, int ixo, const DasArgs &a) {
+        if (x == a.xend) return v;
         const float frac =
             __fdiv_rn(__fsub_rn(__fsub_rn(x, __fmul_rn((float)ixo, a.dt)), a.t0), a.dt);
-        const float v = load_sample(y + ixo);
         return __fadd_rn(__fmul_rn(v, __fsub_rn(1.0f, frac)), __fmul_rn(v, frac));
     }
 };
@@ -196,8 +217,11 @@ __device__ __forceinline__ float synth_rx_delay(const DasArgs &a, int r, const f
 // ---------------------------------------------------------------------------
 // the kernel
 // ---------------------------------------------------------------------------
+constexpr int kGroup = 6;  // taps whose gathers a thread keeps in flight together
+
 template <int GEOM, int KIND, int SUM, typename T, bool CENSUS>
-__global__ void __launch_bounds__(kBlock) das_kernel(const __grid_constant__ DasArgs a) {
+__global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ DasArgs a) {
+    using K = Kind<KIND, T>;
     extern __shared__ float sm[];
     const int tid = threadIdx.x;
     const long long i = (long long)blockIdx.x * kBlock + tid;
@@ -208,33 +232,39 @@ __global__ void __launch_bounds__(kBlock) das_kernel(const __grid_constant__ Das
     const long long op = a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i;
     const bool in_regs = ntx <= kTxReg;
     const long long frame_ch = (long long)f * ntx * nrx;
+    const long long chs = (long long)nrx * a.nt;  // channel stride between transmits
 
     float pnt[3] = {0.f, 0.f, 0.f};
     if (GEOM == GEOM_SYNTH)
         for (int k = 0; k < a.ndim; ++k) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
 
-    // transmit side: registers or this thread's column of shared memory
+    // transmit side: registers (ntx <= kTxReg) or this thread's column of shared memory.
+    // Synthetic masks travel as +inf delays, which the range test rejects.
     float rtau[kTxReg], rapod[kTxReg], racc[kTxReg];
     float *stau = sm + tid;
     float *sapod = stau + (size_t)ntx * kBlock;
     float *sacc = sapod + (GEOM == GEOM_TABBED ? (size_t)ntx * kBlock : 0);
+    float amax = 0.f;  // max |apodtx| of this pixel, for the exact receive-level reject
     auto tx_side = [&](int t, float &tau, float &apod) {
         if (GEOM == GEOM_TABBED) {
             tau = __ldg(a.tautx + (long long)t * np + i);
             apod = __ldg(a.apodtx + (long long)t * np + i);
+            amax = fmaxf(amax, fabsf(apod));
         } else {
             tau = synth_tx_delay(a, t, pnt);
             apod = 1.f;
         }
     };
+#pragma unroll
+    for (int k = 0; k < kTxReg; ++k) {
+        rtau[k] = 0.f;
+        rapod[k] = 0.f;
+        racc[k] = 0.f;
+    }
     if (in_regs) {
 #pragma unroll
-        for (int k = 0; k < kTxReg; ++k) {
-            rtau[k] = 0.f;
-            rapod[k] = 0.f;
-            racc[k] = 0.f;
+        for (int k = 0; k < kTxReg; ++k)
             if (k < ntx) tx_side(k, rtau[k], rapod[k]);
-        }
     } else {
         for (int k = 0; k < ntx; ++k) {
             float tau, apod;
@@ -249,8 +279,8 @@ __global__ void __launch_bounds__(kBlock) das_kernel(const __grid_constant__ Das
     int cnt = 0;
     long long isum = 0;
 
-    for (int r = 0; r < nrx; ++r) {
-        float trx, arx;
+    // receive-side values, fetched one receive ahead
+    auto rx_side = [&](int r, float &trx, float &arx) {
         if (GEOM == GEOM_TABBED) {
             trx = __ldg(a.taurx + (long long)r * np + i);
             arx = __ldg(a.apodrx + (long long)r * np + i);
@@ -258,54 +288,123 @@ __global__ void __launch_bounds__(kBlock) das_kernel(const __grid_constant__ Das
             trx = synth_rx_delay(a, r, pnt);
             arx = 1.f;
         }
+    };
+    float trx_next = 0.f, arx_next = 0.f;
+    if (GEOM == GEOM_TABBED && nrx > 0) rx_side(0, trx_next, arx_next);
+
+    for (int r = 0; r < nrx; ++r) {
+        float trx, arx;
+        if (GEOM == GEOM_TABBED) {
+            trx = trx_next;
+            arx = arx_next;
+            if (r + 1 < nrx) rx_side(r + 1, trx_next, arx_next);
+        } else {
+            rx_side(r, trx, arx);
+        }
+        // Exact reject of the whole receive: rounding is monotonic, so
+        // fl(amax*|arx|) < thresh implies fl(|apodtx*apodrx|) < thresh for every
+        // transmit.  A masked synthetic receive has an infinite delay.
+        bool live;
+        if (GEOM == GEOM_TABBED) live = __fmul_rn(amax, fabsf(arx)) >= a.thresh;
+        else live = trx != __int_as_float(0x7f800000);
+        if (!live && SUM != PYCBF_GB_SUM_NONE) {
+            if (!CENSUS && SUM == PYCBF_GB_SUM_TX_ONLY) a.out[((long long)f * nrx + r) * np + op] = 0.f;
+            continue;
+        }
+        const long long ch0 = (frame_ch + r) * a.nt;  // channel (tx 0, rx r)
         float accr = 0.f;
-        auto tap = [&](int t, float ttx, float atx) -> float {
-            bool hit;
-            float apod;
-            if (GEOM == GEOM_TABBED) {
-                apod = __fmul_rn(atx, arx);
-                hit = fabsf(apod) >= a.thresh;
-            } else {
-                apod = 1.f;
-                hit = true;
+
+        // one group of up to kGroup transmits taken from registers or shared memory
+        auto group = [&](int k0, int nk, const float *tt, const float *at) {
+            float xs[kGroup], ap[kGroup];
+            int ix[kGroup];
+            unsigned hit = 0u, fix = 0u;
+#pragma unroll
+            for (int k = 0; k < kGroup; ++k) {
+                xs[k] = 0.f;
+                ap[k] = 0.f;
+                ix[k] = 0;
+                if (k < nk) {
+                    const float x = __fadd_rn(tt[k], trx);
+                    float apod = 1.f;
+                    bool h = true;
+                    if (GEOM == GEOM_TABBED) {
+                        apod = __fmul_rn(at[k], arx);
+                        h = fabsf(apod) >= a.thresh;
+                    }
+                    bool fx;
+                    int idx;
+                    const bool inr = K::index(x, a, idx, fx);
+                    xs[k] = x;
+                    ap[k] = apod;
+                    ix[k] = idx;
+                    hit |= (unsigned)(h && inr) << k;
+                    fix |= (unsigned)(h && fx) << k;
+                }
             }
-            float contrib = 0.f;
-            if (hit) {
-                const float x = __fadd_rn(ttx, trx);
-                int idx = 0;
-                bool inr;
-                const long long ch = (frame_ch + (long long)t * nrx + r) * a.nt;
-                const float v = Interp<KIND, T>::template eval<!CENSUS>(a.data, ch, x, a, idx, inr);
-                if (inr) {
-                    contrib = (GEOM == GEOM_TABBED) ? apod * v : v;
-                    if (CENSUS) {
-                        cnt += 1;
-                        isum += idx;
+            if (fix) {  // rare: a quotient next to a rounding boundary, redo it exactly
+#pragma unroll
+                for (int k = 0; k < kGroup; ++k) {
+                    if ((fix >> k) & 1u) {
+                        int idx;
+                        const bool inr = K::index_exact(xs[k], a, idx);
+                        ix[k] = idx;
+                        hit = inr ? (hit | (1u << k)) : (hit & ~(1u << k));
                     }
                 }
             }
-            if (!CENSUS && SUM == PYCBF_GB_SUM_NONE)
-                a.out[((long long)(f * ntx + t) * nrx + r) * np + op] = contrib;
-            return contrib;
-        };
-        if (in_regs) {
+            typename K::P pv[kGroup];
 #pragma unroll
-            for (int k = 0; k < kTxReg; ++k) {
-                if (k < ntx) {
-                    const float c = tap(k, rtau[k], rapod[k]);
-                    if (SUM == PYCBF_GB_SUM_RX_ONLY) racc[k] += c;
-                    else accr += c;
+            for (int k = 0; k < kGroup; ++k)
+                if ((hit >> k) & 1u) pv[k] = K::load(a.data, ch0 + (long long)(k0 + k) * chs, ix[k], a);
+#pragma unroll
+            for (int k = 0; k < kGroup; ++k) {
+                if (k < nk) {
+                    float c = 0.f;
+                    if ((hit >> k) & 1u) {
+                        if (!CENSUS) {
+                            const float v = K::value(pv[k], xs[k], ix[k], a);
+                            c = (GEOM == GEOM_TABBED) ? ap[k] * v : v;
+                        } else {
+                            cnt += 1;
+                            isum += ix[k];
+                        }
+                    }
+                    const int t = k0 + k;
+                    if (!CENSUS && SUM == PYCBF_GB_SUM_NONE)
+                        a.out[((long long)(f * ntx + t) * nrx + r) * np + op] = c;
+                    if (SUM == PYCBF_GB_SUM_RX_ONLY) {
+                        if (in_regs) {
+#pragma unroll
+                            for (int kk = 0; kk < kTxReg; ++kk)
+                                if (kk == t) racc[kk] += c;
+                        } else {
+                            sacc[(size_t)t * kBlock] += c;
+                        }
+                    } else {
+                        accr += c;
+                    }
                 }
             }
+        };
+
+        if (in_regs) {
+#pragma unroll
+            for (int g = 0; g < kTxReg; g += kGroup)
+                if (g < ntx) group(g, min(kGroup, ntx - g), rtau + g, rapod + g);
         } else {
-            for (int k = 0; k < ntx; ++k) {
-                const float ttx = stau[(size_t)k * kBlock];
-                const float atx = (GEOM == GEOM_TABBED) ? sapod[(size_t)k * kBlock] : 1.f;
-                const float c = tap(k, ttx, atx);
-                if (SUM == PYCBF_GB_SUM_RX_ONLY) sacc[(size_t)k * kBlock] += c;
-                else accr += c;
+            for (int g = 0; g < ntx; g += kGroup) {
+                const int nk = min(kGroup, ntx - g);
+                float tt[kGroup], at[kGroup];
+#pragma unroll
+                for (int k = 0; k < kGroup; ++k) {
+                    tt[k] = (k < nk) ? stau[(size_t)(g + k) * kBlock] : 0.f;
+                    at[k] = (GEOM == GEOM_TABBED && k < nk) ? sapod[(size_t)(g + k) * kBlock] : 1.f;
+                }
+                group(g, nk, tt, at);
             }
         }
+
         if (SUM == PYCBF_GB_SUM_TX_AND_RX) acc += accr;
         if (!CENSUS && SUM == PYCBF_GB_SUM_TX_ONLY) a.out[((long long)f * nrx + r) * np + op] = accr;
         if (SUM == PYCBF_GB_SUM_DMAS_SSR || SUM == PYCBF_GB_SUM_DMAS_POWER) {
@@ -322,17 +421,12 @@ __global__ void __launch_bounds__(kBlock) das_kernel(const __grid_constant__ Das
                     SUM == PYCBF_GB_SUM_DMAS_POWER))
         a.out[(long long)f * np + op] = acc;
     if (!CENSUS && SUM == PYCBF_GB_SUM_RX_ONLY) {
-        for (int k = 0; k < ntx; ++k) {
-            float v;
-            if (in_regs) {
-                v = 0.f;
+        if (in_regs) {
 #pragma unroll
-                for (int kk = 0; kk < kTxReg; ++kk)
-                    if (kk == k) v = racc[kk];
-            } else {
-                v = sacc[(size_t)k * kBlock];
-            }
-            a.out[((long long)f * ntx + k) * np + op] = v;
+            for (int k = 0; k < kTxReg; ++k)
+                if (k < ntx) a.out[((long long)f * ntx + k) * np + op] = racc[k];
+        } else {
+            for (int k = 0; k < ntx; ++k) a.out[((long long)f * ntx + k) * np + op] = sacc[(size_t)k * kBlock];
         }
     }
     if (CENSUS) {

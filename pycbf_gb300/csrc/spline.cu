@@ -42,13 +42,26 @@ spline_coef_kernel(const T *__restrict__ rf, typename CoefRec<T>::raw *__restric
     const int wpb = blockDim.x >> 5;
     const long long ch = (long long)blockIdx.x * wpb + w;
     if (ch >= nch) return;
-    const int stride = nt + 1;
+    const int stride = (nt + 4) & ~3;  // >= nt+1, keeps every array 16-byte aligned
     float *y = smem + (size_t)w * 3 * stride;
     float *u = y + stride;
     float *z = u + stride;
 
+    // stage the channel: 16-byte vector loads, several in flight per lane
     const T *src = rf + ch * (long long)nt;
-    for (int k = lane; k < nt; k += 32) y[k] = load_sample(src + k);
+    constexpr int V = 16 / sizeof(T);
+    if ((nt % V) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+#pragma unroll 8
+        for (int k = lane; k < nt / V; k += 32) {
+            const uint4 v = __ldg(s4 + k);
+            const T *e = reinterpret_cast<const T *>(&v);
+#pragma unroll
+            for (int m = 0; m < V; ++m) y[k * V + m] = load_sample_reg(e[m]);
+        }
+    } else {
+        for (int k = lane; k < nt; k += 32) y[k] = load_sample(src + k);
+    }
     if (lane == 0) {
         y[nt] = 0.f;
         u[0] = 0.f;
@@ -99,7 +112,7 @@ spline_coef_kernel(const T *__restrict__ rf, typename CoefRec<T>::raw *__restric
 
 template <typename T>
 static cudaError_t launch_spline_t(const SplineArgs &a, cudaStream_t s) {
-    const size_t per_warp = sizeof(float) * 3 * (size_t)(a.nt + 1);
+    const size_t per_warp = sizeof(float) * 3 * (size_t)((a.nt + 4) & ~3);
     int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (96 * 1024) / per_warp));
     const size_t smem = per_warp * wpb;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
