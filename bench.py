@@ -218,8 +218,9 @@ def main_ours(a):
     pidx = ct.c_void_p(bf._pixel_index.data_ptr()) if bf._pixel_index is not None else None
     P = lambda t: ct.c_void_p(t.data_ptr())
     args_spline = (ct.byref(info), P(rf), P(ws), nws)
+    plan = ct.c_void_p(bf._plan.data_ptr()) if bf._plan is not None else None
     args_das = (ct.byref(info), P(ws), P(tautx), P(apodtx), P(taurx), P(apodrx), bf.nop, pidx,
-                ct.c_float(0.01), 3, P(out))
+                ct.c_float(0.01), 3, plan, P(out))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > L2
     stream = torch.cuda.current_stream()
     sp = ct.c_void_p(stream.cuda_stream)
@@ -291,7 +292,8 @@ def main_ours(a):
     achieved = alg_bytes / das_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": None,
-                "kernel": "das_kernel<tabbed, cubic, tx_and_rx, f32>",
+                "kernel": ("das_staged_kernel<cubic, tx_and_rx, f32>" if bf._plan is not None
+                           else "das_kernel<tabbed, cubic, tx_and_rx, f32>"),
                 "kernel_ms": 1e3 * das_s, "spline_ms": statistics.mean(spline_ms),
                 "peak_source": "measured" if peaks.get("hbm_gbs") else "fallback",
                 "algorithmic_bytes": alg_bytes}

@@ -133,13 +133,28 @@ int pycbf_gb_spline_coefficients(const pycbf_gb_rfinfo *rf, const void *rfdata, 
 /* the delay tautx+taurx is in range (pycbf.c:200-203, 84-87, 264-267).    */
 /* pixel_index: NULL, or int32[np]: table column i is written to output    */
 /* pixel pixel_index[i] (lets callers store the tables in a                */
-/* locality-friendly order).  out is written, not accumulated.             */
+/* locality-friendly order).  plan: NULL, or a staging plan built by       */
+/* pycbf_gb_tabbed_plan for these tables, this thresh and this interp;     */
+/* with it, ntx <= 12 and sumtype tx_only / tx_and_rx / dmas, the kernel   */
+/* stages channel windows in shared memory by TMA (same results).  out is  */
+/* written, not accumulated.                                               */
 /* ---------------------------------------------------------------------- */
 int pycbf_gb_das_tabbed(const pycbf_gb_rfinfo *rf, const void *rfdata, const float *tautx,
                         const float *apodtx, const float *taurx, const float *apodrx,
                         long long np, const int *pixel_index, int interp, float thresh,
-                        int sumtype, float *out, void *workspace, size_t workspace_bytes,
-                        void *stream);
+                        int sumtype, const void *plan, float *out, void *workspace,
+                        size_t workspace_bytes, void *stream);
+
+/* Staging plan of a Tabbed table set (no counterpart in the reference: it  */
+/* precomputes, per tile of 128 table columns, the receives that can        */
+/* contribute and the delay bounds that size each channel window).  plan    */
+/* needs pycbf_gb_tabbed_plan_bytes bytes, 16-byte aligned; ntx <= 12.      */
+/* Its first int32 is a status word: 0, or 1 after a kernel gave up a       */
+/* bounded wait (its outputs are then NaN).                                 */
+size_t pycbf_gb_tabbed_plan_bytes(long long np, int ntx, int nrx);
+int pycbf_gb_tabbed_plan(const pycbf_gb_rfinfo *rf, const float *tautx, const float *apodtx,
+                         const float *taurx, const float *apodrx, long long np, int interp,
+                         float thresh, void *plan, size_t plan_bytes, void *stream);
 
 /* The cubic Tabbed delay-and-sum on coefficients already produced by      */
 /* pycbf_gb_spline_coefficients (prefilter once, beamform with several     */
@@ -148,7 +163,8 @@ int pycbf_gb_das_tabbed(const pycbf_gb_rfinfo *rf, const void *rfdata, const flo
 int pycbf_gb_das_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef,
                                     const float *tautx, const float *apodtx, const float *taurx,
                                     const float *apodrx, long long np, const int *pixel_index,
-                                    float thresh, int sumtype, float *out, void *stream);
+                                    float thresh, int sumtype, const void *plan, float *out,
+                                    void *stream);
 
 /* ---------------------------------------------------------------------- */
 /* Synthetic-point delay-and-sum: delays and masks computed per pixel on   */

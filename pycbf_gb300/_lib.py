@@ -24,7 +24,7 @@ SUMTYPE = {"none": 0, "tx_only": 1, "rx_only": 2, "tx_and_rx": 3, "dmas_ssr": 4,
 EXPORTS = (
     "pycbf_gb_abi_version", "pycbf_gb_status_string", "pycbf_gb_last_cuda_error",
     "pycbf_gb_workspace_bytes", "pycbf_gb_spline_coefficients", "pycbf_gb_das_tabbed",
-    "pycbf_gb_das_tabbed_prefiltered",
+    "pycbf_gb_das_tabbed_prefiltered", "pycbf_gb_tabbed_plan_bytes", "pycbf_gb_tabbed_plan",
     "pycbf_gb_das_synthetic", "pycbf_gb_tap_census_tabbed", "pycbf_gb_tap_census_synthetic",
     "pycbf_gb_synthetic_rx_mask", "pycbf_gb_dmas", "pycbf_gb_slsc", "pycbf_gb_fp32_probe",
 )
@@ -72,9 +72,12 @@ def load() -> ct.CDLL:
         L.pycbf_gb_workspace_bytes.restype = sz
         L.pycbf_gb_spline_coefficients.argtypes = [P(RFInfo), vp, vp, sz, vp]
         L.pycbf_gb_das_tabbed.argtypes = [P(RFInfo), vp, vp, vp, vp, vp, ll, vp, i, f, i, vp, vp,
-                                          sz, vp]
+                                          vp, sz, vp]
+        L.pycbf_gb_tabbed_plan_bytes.argtypes = [ll, i, i]
+        L.pycbf_gb_tabbed_plan_bytes.restype = sz
+        L.pycbf_gb_tabbed_plan.argtypes = [P(RFInfo), vp, vp, vp, vp, ll, i, f, vp, sz, vp]
         L.pycbf_gb_das_tabbed_prefiltered.argtypes = [P(RFInfo), vp, vp, vp, vp, vp, ll, vp, f, i,
-                                                      vp, vp]
+                                                      vp, vp, vp]
         L.pycbf_gb_das_synthetic.argtypes = [P(RFInfo), vp, P(SyntheticGeom), vp, i, i, vp, vp,
                                              sz, vp]
         L.pycbf_gb_tap_census_tabbed.argtypes = [P(RFInfo), vp, vp, vp, vp, ll, i, f, vp, vp, vp]
@@ -85,7 +88,8 @@ def load() -> ct.CDLL:
         L.pycbf_gb_fp32_probe.argtypes = [vp, i, i, vp]
         for name in EXPORTS:
             if name not in ("pycbf_gb_abi_version", "pycbf_gb_status_string",
-                            "pycbf_gb_last_cuda_error", "pycbf_gb_workspace_bytes"):
+                            "pycbf_gb_last_cuda_error", "pycbf_gb_workspace_bytes",
+                            "pycbf_gb_tabbed_plan_bytes"):
                 getattr(L, name).restype = i
         _lib = L
         return L

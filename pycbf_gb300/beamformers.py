@@ -237,6 +237,7 @@ class _GPUBeamformer(Beamformer):
     thresh: float = 1e-2
     storage: Literal["float32", "float16", "bfloat16"] = "float32"
     pixel_order: Literal["auto", "natural"] = "auto"
+    stage_channels: bool = True             # Tabbed: TMA-staged kernel where it applies
 
     def __post_init__(self):
         Beamformer.__post_init__(self)
@@ -365,6 +366,16 @@ class TabbedBeamformer(Tabbed, _GPUBeamformer):
             apodtx, apodrx = apodtx[:, perm].contiguous(), apodrx[:, perm].contiguous()
             self._pixel_index = perm.to(torch.int32).contiguous()
         self._tables = (tautx, apodtx, taurx, apodrx)
+        self._plan = None
+        if self.stage_channels and self.ntx <= 12 and self._interp_code <= _lib.INTERP["cubic"]:
+            nbytes = self._lib.pycbf_gb_tabbed_plan_bytes(self.nop, self.ntx, self.nrx)
+            self._plan = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
+            info = self._rfinfo(1)
+            st = self._lib.pycbf_gb_tabbed_plan(
+                ct.byref(info), _ptr(tautx), _ptr(apodtx), _ptr(taurx), _ptr(apodrx), self.nop,
+                self._interp_code, float(np.float32(self.thresh)), _ptr(self._plan), nbytes,
+                _stream_ptr())
+            _lib.check(st, "pycbf_gb_tabbed_plan")
 
     def _launch(self, rf, info, out, sumtype_code):
         tautx, apodtx, taurx, apodrx = self._tables
@@ -372,8 +383,14 @@ class TabbedBeamformer(Tabbed, _GPUBeamformer):
         st = self._lib.pycbf_gb_das_tabbed(
             ct.byref(info), _ptr(rf), _ptr(tautx), _ptr(apodtx), _ptr(taurx), _ptr(apodrx),
             self.nop, _ptr(self._pixel_index), self._interp_code, float(np.float32(self.thresh)),
-            sumtype_code, _ptr(out), _ptr(ws), nws, _stream_ptr())
+            sumtype_code, _ptr(self._plan), _ptr(out), _ptr(ws), nws, _stream_ptr())
         _lib.check(st, "pycbf_gb_das_tabbed")
+
+    def kernel_status(self) -> int:
+        """0, or 1 if a staged launch gave up a bounded wait (its outputs are NaN)."""
+        if self._plan is None:
+            return 0
+        return int(self._plan[:4].view(torch.int32)[0].item())
 
     def tap_census(self):
         """Per pixel (original order): contributing taps and the sum of their sample indices."""

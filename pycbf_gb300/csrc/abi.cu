@@ -73,6 +73,33 @@ bool das_shape_ok(int geom, int sumtype, long long ntx) {
     return per * (size_t)ntx * 128 * sizeof(float) <= 227 * 1024;
 }
 
+// The TMA-staged kernel covers ntx <= 12 with the sums over transmits per
+// receive; its 16-byte bulk copies need channel strides and the data base
+// aligned to 16 bytes.
+bool staged_ok(const pycbf_gb_rfinfo *rf, int interp, int sumtype, const void *data) {
+    if (rf->ntx > 12 || interp > PYCBF_GB_INTERP_CUBIC) return false;
+    if (sumtype != PYCBF_GB_SUM_TX_ONLY && sumtype != PYCBF_GB_SUM_TX_AND_RX &&
+        sumtype != PYCBF_GB_SUM_DMAS_SSR && sumtype != PYCBF_GB_SUM_DMAS_POWER)
+        return false;
+    const size_t elem = interp == PYCBF_GB_INTERP_CUBIC ? (rf->dtype == PYCBF_GB_F32 ? 16 : 8)
+                                                        : dtype_bytes(rf->dtype);
+    return ((size_t)rf->nt * elem) % 16 == 0 && reinterpret_cast<uintptr_t>(data) % 16 == 0;
+}
+
+int launch_tabbed(const pycbf_gb_rfinfo *rf, DasArgs &a, int interp, int sumtype, const void *plan,
+                  cudaStream_t s) {
+    if (plan && staged_ok(rf, interp, sumtype, a.data)) {
+        if (sumtype == PYCBF_GB_SUM_TX_ONLY) {  // rows of receives no pixel of a tile uses stay 0
+            const size_t bytes = sizeof(float) * (size_t)rf->nframes * rf->nrx * (size_t)a.np;
+            int st = cuda_status(cudaMemsetAsync(a.out, 0, bytes, s));
+            if (st) return st;
+        }
+        int *pl = static_cast<int *>(const_cast<void *>(plan));
+        return cuda_status(launch_das_staged(a, interp, sumtype, rf->dtype, pl, pl, s));
+    }
+    return cuda_status(launch_das(a, GEOM_TABBED, interp, sumtype, rf->dtype, false, s));
+}
+
 int prepare_data(const pycbf_gb_rfinfo *rf, const void *rfdata, int interp, void *workspace,
                  size_t workspace_bytes, cudaStream_t s, const void **data) {
     if (interp != PYCBF_GB_INTERP_CUBIC) {
@@ -138,11 +165,42 @@ int pycbf_gb_spline_coefficients(const pycbf_gb_rfinfo *rf, const void *rfdata, 
                         static_cast<cudaStream_t>(stream), &data);
 }
 
+size_t pycbf_gb_tabbed_plan_bytes(long long np, int ntx, int nrx) {
+    if (np <= 0 || ntx <= 0 || nrx <= 0) return 0;
+    return sizeof(int) * (size_t)tabbed_plan_words(np, ntx, nrx);
+}
+
+int pycbf_gb_tabbed_plan(const pycbf_gb_rfinfo *rf, const float *tautx, const float *apodtx,
+                         const float *taurx, const float *apodrx, long long np, int interp,
+                         float thresh, void *plan, size_t plan_bytes, void *stream) {
+    int st = check_rf(rf, false);
+    if (st) return st;
+    if (!tautx || !apodtx || !taurx || !apodrx || !plan) return PYCBF_GB_EINVAL;
+    if (np <= 0 || np >= (1LL << 31)) return PYCBF_GB_ERANGE;
+    if (interp < 0 || interp > PYCBF_GB_INTERP_CUBIC || std::isnan(thresh)) return PYCBF_GB_EINVAL;
+    if (rf->ntx > 12) return PYCBF_GB_EUNSUPPORTED;
+    if (plan_bytes < pycbf_gb_tabbed_plan_bytes(np, (int)rf->ntx, (int)rf->nrx) ||
+        reinterpret_cast<uintptr_t>(plan) % 16)
+        return PYCBF_GB_EWORKSPACE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    DasArgs a = {};
+    fill_time_axis(a, rf);
+    a.tautx = tautx;
+    a.apodtx = apodtx;
+    a.taurx = taurx;
+    a.apodrx = apodrx;
+    a.np = np;
+    a.thresh = thresh;
+    st = cuda_status(cudaMemsetAsync(plan, 0, sizeof(int) * 4, s));
+    if (st) return st;
+    return cuda_status(launch_tabbed_plan(a, interp, rf->dtype, static_cast<int *>(plan), s));
+}
+
 int pycbf_gb_das_tabbed(const pycbf_gb_rfinfo *rf, const void *rfdata, const float *tautx,
                         const float *apodtx, const float *taurx, const float *apodrx,
                         long long np, const int *pixel_index, int interp, float thresh,
-                        int sumtype, float *out, void *workspace, size_t workspace_bytes,
-                        void *stream) {
+                        int sumtype, const void *plan, float *out, void *workspace,
+                        size_t workspace_bytes, void *stream) {
     int st = check_rf(rf, false);
     if (st) return st;
     if (!rfdata || !tautx || !apodtx || !taurx || !apodrx || !out) return PYCBF_GB_EINVAL;
@@ -165,13 +223,14 @@ int pycbf_gb_das_tabbed(const pycbf_gb_rfinfo *rf, const void *rfdata, const flo
     a.out = out;
     a.np = np;
     a.thresh = thresh;
-    return cuda_status(launch_das(a, GEOM_TABBED, interp, sumtype, rf->dtype, false, s));
+    return launch_tabbed(rf, a, interp, sumtype, plan, s);
 }
 
 int pycbf_gb_das_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef,
                                     const float *tautx, const float *apodtx, const float *taurx,
                                     const float *apodrx, long long np, const int *pixel_index,
-                                    float thresh, int sumtype, float *out, void *stream) {
+                                    float thresh, int sumtype, const void *plan, float *out,
+                                    void *stream) {
     int st = check_rf(rf, false);
     if (st) return st;
     if (!coef || !tautx || !apodtx || !taurx || !apodrx || !out) return PYCBF_GB_EINVAL;
@@ -190,8 +249,8 @@ int pycbf_gb_das_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef,
     a.out = out;
     a.np = np;
     a.thresh = thresh;
-    return cuda_status(launch_das(a, GEOM_TABBED, PYCBF_GB_INTERP_CUBIC, sumtype, rf->dtype, false,
-                                  static_cast<cudaStream_t>(stream)));
+    return launch_tabbed(rf, a, PYCBF_GB_INTERP_CUBIC, sumtype, plan,
+                         static_cast<cudaStream_t>(stream));
 }
 
 int pycbf_gb_das_synthetic(const pycbf_gb_rfinfo *rf, const void *rfdata,

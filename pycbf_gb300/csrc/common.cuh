@@ -31,14 +31,15 @@ template <typename T> struct CoefRec;
 template <> struct CoefRec<float> {
     using raw = float4;
     static __device__ __forceinline__ float4 load(const raw *p) { return __ldg(p); }
+    static __device__ __forceinline__ float4 unpack(const raw &r) { return r; }
     static __device__ __forceinline__ raw pack(float a, float b, float c, float d) {
         return make_float4(a, b, c, d);
     }
 };
 template <> struct CoefRec<__half> {
     using raw = uint2;
-    static __device__ __forceinline__ float4 load(const raw *p) {
-        uint2 r = __ldg(p);
+    static __device__ __forceinline__ float4 load(const raw *p) { return unpack(__ldg(p)); }
+    static __device__ __forceinline__ float4 unpack(raw r) {
         __half2 h0 = *reinterpret_cast<__half2 *>(&r.x);
         __half2 h1 = *reinterpret_cast<__half2 *>(&r.y);
         float2 a = __half22float2(h0), b = __half22float2(h1);
@@ -54,8 +55,8 @@ template <> struct CoefRec<__half> {
 };
 template <> struct CoefRec<__nv_bfloat16> {
     using raw = uint2;
-    static __device__ __forceinline__ float4 load(const raw *p) {
-        uint2 r = __ldg(p);
+    static __device__ __forceinline__ float4 load(const raw *p) { return unpack(__ldg(p)); }
+    static __device__ __forceinline__ float4 unpack(raw r) {
         __nv_bfloat162 h0 = *reinterpret_cast<__nv_bfloat162 *>(&r.x);
         __nv_bfloat162 h1 = *reinterpret_cast<__nv_bfloat162 *>(&r.y);
         float2 a = __bfloat1622float2(h0), b = __bfloat1622float2(h1);
@@ -117,6 +118,11 @@ struct DasArgs {
 cudaError_t launch_das(const DasArgs &a, int geom, int interp, int sumtype, int dtype, bool census,
                        cudaStream_t s);
 cudaError_t launch_synth_rx_mask(const DasArgs &a, unsigned char *mask, cudaStream_t s);
+// TMA-staged Tabbed path (ntx <= 12; sums over transmits per receive)
+long long tabbed_plan_words(long long np, int ntx, int nrx);
+cudaError_t launch_tabbed_plan(const DasArgs &a, int interp, int dtype, int *plan, cudaStream_t s);
+cudaError_t launch_das_staged(const DasArgs &a, int interp, int sumtype, int dtype, const int *plan,
+                              int *status, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // coherence

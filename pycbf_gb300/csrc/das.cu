@@ -1,5 +1,5 @@
 // Dispatch of the delay-and-sum kernels by geometry and channel-data type.
-#include "das_impl.cuh"
+#include "das_staged.cuh"
 
 namespace pgb {
 
@@ -9,6 +9,36 @@ cudaError_t launch_das_tabbed_bf16(const DasArgs &, int, int, bool, cudaStream_t
 cudaError_t launch_das_synth_f32(const DasArgs &, int, int, bool, cudaStream_t);
 cudaError_t launch_das_synth_f16(const DasArgs &, int, int, bool, cudaStream_t);
 cudaError_t launch_das_synth_bf16(const DasArgs &, int, int, bool, cudaStream_t);
+cudaError_t launch_plan_f32(const DasArgs &, int, int *, cudaStream_t);
+cudaError_t launch_plan_f16(const DasArgs &, int, int *, cudaStream_t);
+cudaError_t launch_plan_bf16(const DasArgs &, int, int *, cudaStream_t);
+cudaError_t launch_staged_f32(const DasArgs &, int, int, const int *, int *, cudaStream_t);
+cudaError_t launch_staged_f16(const DasArgs &, int, int, const int *, int *, cudaStream_t);
+cudaError_t launch_staged_bf16(const DasArgs &, int, int, const int *, int *, cudaStream_t);
+
+long long tabbed_plan_words(long long np, int ntx, int nrx) {
+    const long long tiles = (np + kBlock - 1) / kBlock;
+    return kPlanHeaderWords + tiles * plan_tile_words(ntx, nrx);
+}
+
+cudaError_t launch_tabbed_plan(const DasArgs &a, int interp, int dtype, int *plan, cudaStream_t s) {
+    switch (dtype) {
+        case PYCBF_GB_F32: return launch_plan_f32(a, interp, plan, s);
+        case PYCBF_GB_F16: return launch_plan_f16(a, interp, plan, s);
+        case PYCBF_GB_BF16: return launch_plan_bf16(a, interp, plan, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_das_staged(const DasArgs &a, int interp, int sumtype, int dtype, const int *plan,
+                              int *status, cudaStream_t s) {
+    switch (dtype) {
+        case PYCBF_GB_F32: return launch_staged_f32(a, interp, sumtype, plan, status, s);
+        case PYCBF_GB_F16: return launch_staged_f16(a, interp, sumtype, plan, status, s);
+        case PYCBF_GB_BF16: return launch_staged_bf16(a, interp, sumtype, plan, status, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
 
 cudaError_t launch_das(const DasArgs &a, int geom, int interp, int sumtype, int dtype, bool census,
                        cudaStream_t s) {

@@ -360,11 +360,15 @@ __global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ 
 #pragma unroll
             for (int k = 0; k < kGroup; ++k) {
                 if (k < nk) {
+                    // per-receive sums accumulate with one fma per tap (the staged
+                    // kernel does the same, so both give identical bits)
+                    constexpr bool kPerTap = SUM == PYCBF_GB_SUM_NONE || SUM == PYCBF_GB_SUM_RX_ONLY;
                     float c = 0.f;
                     if ((hit >> k) & 1u) {
                         if (!CENSUS) {
                             const float v = K::value(pv[k], xs[k], ix[k], a);
-                            c = (GEOM == GEOM_TABBED) ? ap[k] * v : v;
+                            if (kPerTap) c = (GEOM == GEOM_TABBED) ? ap[k] * v : v;
+                            else accr = fmaf(ap[k], v, accr);
                         } else {
                             cnt += 1;
                             isum += ix[k];
@@ -381,8 +385,6 @@ __global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ 
                         } else {
                             sacc[(size_t)t * kBlock] += c;
                         }
-                    } else {
-                        accr += c;
                     }
                 }
             }

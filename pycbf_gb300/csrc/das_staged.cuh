@@ -1,0 +1,483 @@
+// Tabbed delay-and-sum with channel windows staged in shared memory by TMA.
+//
+// The pixels of a CTA (a "tile": 128 consecutive table columns, which the
+// host stores in Morton order of their delays) need, for each (tx, rx)
+// channel, only the samples between the smallest and largest delay of the
+// tile.  A plan, built once per table set (tabbed_plan_kernel), records per
+// tile the receives that can contribute at all (the exact reject
+// fl(max|apodtx| * |apodrx|) >= thresh of at least one pixel), and per tile
+// the delay bounds of every transmit and of every live receive.  In the main
+// kernel warp 0 turns those bounds into sample windows (the same exact index
+// rule as the taps, and indices are monotonic in the delay, so every
+// contributing tap falls inside) and issues one cp.async.bulk per transmit
+// into a 4-stage ring, completing on an mbarrier; all warps then gather from
+// shared memory.  A receive whose windows exceed a stage is not staged and its
+// taps gather from global memory instead.
+//
+// Every mbarrier wait is bounded.  A wait that runs out marks the CTA's
+// outputs NaN, sets the plan's status word, waits (bounded) for its copies in
+// flight and returns.
+#pragma once
+
+#include "das_impl.cuh"
+
+namespace pgb {
+
+constexpr int kStages = 4;
+constexpr int kStageBytes = 12 * 1024;
+constexpr unsigned kWaitLimit = 1u << 20;
+
+// plan layout (int32 words): [0] status, [1] reserved, [2..3] pad, then per
+// tile a record of plan_tile_words(ntx, nrx) words:
+//   nlive | rx index per live receive (nrx) | rx lo,hi per live receive (2*nrx floats)
+//   | tx lo,hi per transmit (2*ntx floats)
+__host__ __device__ inline long long plan_tile_words(int ntx, int nrx) {
+    return 1 + (long long)nrx + 2LL * nrx + 2LL * ntx;
+}
+constexpr int kPlanHeaderWords = 4;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity) {
+    for (unsigned it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// 1-D bulk copy global -> shared (both 16-byte aligned, bytes a multiple of 16)
+__device__ __forceinline__ void tma_bulk_load(void *dst, const void *src, unsigned bytes,
+                                              unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Element (record or sample) of the staged data and its window rule.
+template <int KIND, typename T> struct StagedElem {
+    using E = T;  // samples
+    static constexpr int kExtra = (KIND == PYCBF_GB_INTERP_LINEAR) ? 1 : 0;  // j+1 is read
+};
+template <typename T> struct StagedElem<PYCBF_GB_INTERP_CUBIC, T> {
+    using E = typename CoefRec<T>::raw;  // spline records
+    static constexpr int kExtra = 0;
+};
+
+// First and one-past-last element of the window of delays [xlo, xhi], aligned
+// to 16 bytes (nt * sizeof(E) is a multiple of 16, checked on the host); empty
+// (e0 == e1) when no delay in the range can be in range.  The index rule is
+// the taps' own exact rule, and it is monotonic in the delay.
+template <int KIND, typename T>
+__device__ __forceinline__ void staged_window(float xlo, float xhi, const DasArgs &a, int &e0,
+                                              int &e1) {
+    using E = typename StagedElem<KIND, T>::E;
+    constexpr int per16 = 16 / (int)sizeof(E);
+    e0 = e1 = 0;
+    if (xlo != xlo || xhi != xhi || xhi < xlo) return;
+    int i0, i1;
+    if (KIND == PYCBF_GB_INTERP_NEAREST) {
+        Kind<KIND, T>::index_exact(xlo, a, i0);
+        Kind<KIND, T>::index_exact(xhi, a, i1);
+        if (i1 < 0 || i0 >= a.nt) return;
+    } else {
+        if (xhi < a.t0 || xlo > a.xmax) return;
+        i0 = (xlo <= a.t0) ? 0 : (int)floorf(__fdiv_rn(__fsub_rn(xlo, a.t0), a.dt));
+        i1 = (xhi >= a.xmax) ? a.nt - 1 : (int)floorf(__fdiv_rn(__fsub_rn(xhi, a.t0), a.dt));
+    }
+    i0 = min(max(i0, 0), a.nt - 1);
+    i1 = min(max(i1 + StagedElem<KIND, T>::kExtra, 0), a.nt - 1);
+    if (i1 < i0) return;
+    e0 = (i0 / per16) * per16;
+    e1 = min(((i1 + per16) / per16) * per16, a.nt);
+}
+
+// one payload from a staged window (indices clamped into the stage: a tap
+// outside its window cannot occur, and if it did it would read a wrong value,
+// never outside shared memory)
+template <int KIND, typename T>
+__device__ __forceinline__ typename Kind<KIND, T>::P staged_load(
+    const typename StagedElem<KIND, T>::E *stage, int base, int idx, unsigned cap,
+    const DasArgs &a) {
+    const unsigned e = min((unsigned)(base + idx), cap - 1u);
+    if constexpr (KIND == PYCBF_GB_INTERP_CUBIC) {
+        return CoefRec<T>::unpack(stage[e]);
+    } else if constexpr (KIND == PYCBF_GB_INTERP_LINEAR) {
+        const float y0 = load_sample_reg(stage[e]);
+        const float y1 = (idx + 1 < a.nt) ? load_sample_reg(stage[min(e + 1u, cap - 1u)]) : 0.f;
+        return make_float2(y0, y1);
+    } else {
+        return load_sample_reg(stage[e]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// plan: one CTA per tile
+// ---------------------------------------------------------------------------
+template <int KIND, typename T>
+__global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_constant__ DasArgs a,
+                                                             int *plan) {
+    using E = typename StagedElem<KIND, T>::E;
+    __shared__ float red[3][kBlock / 32];
+    __shared__ int s_any;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const long long tile = blockIdx.x;
+    const long long i = tile * kBlock + tid;
+    const bool valid = i < a.np;
+    const int ntx = a.ntx, nrx = a.nrx;
+    int *rec = plan + kPlanHeaderWords + tile * plan_tile_words(ntx, nrx);
+    int *rxidx = rec + 1;
+    float *rxlh = reinterpret_cast<float *>(rec + 1 + nrx);
+    float *txlh = rxlh + 2 * nrx;
+    const float inf = __int_as_float(0x7f800000);
+
+    auto block_minmax = [&](float lo, float hi, int any, float &blo, float &bhi, int &bany) {
+        for (int o = 16; o; o >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+            any |= __shfl_xor_sync(0xffffffffu, any, o);
+        }
+        __syncthreads();
+        if (lane == 0) {
+            red[0][w] = lo;
+            red[1][w] = hi;
+            red[2][w] = __int_as_float(any);
+        }
+        __syncthreads();
+        blo = red[0][0];
+        bhi = red[1][0];
+        bany = __float_as_int(red[2][0]);
+        for (int k = 1; k < kBlock / 32; ++k) {
+            blo = fminf(blo, red[0][k]);
+            bhi = fmaxf(bhi, red[1][k]);
+            bany |= __float_as_int(red[2][k]);
+        }
+    };
+
+    float amax = 0.f;
+    for (int t = 0; t < ntx; ++t) {
+        float tau = inf, taun = -inf;
+        if (valid) {
+            tau = taun = __ldg(a.tautx + (long long)t * a.np + i);
+            amax = fmaxf(amax, fabsf(__ldg(a.apodtx + (long long)t * a.np + i)));
+        }
+        float lo, hi;
+        int any;
+        block_minmax(tau == tau ? tau : inf, taun == taun ? taun : -inf, 0, lo, hi, any);
+        if (tid == 0) {
+            txlh[2 * t] = lo;
+            txlh[2 * t + 1] = hi;
+        }
+    }
+    __syncthreads();
+    int nlive = 0;
+    for (int r = 0; r < nrx; ++r) {
+        float trx = 0.f, arx = 0.f;
+        if (valid) {
+            trx = __ldg(a.taurx + (long long)r * a.np + i);
+            arx = __ldg(a.apodrx + (long long)r * a.np + i);
+        }
+        const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh) && (trx == trx);
+        float lo, hi;
+        int any;
+        block_minmax(live ? trx : inf, live ? trx : -inf, live ? 1 : 0, lo, hi, any);
+        if (!any) continue;
+        // staged only if all windows of this receive fit one stage
+        int bytes = 0;
+        if (tid < ntx) {
+            const float xlo = __fadd_rn(txlh[2 * tid], lo), xhi = __fadd_rn(txlh[2 * tid + 1], hi);
+            int e0, e1;
+            staged_window<KIND, T>(xlo, xhi, a, e0, e1);
+            bytes = (e1 - e0) * (int)sizeof(E);
+        }
+        for (int o = 16; o; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+        if (w == 0 && lane == 0) s_any = bytes;
+        __syncthreads();
+        const bool staged = s_any <= kStageBytes;
+        if (tid == 0) {
+            rxidx[nlive] = staged ? r : (r | 0x40000000);
+            rxlh[2 * nlive] = lo;
+            rxlh[2 * nlive + 1] = hi;
+        }
+        ++nlive;
+        __syncthreads();
+    }
+    if (tid == 0) rec[0] = nlive;
+}
+
+// ---------------------------------------------------------------------------
+// the staged kernel (Tabbed, ntx <= kTxReg, sums over transmits per receive)
+// ---------------------------------------------------------------------------
+template <int KIND, int SUM, typename T>
+__global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_constant__ DasArgs a,
+                                                              const int *__restrict__ plan,
+                                                              int *status) {
+    using K = Kind<KIND, T>;
+    using E = typename StagedElem<KIND, T>::E;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned long long full[kStages];
+    __shared__ int2 stab[kStages][kTxReg];  // per stage and transmit: (element base, count)
+    __shared__ float s_txlh[2 * kTxReg];
+
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const long long tile = blockIdx.x;
+    const long long i = tile * kBlock + tid;
+    const bool valid = i < a.np;
+    const int f = blockIdx.y;
+    const int ntx = a.ntx, nrx = a.nrx;
+    const long long np = a.np;
+    const int *rec = plan + kPlanHeaderWords + tile * plan_tile_words(ntx, nrx);
+    const int nlive = __ldg(rec);
+    const int *rxidx = rec + 1;
+    const float *rxlh = reinterpret_cast<const float *>(rec + 1 + nrx);
+    const float *txlh = rxlh + 2 * nrx;
+    const long long frame_ch = (long long)f * ntx * nrx;
+    const long long chs = (long long)nrx * a.nt;
+    const long long op = valid ? (a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i) : 0;
+
+    if (tid < kStages) mbar_init(&full[tid], 1);
+    if (tid < 2 * ntx) s_txlh[tid] = __ldg(txlh + tid);
+    mbar_fence_init();
+    __syncthreads();
+
+    // producer: warp 0 stages the windows of live receive `it` into slot it % kStages
+    auto produce = [&](int it) {
+        const int slot = it % kStages;
+        const int code = __ldg(rxidx + it);
+        bool staged = !(code & 0x40000000);
+        const int r = code & 0x3fffffff;
+        int e0 = 0, e1 = 0;
+        if (staged && lane < ntx) {
+            const float xlo = __fadd_rn(s_txlh[2 * lane], __ldg(rxlh + 2 * it));
+            const float xhi = __fadd_rn(s_txlh[2 * lane + 1], __ldg(rxlh + 2 * it + 1));
+            staged_window<KIND, T>(xlo, xhi, a, e0, e1);
+        }
+        const int cnt = e1 - e0;
+        int off = cnt;  // inclusive scan of counts over lanes
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, off, o);
+            if (lane >= o) off += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, off, 31);
+        off -= cnt;
+        // the plan sized these windows to fit; a plan from other tables could
+        // not, and then this receive is gathered from global memory instead
+        if ((long long)total * (long long)sizeof(E) > kStageBytes) staged = false;
+        if (lane < ntx) stab[slot][lane] = make_int2(staged ? off - e0 : 0, staged ? cnt : -1);
+        __syncwarp();
+        if (lane == 0) mbar_arrive_expect_tx(&full[slot], staged ? (unsigned)(total * sizeof(E)) : 0u);
+        __syncwarp();
+        if (staged && cnt > 0) {
+            const E *src = static_cast<const E *>(a.data) + (frame_ch + (long long)lane * nrx + r) * a.nt + e0;
+            E *dst = reinterpret_cast<E *>(smem_raw + (size_t)slot * kStageBytes) + off;
+            tma_bulk_load(dst, src, (unsigned)(cnt * sizeof(E)), &full[slot]);
+        }
+    };
+    if (w == 0)
+        for (int it = 0; it < kStages && it < nlive; ++it) produce(it);
+
+    // transmit side of this pixel
+    float rtau[kTxReg], rapod[kTxReg];
+    float amax = 0.f;
+#pragma unroll
+    for (int k = 0; k < kTxReg; ++k) {
+        rtau[k] = 0.f;
+        rapod[k] = 0.f;
+        if (k < ntx && valid) {
+            rtau[k] = __ldg(a.tautx + (long long)k * np + i);
+            rapod[k] = __ldg(a.apodtx + (long long)k * np + i);
+            amax = fmaxf(amax, fabsf(rapod[k]));
+        }
+    }
+
+    float acc = 0.f, s1 = 0.f;
+    bool failed = false;
+    int fail_it = 0;
+    float trx_n = 0.f, arx_n = 0.f;
+    auto rx_load = [&](int it, float &trx, float &arx) {
+        const int r = __ldg(rxidx + it) & 0x3fffffff;
+        trx = valid ? __ldg(a.taurx + (long long)r * np + i) : 0.f;
+        arx = valid ? __ldg(a.apodrx + (long long)r * np + i) : 0.f;
+    };
+    if (nlive > 0) rx_load(0, trx_n, arx_n);
+
+    for (int it = 0; it < nlive; ++it) {
+        const int slot = it % kStages;
+        const unsigned parity = (unsigned)(it / kStages) & 1u;
+        const int code = __ldg(rxidx + it);
+        const int r = code & 0x3fffffff;
+        const float trx = trx_n, arx = arx_n;
+        if (it + 1 < nlive) rx_load(it + 1, trx_n, arx_n);
+        if (!mbar_wait_bounded(&full[slot], parity)) failed = true;
+
+        const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh);
+        float accr = 0.f;
+        if (live && !failed) {
+            const long long ch0 = (frame_ch + r) * a.nt;
+            const E *stage = reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes);
+            constexpr unsigned cap = kStageBytes / sizeof(E);
+#pragma unroll
+            for (int g = 0; g < kTxReg; g += kGroup) {
+                if (g < ntx) {
+                    const int nk = min(kGroup, ntx - g);
+                    float xs[kGroup], ap[kGroup];
+                    int ix[kGroup];
+                    unsigned hit = 0u, fix = 0u;
+#pragma unroll
+                    for (int k = 0; k < kGroup; ++k) {
+                        xs[k] = 0.f;
+                        ap[k] = 0.f;
+                        ix[k] = 0;
+                        if (k < nk) {
+                            const float x = __fadd_rn(rtau[g + k], trx);
+                            const float apod = __fmul_rn(rapod[g + k], arx);
+                            bool fx;
+                            int idx;
+                            const bool inr = K::index(x, a, idx, fx);
+                            const bool h = fabsf(apod) >= a.thresh;
+                            xs[k] = x;
+                            ap[k] = apod;
+                            ix[k] = idx;
+                            hit |= (unsigned)(h && inr) << k;
+                            fix |= (unsigned)(h && fx) << k;
+                        }
+                    }
+                    if (fix) {
+#pragma unroll
+                        for (int k = 0; k < kGroup; ++k) {
+                            if ((fix >> k) & 1u) {
+                                int idx;
+                                const bool inr = K::index_exact(xs[k], a, idx);
+                                ix[k] = idx;
+                                hit = inr ? (hit | (1u << k)) : (hit & ~(1u << k));
+                            }
+                        }
+                    }
+                    typename K::P pv[kGroup];
+#pragma unroll
+                    for (int k = 0; k < kGroup; ++k) {
+                        if ((hit >> k) & 1u) {
+                            const int2 st = stab[slot][g + k];
+                            if (st.y >= 0) {
+                                pv[k] = staged_load<KIND, T>(stage, st.x, ix[k], cap, a);
+                            } else {
+                                pv[k] = K::load(a.data, ch0 + (long long)(g + k) * chs, ix[k], a);
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < kGroup; ++k)
+                        if ((hit >> k) & 1u) accr = fmaf(ap[k], K::value(pv[k], xs[k], ix[k], a), accr);
+                }
+            }
+        }
+        if (SUM == PYCBF_GB_SUM_TX_AND_RX) acc += accr;
+        if (SUM == PYCBF_GB_SUM_TX_ONLY && valid) a.out[((long long)f * nrx + r) * np + op] = accr;
+        if (SUM == PYCBF_GB_SUM_DMAS_SSR || SUM == PYCBF_GB_SUM_DMAS_POWER) {
+            const float s = (SUM == PYCBF_GB_SUM_DMAS_SSR) ? copysignf(sqrtf(fabsf(accr)), accr) : accr;
+            acc = fmaf(s, s1, acc);
+            s1 += s;
+        }
+        // all warps are done with this slot (and agree on whether a wait ran out)
+        if (__syncthreads_or(failed)) {
+            failed = true;
+            fail_it = it;
+            break;
+        }
+        if (w == 0 && it + kStages < nlive) produce(it + kStages);
+    }
+
+    if (failed) {
+        // drain the copies still in flight before the CTA's shared memory goes away
+        if (tid == 0) {
+            if (status) atomicExch(status, 1);
+            // the phases issued for iterations fail_it .. fail_it + kStages - 1
+            const int issued = min(nlive, fail_it + kStages);
+            for (int j = fail_it; j < issued; ++j)
+                (void)mbar_wait_bounded(&full[j % kStages], (unsigned)(j / kStages) & 1u);
+        }
+        __syncthreads();
+        if (valid) {
+            const float nan = __int_as_float(0x7fc00000);
+            if (SUM == PYCBF_GB_SUM_TX_ONLY)
+                for (int r = 0; r < nrx; ++r) a.out[((long long)f * nrx + r) * np + op] = nan;
+            else
+                a.out[(long long)f * np + op] = nan;
+        }
+        return;
+    }
+    if (valid && SUM != PYCBF_GB_SUM_TX_ONLY) a.out[(long long)f * np + op] = acc;
+}
+
+template <int KIND, typename T>
+cudaError_t launch_plan_one(const DasArgs &a, int *plan, cudaStream_t s) {
+    const long long tiles = (a.np + kBlock - 1) / kBlock;
+    tabbed_plan_kernel<KIND, T><<<(unsigned)tiles, kBlock, 0, s>>>(a, plan);
+    return cudaGetLastError();
+}
+
+template <int KIND, int SUM, typename T>
+cudaError_t launch_staged_one(const DasArgs &a, const int *plan, int *status, cudaStream_t s) {
+    auto kern = das_staged_kernel<KIND, SUM, T>;
+    const int smem = kStages * kStageBytes;
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (err != cudaSuccess) return err;
+    const long long tiles = (a.np + kBlock - 1) / kBlock;
+    kern<<<dim3((unsigned)tiles, (unsigned)a.nframes), kBlock, smem, s>>>(a, plan, status);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_plan_type(const DasArgs &a, int interp, int *plan, cudaStream_t s) {
+    switch (interp) {
+        case PYCBF_GB_INTERP_CUBIC: return launch_plan_one<PYCBF_GB_INTERP_CUBIC, T>(a, plan, s);
+        case PYCBF_GB_INTERP_LINEAR: return launch_plan_one<PYCBF_GB_INTERP_LINEAR, T>(a, plan, s);
+        case PYCBF_GB_INTERP_NEAREST: return launch_plan_one<PYCBF_GB_INTERP_NEAREST, T>(a, plan, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int KIND, typename T>
+cudaError_t launch_staged_kind(const DasArgs &a, int sum, const int *plan, int *status, cudaStream_t s) {
+    switch (sum) {
+        case PYCBF_GB_SUM_TX_AND_RX: return launch_staged_one<KIND, PYCBF_GB_SUM_TX_AND_RX, T>(a, plan, status, s);
+        case PYCBF_GB_SUM_TX_ONLY: return launch_staged_one<KIND, PYCBF_GB_SUM_TX_ONLY, T>(a, plan, status, s);
+        case PYCBF_GB_SUM_DMAS_SSR: return launch_staged_one<KIND, PYCBF_GB_SUM_DMAS_SSR, T>(a, plan, status, s);
+        case PYCBF_GB_SUM_DMAS_POWER: return launch_staged_one<KIND, PYCBF_GB_SUM_DMAS_POWER, T>(a, plan, status, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <typename T>
+cudaError_t launch_staged_type(const DasArgs &a, int interp, int sum, const int *plan, int *status,
+                               cudaStream_t s) {
+    switch (interp) {
+        case PYCBF_GB_INTERP_CUBIC: return launch_staged_kind<PYCBF_GB_INTERP_CUBIC, T>(a, sum, plan, status, s);
+        case PYCBF_GB_INTERP_LINEAR: return launch_staged_kind<PYCBF_GB_INTERP_LINEAR, T>(a, sum, plan, status, s);
+        case PYCBF_GB_INTERP_NEAREST: return launch_staged_kind<PYCBF_GB_INTERP_NEAREST, T>(a, sum, plan, status, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace pgb

@@ -1,11 +1,21 @@
-// Instantiations of the delay-and-sum kernels: tabbed geometry, f16 channel data.
-// (Split per geometry and storage type so the library's files compile in parallel.)
-#include "das_impl.cuh"
+// Instantiations of the Tabbed delay-and-sum kernels (generic and TMA-staged) and
+// of the staging plan for f16 channel data.  Split per storage type so the
+// library's files compile in parallel.
+#include "das_staged.cuh"
 
 namespace pgb {
 
 cudaError_t launch_das_tabbed_f16(const DasArgs &a, int interp, int sum, bool census, cudaStream_t s) {
     return launch_das_geom_type<GEOM_TABBED, __half>(a, interp, sum, census, s);
+}
+
+cudaError_t launch_plan_f16(const DasArgs &a, int interp, int *plan, cudaStream_t s) {
+    return launch_plan_type<__half>(a, interp, plan, s);
+}
+
+cudaError_t launch_staged_f16(const DasArgs &a, int interp, int sum, const int *plan, int *status,
+                               cudaStream_t s) {
+    return launch_staged_type<__half>(a, interp, sum, plan, status, s);
 }
 
 }  // namespace pgb

@@ -67,8 +67,8 @@ def test_tabbed_rejects_bad_rfinfo(bad, code):
     L = _lib.load()
     info = _info(**bad)
     p = ct.c_void_p(16)  # never dereferenced: validation fails first
-    st = L.pycbf_gb_das_tabbed(ct.byref(info), p, p, p, p, p, 10, None, 2, 0.01, 3, p, p, 1 << 20,
-                               None)
+    st = L.pycbf_gb_das_tabbed(ct.byref(info), p, p, p, p, p, 10, None, 2, 0.01, 3, None, p, p,
+                               1 << 20, None)
     assert st == code
 
 
@@ -78,7 +78,7 @@ def test_tabbed_rejects_null_and_codes():
     p = ct.c_void_p(16)
     call = lambda **kw: L.pycbf_gb_das_tabbed(
         ct.byref(info), kw.get("rf", p), p, p, p, p, kw.get("np", 10), None, kw.get("interp", 2),
-        kw.get("thresh", 0.01), kw.get("sum", 3), kw.get("out", p), kw.get("ws", p),
+        kw.get("thresh", 0.01), kw.get("sum", 3), None, kw.get("out", p), kw.get("ws", p),
         kw.get("wsb", 1 << 20), None)
     assert call(rf=None) == _lib.EINVAL
     assert call(out=None) == _lib.EINVAL
@@ -90,6 +90,22 @@ def test_tabbed_rejects_null_and_codes():
     assert call(ws=None) == _lib.EWORKSPACE
     assert call(wsb=100) == _lib.EWORKSPACE
     assert call(ws=ct.c_void_p(8)) == _lib.EINVAL  # misaligned workspace
+
+
+def test_plan_validation():
+    L = _lib.load()
+    info = _info()
+    p = ct.c_void_p(16)
+    assert L.pycbf_gb_tabbed_plan_bytes(1000, 11, 128) == 4 * (4 + 8 * (1 + 128 * 3 + 22))
+    assert L.pycbf_gb_tabbed_plan_bytes(0, 11, 128) == 0
+    call = lambda **kw: L.pycbf_gb_tabbed_plan(
+        ct.byref(kw.get("info", info)), p, p, p, p, kw.get("np", 10), kw.get("interp", 2), 0.01,
+        kw.get("plan", p), kw.get("nb", 1 << 20), None)
+    assert call(plan=None) == _lib.EINVAL
+    assert call(interp=3) == _lib.EINVAL
+    assert call(nb=8) == _lib.EWORKSPACE
+    assert call(plan=ct.c_void_p(20)) == _lib.EWORKSPACE
+    assert call(info=_info(ntx=13)) == _lib.EUNSUPPORTED
 
 
 def test_synthetic_and_coherence_validation():
