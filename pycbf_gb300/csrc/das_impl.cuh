@@ -38,9 +38,8 @@ __device__ __forceinline__ int small_int(float fl) {
 // xhi = t0 + dt*(j+1), xlo = t0 + dt*j, a = (xhi - x)/dt, b = (x - xlo)/dt.
 // x carries ~q*2^-24 of rounding relative to dt, so deriving b from the
 // quotient instead would differ from the reference by that much.
-__device__ __forceinline__ void knot_fractions(float x, int j, const DasArgs &a, float &am,
+__device__ __forceinline__ void knot_fractions(float x, float fj, const DasArgs &a, float &am,
                                                float &b) {
-    const float fj = (float)j;
     const float xlo = __fadd_rn(a.t0, __fmul_rn(a.dt, fj));
     const float xhi = __fadd_rn(a.t0, __fmul_rn(a.dt, __fadd_rn(fj, 1.0f)));
     am = __fmul_rn(__fsub_rn(xhi, x), a.inv_dt);
@@ -78,9 +77,10 @@ template <typename T> struct Kind<PYCBF_GB_INTERP_CUBIC, T> {
         using rec = typename CoefRec<T>::raw;
         return CoefRec<T>::load(static_cast<const rec *>(data) + ch + idx);
     }
-    static __device__ __forceinline__ float value(const P &c, float x, int j, const DasArgs &a) {
+    // fj: the knot index as a float (exact: j < 2^23)
+    static __device__ __forceinline__ float value(const P &c, float x, float fj, const DasArgs &a) {
         float am, b;
-        knot_fractions(x, j, a, am, b);
+        knot_fractions(x, fj, a, am, b);
         const float wa = fmaf(am * am, am, -am);
         const float wb = fmaf(b * b, b, -b);
         return fmaf(am, c.x, fmaf(b, c.y, fmaf(wa, c.z, wb * c.w)));
@@ -100,9 +100,9 @@ template <typename T> struct Kind<PYCBF_GB_INTERP_LINEAR, T> {
         const T *y = static_cast<const T *>(data) + ch;
         return make_float2(load_sample(y + idx), idx + 1 < a.nt ? load_sample(y + idx + 1) : 0.f);
     }
-    static __device__ __forceinline__ float value(const P &c, float x, int j, const DasArgs &a) {
+    static __device__ __forceinline__ float value(const P &c, float x, float fj, const DasArgs &a) {
         float am, b;
-        knot_fractions(x, j, a, am, b);
+        knot_fractions(x, fj, a, am, b);
         return fmaf(am, c.x, b * c.y);
     }
 };
@@ -126,7 +126,7 @@ template <typename T> struct Kind<PYCBF_GB_INTERP_NEAREST, T> {
                                             const DasArgs &a) {
         return load_sample(static_cast<const T *>(data) + ch + idx);
     }
-    static __device__ __forceinline__ float value(const P &c, float, int, const DasArgs &) {
+    static __device__ __forceinline__ float value(const P &c, float, float, const DasArgs &) {
         return c;
     }
 };
@@ -157,10 +157,10 @@ template <typename T> struct Kind<PYCBF_GB_INTERP_LINEAR_FLOOR, T> {
                                             const DasArgs &a) {
         return load_sample(static_cast<const T *>(data) + ch + idx);
     }
-    static __device__ __forceinline__ float value(const P &v, float x, int ixo, const DasArgs &a) {
+    static __device__ __forceinline__ float value(const P &v, float x, float fixo, const DasArgs &a) {
         if (x == a.xend) return v;
         const float frac =
-            __fdiv_rn(__fsub_rn(__fsub_rn(x, __fmul_rn((float)ixo, a.dt)), a.t0), a.dt);
+            __fdiv_rn(__fsub_rn(__fsub_rn(x, __fmul_rn(fixo, a.dt)), a.t0), a.dt);
         return __fadd_rn(__fmul_rn(v, __fsub_rn(1.0f, frac)), __fmul_rn(v, frac));
     }
 };
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ 
                     float c = 0.f;
                     if ((hit >> k) & 1u) {
                         if (!CENSUS) {
-                            const float v = K::value(pv[k], xs[k], ix[k], a);
+                            const float v = K::value(pv[k], xs[k], (float)ix[k], a);
                             if (kPerTap) c = (GEOM == GEOM_TABBED) ? ap[k] * v : v;
                             else accr = fmaf(ap[k], v, accr);
                         } else {

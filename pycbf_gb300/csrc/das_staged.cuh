@@ -25,7 +25,7 @@ namespace pgb {
 
 constexpr int kStages = 4;
 constexpr int kStageBytes = 12 * 1024;
-constexpr unsigned kWaitLimit = 1u << 20;
+constexpr unsigned kWaitLimit = 1u << 24;
 
 // plan layout (int32 words): [0] status, [1] reserved, [2..3] pad, then per
 // tile a record of plan_tile_words(ntx, nrx) words:
@@ -50,6 +50,9 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, u
                  "r"(bytes)
                  : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
     unsigned ok;
     asm volatile(
@@ -60,9 +63,15 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned 
         : "memory");
     return ok != 0;
 }
+// Bounded wait: gives up after kWaitLimit polls or ~1 s of SM clock (2^31
+// cycles at ~2 GHz), whichever comes first.
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity) {
-    for (unsigned it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    for (unsigned it = 0; it < kWaitLimit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
+        if (clock64() - t0 > (1LL << 31)) break;
+    }
     return false;
 }
 // 1-D bulk copy global -> shared (both 16-byte aligned, bytes a multiple of 16)
@@ -228,17 +237,36 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
 
 // ---------------------------------------------------------------------------
 // the staged kernel (Tabbed, ntx <= kTxReg, sums over transmits per receive)
+//
+// Per receive and transmit group (4 taps, transmits padded with zero weights)
+// the inner loop has no data-dependent branch: indices are computed for all
+// taps, the gathers read shared memory at clamped indices (always inside the
+// stage), and a tap is added only where it contributes, by a select.  The
+// exact-quotient redo runs only when some tap of the group is within eps of a
+// rounding boundary.
+//
+// Ring protocol: full[s] completes when the copies of a stage land (one arrive
+// with the byte count); empty[s] completes when all warps are done with it.
+// Warp 0 refills the slot of iteration it-1 at the end of iteration it, so it
+// waits only for warps that are a whole receive behind.
 // ---------------------------------------------------------------------------
+constexpr int kTapGroup = 4;
+
 template <int KIND, int SUM, typename T>
 __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_constant__ DasArgs a,
                                                               const int *__restrict__ plan,
                                                               int *status) {
     using K = Kind<KIND, T>;
     using E = typename StagedElem<KIND, T>::E;
+    constexpr int kWarps = kBlock / 32;
+    constexpr unsigned cap = kStageBytes / sizeof(E);
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long full[kStages];
-    __shared__ int2 stab[kStages][kTxReg];  // per stage and transmit: (element base, count)
+    __shared__ __align__(8) unsigned long long empty[kStages];
+    __shared__ __align__(16) int sbase[kStages][kTxReg];  // element base of each window - its e0
+    __shared__ int sstaged[kStages];
     __shared__ float s_txlh[2 * kTxReg];
+    __shared__ int s_failed;
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const long long tile = blockIdx.x;
@@ -256,12 +284,16 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     const long long chs = (long long)nrx * a.nt;
     const long long op = valid ? (a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i) : 0;
 
-    if (tid < kStages) mbar_init(&full[tid], 1);
+    if (tid < kStages) {
+        mbar_init(&full[tid], 1);
+        mbar_init(&empty[tid], kWarps);
+    }
     if (tid < 2 * ntx) s_txlh[tid] = __ldg(txlh + tid);
+    if (tid == 0) s_failed = 0;
     mbar_fence_init();
     __syncthreads();
 
-    // producer: warp 0 stages the windows of live receive `it` into slot it % kStages
+    // producer (warp 0): windows of live receive `it` into slot it % kStages
     auto produce = [&](int it) {
         const int slot = it % kStages;
         const int code = __ldg(rxidx + it);
@@ -274,7 +306,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             staged_window<KIND, T>(xlo, xhi, a, e0, e1);
         }
         const int cnt = e1 - e0;
-        int off = cnt;  // inclusive scan of counts over lanes
+        int off = cnt;
         for (int o = 1; o < 32; o <<= 1) {
             const int v = __shfl_up_sync(0xffffffffu, off, o);
             if (lane >= o) off += v;
@@ -284,25 +316,27 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         // the plan sized these windows to fit; a plan from other tables could
         // not, and then this receive is gathered from global memory instead
         if ((long long)total * (long long)sizeof(E) > kStageBytes) staged = false;
-        if (lane < ntx) stab[slot][lane] = make_int2(staged ? off - e0 : 0, staged ? cnt : -1);
+        if (lane < kTxReg) sbase[slot][lane] = (staged && lane < ntx) ? off - e0 : 0;
+        if (lane == 0) sstaged[slot] = staged ? 1 : 0;
         __syncwarp();
         if (lane == 0) mbar_arrive_expect_tx(&full[slot], staged ? (unsigned)(total * sizeof(E)) : 0u);
         __syncwarp();
-        if (staged && cnt > 0) {
+        if (staged && lane < ntx && cnt > 0) {
             const E *src = static_cast<const E *>(a.data) + (frame_ch + (long long)lane * nrx + r) * a.nt + e0;
             E *dst = reinterpret_cast<E *>(smem_raw + (size_t)slot * kStageBytes) + off;
             tma_bulk_load(dst, src, (unsigned)(cnt * sizeof(E)), &full[slot]);
         }
     };
+    int produced = 0;  // iterations warp 0 has issued copies for
     if (w == 0)
-        for (int it = 0; it < kStages && it < nlive; ++it) produce(it);
+        for (int it = 0; it < kStages && it < nlive; ++it) produce(it), produced = it + 1;
 
-    // transmit side of this pixel
+    // transmit side of this pixel; slots past ntx carry zero weights
     float rtau[kTxReg], rapod[kTxReg];
     float amax = 0.f;
 #pragma unroll
     for (int k = 0; k < kTxReg; ++k) {
-        rtau[k] = 0.f;
+        rtau[k] = a.t0;
         rapod[k] = 0.f;
         if (k < ntx && valid) {
             rtau[k] = __ldg(a.tautx + (long long)k * np + i);
@@ -313,7 +347,6 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
 
     float acc = 0.f, s1 = 0.f;
     bool failed = false;
-    int fail_it = 0;
     float trx_n = 0.f, arx_n = 0.f;
     auto rx_load = [&](int it, float &trx, float &arx) {
         const int r = __ldg(rxidx + it) & 0x3fffffff;
@@ -324,71 +357,79 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
 
     for (int it = 0; it < nlive; ++it) {
         const int slot = it % kStages;
-        const unsigned parity = (unsigned)(it / kStages) & 1u;
-        const int code = __ldg(rxidx + it);
-        const int r = code & 0x3fffffff;
+        const int r = __ldg(rxidx + it) & 0x3fffffff;
         const float trx = trx_n, arx = arx_n;
         if (it + 1 < nlive) rx_load(it + 1, trx_n, arx_n);
-        if (!mbar_wait_bounded(&full[slot], parity)) failed = true;
+        if (!mbar_wait_bounded(&full[slot], (unsigned)(it / kStages) & 1u)) failed = true;
+        if (failed || *(volatile int *)&s_failed) {
+            failed = true;
+            s_failed = 1;
+            break;
+        }
 
         const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh);
         float accr = 0.f;
-        if (live && !failed) {
-            const long long ch0 = (frame_ch + r) * a.nt;
+        if (live) {
             const E *stage = reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes);
-            constexpr unsigned cap = kStageBytes / sizeof(E);
+            const bool staged = sstaged[slot] != 0;
+            const long long ch0 = (frame_ch + r) * a.nt;
 #pragma unroll
-            for (int g = 0; g < kTxReg; g += kGroup) {
+            for (int g = 0; g < kTxReg; g += kTapGroup) {
                 if (g < ntx) {
-                    const int nk = min(kGroup, ntx - g);
-                    float xs[kGroup], ap[kGroup];
-                    int ix[kGroup];
-                    unsigned hit = 0u, fix = 0u;
+                    const int4 base = *reinterpret_cast<const int4 *>(&sbase[slot][g]);
+                    const int bk[kTapGroup] = {base.x, base.y, base.z, base.w};
+                    float xs[kTapGroup], ap[kTapGroup], fl[kTapGroup];
+                    bool ok[kTapGroup];
+                    bool nearb = false;
 #pragma unroll
-                    for (int k = 0; k < kGroup; ++k) {
-                        xs[k] = 0.f;
-                        ap[k] = 0.f;
-                        ix[k] = 0;
-                        if (k < nk) {
-                            const float x = __fadd_rn(rtau[g + k], trx);
-                            const float apod = __fmul_rn(rapod[g + k], arx);
-                            bool fx;
-                            int idx;
-                            const bool inr = K::index(x, a, idx, fx);
-                            const bool h = fabsf(apod) >= a.thresh;
-                            xs[k] = x;
-                            ap[k] = apod;
-                            ix[k] = idx;
-                            hit |= (unsigned)(h && inr) << k;
-                            fix |= (unsigned)(h && fx) << k;
+                    for (int k = 0; k < kTapGroup; ++k) {
+                        const float x = __fadd_rn(rtau[g + k], trx);
+                        const float apod = __fmul_rn(rapod[g + k], arx);
+                        const float q = __fmul_rn(__fsub_rn(x, a.t0), a.inv_dt);
+                        float flk;
+                        bool inr;
+                        if (KIND == PYCBF_GB_INTERP_NEAREST) {
+                            flk = truncf(q + 0.5f);
+                            inr = (x == x) && (flk >= 0.f) && (flk < (float)a.nt);
+                            const float fr = q - floorf(q);
+                            nearb |= fabsf(fr - 0.5f) < a.eps;
+                        } else {
+                            flk = floorf(q);
+                            inr = (x >= a.t0) && (x <= a.xmax);
+                            nearb |= fabsf(q - flk - 0.5f) > 0.5f - a.eps;
                         }
+                        xs[k] = x;
+                        ap[k] = apod;
+                        fl[k] = flk;
+                        ok[k] = inr && (fabsf(apod) >= a.thresh);
                     }
-                    if (fix) {
+                    if (nearb) {  // rare: redo the quotients with the IEEE division
 #pragma unroll
-                        for (int k = 0; k < kGroup; ++k) {
-                            if ((fix >> k) & 1u) {
-                                int idx;
-                                const bool inr = K::index_exact(xs[k], a, idx);
-                                ix[k] = idx;
-                                hit = inr ? (hit | (1u << k)) : (hit & ~(1u << k));
-                            }
-                        }
-                    }
-                    typename K::P pv[kGroup];
-#pragma unroll
-                    for (int k = 0; k < kGroup; ++k) {
-                        if ((hit >> k) & 1u) {
-                            const int2 st = stab[slot][g + k];
-                            if (st.y >= 0) {
-                                pv[k] = staged_load<KIND, T>(stage, st.x, ix[k], cap, a);
+                        for (int k = 0; k < kTapGroup; ++k) {
+                            const float qe = __fdiv_rn(__fsub_rn(xs[k], a.t0), a.dt);
+                            if (KIND == PYCBF_GB_INTERP_NEAREST) {
+                                fl[k] = truncf(qe + 0.5f);
+                                ok[k] = (xs[k] == xs[k]) && (fl[k] >= 0.f) && (fl[k] < (float)a.nt) &&
+                                        (fabsf(ap[k]) >= a.thresh);
                             } else {
-                                pv[k] = K::load(a.data, ch0 + (long long)(g + k) * chs, ix[k], a);
+                                fl[k] = floorf(qe);
                             }
                         }
                     }
+                    typename K::P pv[kTapGroup];
 #pragma unroll
-                    for (int k = 0; k < kGroup; ++k)
-                        if ((hit >> k) & 1u) accr = fmaf(ap[k], K::value(pv[k], xs[k], ix[k], a), accr);
+                    for (int k = 0; k < kTapGroup; ++k) {
+                        // knot / sample index; taps that do not contribute read a clamped
+                        // in-stage element and are dropped below
+                        const int j = min(max((int)fl[k], 0), a.nt - 1);
+                        if (staged) pv[k] = staged_load<KIND, T>(stage, bk[k], j, cap, a);
+                        else pv[k] = K::load(a.data, ch0 + (long long)(g + k) * chs, j, a);
+                    }
+#pragma unroll
+                    for (int k = 0; k < kTapGroup; ++k) {
+                        const float c = fmaf(ap[k], K::value(pv[k], xs[k], fl[k], a), accr);
+                        accr = ok[k] ? c : accr;
+                    }
                 }
             }
         }
@@ -399,22 +440,28 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             acc = fmaf(s, s1, acc);
             s1 += s;
         }
-        // all warps are done with this slot (and agree on whether a wait ran out)
-        if (__syncthreads_or(failed)) {
-            failed = true;
-            fail_it = it;
-            break;
+        // this warp is done with the slot
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[slot]);
+        // warp 0 refills the slot of the previous iteration once every warp left it
+        if (w == 0 && it >= 1 && it - 1 + kStages < nlive) {
+            const int pit = it - 1;
+            if (!mbar_wait_bounded(&empty[pit % kStages], (unsigned)(pit / kStages) & 1u)) {
+                failed = true;
+                s_failed = 1;
+                break;
+            }
+            produce(pit + kStages);
+            produced = pit + kStages + 1;
         }
-        if (w == 0 && it + kStages < nlive) produce(it + kStages);
     }
-
-    if (failed) {
-        // drain the copies still in flight before the CTA's shared memory goes away
+    __syncthreads();
+    if (s_failed) {
+        // drain the copies still in flight before the CTA's shared memory goes
+        // away: the latest phase of each slot is one of the last kStages issued
         if (tid == 0) {
             if (status) atomicExch(status, 1);
-            // the phases issued for iterations fail_it .. fail_it + kStages - 1
-            const int issued = min(nlive, fail_it + kStages);
-            for (int j = fail_it; j < issued; ++j)
+            for (int j = max(0, produced - kStages); j < produced; ++j)
                 (void)mbar_wait_bounded(&full[j % kStages], (unsigned)(j / kStages) & 1u);
         }
         __syncthreads();
