@@ -422,8 +422,11 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
                         // knot / sample index; taps that do not contribute read a clamped
                         // in-stage element and are dropped below
                         const int j = min(max((int)fl[k], 0), a.nt - 1);
+                        // padded transmit slots (g + k >= ntx) read the last real
+                        // channel: their weight is zero and the select drops them
+                        const int t = min(g + k, ntx - 1);
                         if (staged) pv[k] = staged_load<KIND, T>(stage, bk[k], j, cap, a);
-                        else pv[k] = K::load(a.data, ch0 + (long long)(g + k) * chs, j, a);
+                        else pv[k] = K::load(a.data, ch0 + (long long)t * chs, j, a);
                     }
 #pragma unroll
                     for (int k = 0; k < kTapGroup; ++k) {

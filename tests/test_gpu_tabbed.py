@@ -234,3 +234,24 @@ def test_staged_frames_and_half_storage(c1_small):
         a = bf_for(c1_small, "cubic", storage=storage)(frames)
         b = bf_for(c1_small, "cubic", storage=storage, stage_channels=False)(frames)
         np.testing.assert_array_equal(a, b)
+
+
+def test_staged_kernel_unstaged_receives():
+    """Delays spread over the whole record: no window fits a stage, so every
+    receive takes the kernel's global-gather path (with padded transmits)."""
+    rng = np.random.default_rng(5)
+    ntx, nrx, nt, npx = 11, 24, 2048, 640
+    dt = np.float32(4e-8)
+    case = dict(tautx=rng.uniform(0, nt * dt * 0.5, (ntx, npx)).astype(np.float32),
+                taurx=rng.uniform(0, nt * dt * 0.5, (nrx, npx)).astype(np.float32),
+                apodtx=rng.uniform(0.5, 1, (ntx, npx)).astype(np.float32),
+                apodrx=rng.uniform(-1, 1, (nrx, npx)).astype(np.float32),
+                t0=np.float32(0), dt=dt, nt=nt)
+    frames = rng.normal(size=(3, ntx, nrx, nt)).astype(np.float32)
+    for kind in ("cubic", "nearest", "linear"):
+        a = bf_for(case, kind, pixel_order="natural")(frames)
+        b = bf_for(case, kind, pixel_order="natural", stage_channels=False)(frames)
+        np.testing.assert_array_equal(a, b)
+    ref = oracle.das_tabbed(frames[2], case["tautx"], case["apodtx"], case["taurx"],
+                            case["apodrx"], 0.0, float(dt), nt)
+    assert_image_close(bf_for(case, "cubic")(frames)[2], ref, what="unstaged")
