@@ -25,7 +25,7 @@ namespace pgb {
 
 constexpr int kStages = 4;
 constexpr int kStageBytes = 12 * 1024;
-constexpr unsigned kWaitLimit = 1u << 24;
+constexpr unsigned kWaitLimit = 1u << 16;
 
 // plan layout (int32 words): [0] status, [1] reserved, [2..3] pad, then per
 // tile a record of plan_tile_words(ntx, nrx) words:
@@ -53,13 +53,14 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, u
 __device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
+// try_wait suspends the thread until the phase completes or ~hint ns pass
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
     unsigned ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
         " selp.u32 %0, 1, 0, p;\n}"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(1000000u)
         : "memory");
     return ok != 0;
 }
@@ -252,14 +253,85 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
 // ---------------------------------------------------------------------------
 constexpr int kTapGroup = 4;
 
+// One group of kTapGroup taps of receive (trx, arx): index, gather, weight,
+// accumulate.  STAGED gathers from the shared-memory stage at clamped
+// indices, otherwise from global memory.  A tap whose quotient lies within
+// a few ulp of a rounding boundary has its index redone with the IEEE
+// division; the group branches only when some tap needs it.
+template <int KIND, typename T, bool STAGED>
+__device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt, const float *at,
+                                              float trx, float arx, const int *bk,
+                                              const typename StagedElem<KIND, T>::E *stage,
+                                              long long ch_first, long long chs, int g, int ntx,
+                                              float accr) {
+    using K = Kind<KIND, T>;
+    constexpr unsigned cap = kStageBytes / sizeof(typename StagedElem<KIND, T>::E);
+    float xs[kTapGroup], ap[kTapGroup], fl[kTapGroup];
+    bool ok[kTapGroup];
+    bool nearb = false;
+#pragma unroll
+    for (int k = 0; k < kTapGroup; ++k) {
+        const float x = __fadd_rn(tt[k], trx);
+        const float apod = __fmul_rn(at[k], arx);
+        const float q = __fmul_rn(__fsub_rn(x, a.t0), a.inv_dt);
+        // |q_fast - q_exact| <= 1.5 ulp(q) <= 1.5 |q| 2^-23; flag within |q| 2^-21
+        const float tol = fmaf(fabsf(q), 4.76837158e-7f, 1e-30f);
+        float flk;
+        bool inr;
+        if (KIND == PYCBF_GB_INTERP_NEAREST) {
+            flk = truncf(q + 0.5f);
+            inr = (x == x) && (flk >= 0.f) && (flk < (float)a.nt);
+            nearb |= fabsf(q - floorf(q) - 0.5f) < tol;
+        } else {
+            flk = floorf(q);
+            inr = (x >= a.t0) && (x <= a.xmax);
+            nearb |= (q - flk < tol) || (flk + 1.f - q < tol);
+        }
+        xs[k] = x;
+        ap[k] = apod;
+        fl[k] = flk;
+        ok[k] = inr && (fabsf(apod) >= a.thresh);
+    }
+    if (nearb) {
+#pragma unroll
+        for (int k = 0; k < kTapGroup; ++k) {
+            const float qe = __fdiv_rn(__fsub_rn(xs[k], a.t0), a.dt);
+            if (KIND == PYCBF_GB_INTERP_NEAREST) {
+                fl[k] = truncf(qe + 0.5f);
+                ok[k] = (xs[k] == xs[k]) && (fl[k] >= 0.f) && (fl[k] < (float)a.nt) &&
+                        (fabsf(ap[k]) >= a.thresh);
+            } else {
+                fl[k] = floorf(qe);
+            }
+        }
+    }
+    typename K::P pv[kTapGroup];
+#pragma unroll
+    for (int k = 0; k < kTapGroup; ++k) {
+        const int j = min(max((int)fl[k], 0), a.nt - 1);
+        if (STAGED) {
+            pv[k] = staged_load<KIND, T>(stage, bk[k], j, cap, a);
+        } else {
+            // padded transmit slots (g + k >= ntx) read the last real channel:
+            // their weight is zero and the select below drops them
+            const int t = min(g + k, ntx - 1);
+            pv[k] = K::load(a.data, ch_first + (long long)t * chs, j, a);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kTapGroup; ++k) {
+        const float c = fmaf(ap[k], K::value(pv[k], xs[k], fl[k], a), accr);
+        accr = ok[k] ? c : accr;
+    }
+    return accr;
+}
+
 template <int KIND, int SUM, typename T>
 __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_constant__ DasArgs a,
                                                               const int *__restrict__ plan,
                                                               int *status) {
-    using K = Kind<KIND, T>;
     using E = typename StagedElem<KIND, T>::E;
     constexpr int kWarps = kBlock / 32;
-    constexpr unsigned cap = kStageBytes / sizeof(E);
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long full[kStages];
     __shared__ __align__(8) unsigned long long empty[kStages];
@@ -267,6 +339,9 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     __shared__ int sstaged[kStages];
     __shared__ float s_txlh[2 * kTxReg];
     __shared__ int s_failed;
+    // the tile's plan: live receive indices and their delay bounds
+    int *s_rx = reinterpret_cast<int *>(smem_raw + kStages * kStageBytes);
+    float *s_rxlh = reinterpret_cast<float *>(s_rx + a.nrx);
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const long long tile = blockIdx.x;
@@ -277,9 +352,6 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     const long long np = a.np;
     const int *rec = plan + kPlanHeaderWords + tile * plan_tile_words(ntx, nrx);
     const int nlive = __ldg(rec);
-    const int *rxidx = rec + 1;
-    const float *rxlh = reinterpret_cast<const float *>(rec + 1 + nrx);
-    const float *txlh = rxlh + 2 * nrx;
     const long long frame_ch = (long long)f * ntx * nrx;
     const long long chs = (long long)nrx * a.nt;
     const long long op = valid ? (a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i) : 0;
@@ -288,7 +360,13 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         mbar_init(&full[tid], 1);
         mbar_init(&empty[tid], kWarps);
     }
-    if (tid < 2 * ntx) s_txlh[tid] = __ldg(txlh + tid);
+    {
+        const float *txlh = reinterpret_cast<const float *>(rec + 1 + 3 * nrx);
+        if (tid < 2 * ntx) s_txlh[tid] = __ldg(txlh + tid);
+        for (int k = tid; k < nlive; k += kBlock) s_rx[k] = __ldg(rec + 1 + k);
+        const float *rxlh = reinterpret_cast<const float *>(rec + 1 + nrx);
+        for (int k = tid; k < 2 * nlive; k += kBlock) s_rxlh[k] = __ldg(rxlh + k);
+    }
     if (tid == 0) s_failed = 0;
     mbar_fence_init();
     __syncthreads();
@@ -296,13 +374,13 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     // producer (warp 0): windows of live receive `it` into slot it % kStages
     auto produce = [&](int it) {
         const int slot = it % kStages;
-        const int code = __ldg(rxidx + it);
+        const int code = s_rx[it];
         bool staged = !(code & 0x40000000);
         const int r = code & 0x3fffffff;
         int e0 = 0, e1 = 0;
         if (staged && lane < ntx) {
-            const float xlo = __fadd_rn(s_txlh[2 * lane], __ldg(rxlh + 2 * it));
-            const float xhi = __fadd_rn(s_txlh[2 * lane + 1], __ldg(rxlh + 2 * it + 1));
+            const float xlo = __fadd_rn(s_txlh[2 * lane], s_rxlh[2 * it]);
+            const float xhi = __fadd_rn(s_txlh[2 * lane + 1], s_rxlh[2 * it + 1]);
             staged_window<KIND, T>(xlo, xhi, a, e0, e1);
         }
         const int cnt = e1 - e0;
@@ -347,19 +425,23 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
 
     float acc = 0.f, s1 = 0.f;
     bool failed = false;
-    float trx_n = 0.f, arx_n = 0.f;
+    // receive-side values, fetched two receives ahead
     auto rx_load = [&](int it, float &trx, float &arx) {
-        const int r = __ldg(rxidx + it) & 0x3fffffff;
+        const int r = s_rx[it] & 0x3fffffff;
         trx = valid ? __ldg(a.taurx + (long long)r * np + i) : 0.f;
         arx = valid ? __ldg(a.apodrx + (long long)r * np + i) : 0.f;
     };
-    if (nlive > 0) rx_load(0, trx_n, arx_n);
+    float trx1 = 0.f, arx1 = 0.f, trx2 = 0.f, arx2 = 0.f;
+    if (nlive > 0) rx_load(0, trx1, arx1);
+    if (nlive > 1) rx_load(1, trx2, arx2);
 
     for (int it = 0; it < nlive; ++it) {
         const int slot = it % kStages;
-        const int r = __ldg(rxidx + it) & 0x3fffffff;
-        const float trx = trx_n, arx = arx_n;
-        if (it + 1 < nlive) rx_load(it + 1, trx_n, arx_n);
+        const int r = s_rx[it] & 0x3fffffff;
+        const float trx = trx1, arx = arx1;
+        trx1 = trx2;
+        arx1 = arx2;
+        if (it + 2 < nlive) rx_load(it + 2, trx2, arx2);
         if (!mbar_wait_bounded(&full[slot], (unsigned)(it / kStages) & 1u)) failed = true;
         if (failed || *(volatile int *)&s_failed) {
             failed = true;
@@ -370,68 +452,25 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh);
         float accr = 0.f;
         if (live) {
-            const E *stage = reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes);
-            const bool staged = sstaged[slot] != 0;
-            const long long ch0 = (frame_ch + r) * a.nt;
+            const long long ch_first = (frame_ch + r) * a.nt;
+            if (sstaged[slot]) {
+                const E *stage = reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes);
 #pragma unroll
-            for (int g = 0; g < kTxReg; g += kTapGroup) {
-                if (g < ntx) {
-                    const int4 base = *reinterpret_cast<const int4 *>(&sbase[slot][g]);
-                    const int bk[kTapGroup] = {base.x, base.y, base.z, base.w};
-                    float xs[kTapGroup], ap[kTapGroup], fl[kTapGroup];
-                    bool ok[kTapGroup];
-                    bool nearb = false;
-#pragma unroll
-                    for (int k = 0; k < kTapGroup; ++k) {
-                        const float x = __fadd_rn(rtau[g + k], trx);
-                        const float apod = __fmul_rn(rapod[g + k], arx);
-                        const float q = __fmul_rn(__fsub_rn(x, a.t0), a.inv_dt);
-                        float flk;
-                        bool inr;
-                        if (KIND == PYCBF_GB_INTERP_NEAREST) {
-                            flk = truncf(q + 0.5f);
-                            inr = (x == x) && (flk >= 0.f) && (flk < (float)a.nt);
-                            const float fr = q - floorf(q);
-                            nearb |= fabsf(fr - 0.5f) < a.eps;
-                        } else {
-                            flk = floorf(q);
-                            inr = (x >= a.t0) && (x <= a.xmax);
-                            nearb |= fabsf(q - flk - 0.5f) > 0.5f - a.eps;
-                        }
-                        xs[k] = x;
-                        ap[k] = apod;
-                        fl[k] = flk;
-                        ok[k] = inr && (fabsf(apod) >= a.thresh);
+                for (int g = 0; g < kTxReg; g += kTapGroup) {
+                    if (g < ntx) {
+                        const int4 b = *reinterpret_cast<const int4 *>(&sbase[slot][g]);
+                        const int bk[kTapGroup] = {b.x, b.y, b.z, b.w};
+                        accr = staged_group<KIND, T, true>(a, rtau + g, rapod + g, trx, arx, bk,
+                                                           stage, ch_first, chs, g, ntx, accr);
                     }
-                    if (nearb) {  // rare: redo the quotients with the IEEE division
+                }
+            } else {
 #pragma unroll
-                        for (int k = 0; k < kTapGroup; ++k) {
-                            const float qe = __fdiv_rn(__fsub_rn(xs[k], a.t0), a.dt);
-                            if (KIND == PYCBF_GB_INTERP_NEAREST) {
-                                fl[k] = truncf(qe + 0.5f);
-                                ok[k] = (xs[k] == xs[k]) && (fl[k] >= 0.f) && (fl[k] < (float)a.nt) &&
-                                        (fabsf(ap[k]) >= a.thresh);
-                            } else {
-                                fl[k] = floorf(qe);
-                            }
-                        }
-                    }
-                    typename K::P pv[kTapGroup];
-#pragma unroll
-                    for (int k = 0; k < kTapGroup; ++k) {
-                        // knot / sample index; taps that do not contribute read a clamped
-                        // in-stage element and are dropped below
-                        const int j = min(max((int)fl[k], 0), a.nt - 1);
-                        // padded transmit slots (g + k >= ntx) read the last real
-                        // channel: their weight is zero and the select drops them
-                        const int t = min(g + k, ntx - 1);
-                        if (staged) pv[k] = staged_load<KIND, T>(stage, bk[k], j, cap, a);
-                        else pv[k] = K::load(a.data, ch0 + (long long)t * chs, j, a);
-                    }
-#pragma unroll
-                    for (int k = 0; k < kTapGroup; ++k) {
-                        const float c = fmaf(ap[k], K::value(pv[k], xs[k], fl[k], a), accr);
-                        accr = ok[k] ? c : accr;
+                for (int g = 0; g < kTxReg; g += kTapGroup) {
+                    if (g < ntx) {
+                        const int bk[kTapGroup] = {0, 0, 0, 0};
+                        accr = staged_group<KIND, T, false>(a, rtau + g, rapod + g, trx, arx, bk,
+                                                            nullptr, ch_first, chs, g, ntx, accr);
                     }
                 }
             }
@@ -480,6 +519,10 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     if (valid && SUM != PYCBF_GB_SUM_TX_ONLY) a.out[(long long)f * np + op] = acc;
 }
 
+inline size_t staged_smem_bytes(int nrx) {
+    return (size_t)kStages * kStageBytes + sizeof(int) * 3 * (size_t)nrx;
+}
+
 template <int KIND, typename T>
 cudaError_t launch_plan_one(const DasArgs &a, int *plan, cudaStream_t s) {
     const long long tiles = (a.np + kBlock - 1) / kBlock;
@@ -490,7 +533,7 @@ cudaError_t launch_plan_one(const DasArgs &a, int *plan, cudaStream_t s) {
 template <int KIND, int SUM, typename T>
 cudaError_t launch_staged_one(const DasArgs &a, const int *plan, int *status, cudaStream_t s) {
     auto kern = das_staged_kernel<KIND, SUM, T>;
-    const int smem = kStages * kStageBytes;
+    const int smem = (int)staged_smem_bytes(a.nrx);
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (err != cudaSuccess) return err;
     const long long tiles = (a.np + kBlock - 1) / kBlock;
