@@ -77,7 +77,7 @@ bool das_shape_ok(int geom, int sumtype, long long ntx) {
 // receive; its 16-byte bulk copies need channel strides and the data base
 // aligned to 16 bytes.
 bool staged_ok(const pycbf_gb_rfinfo *rf, int interp, int sumtype, const void *data) {
-    if (rf->ntx > 12 || rf->nrx > 4096 || interp > PYCBF_GB_INTERP_CUBIC) return false;
+    if (rf->ntx > 12 || rf->nrx > 512 || interp > PYCBF_GB_INTERP_CUBIC) return false;
     if (sumtype != PYCBF_GB_SUM_TX_ONLY && sumtype != PYCBF_GB_SUM_TX_AND_RX &&
         sumtype != PYCBF_GB_SUM_DMAS_SSR && sumtype != PYCBF_GB_SUM_DMAS_POWER)
         return false;

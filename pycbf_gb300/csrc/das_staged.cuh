@@ -27,12 +27,23 @@ constexpr int kStages = 4;
 constexpr int kStageBytes = 12 * 1024;
 constexpr unsigned kWaitLimit = 1u << 16;
 
+// A tile's work is a list of items: one receive and a run of whole transmit
+// groups (kTapGroup transmits each) whose windows fit one stage together; a
+// receive whose windows are too large for one stage becomes several items.
+constexpr int kTapGroup = 4;
+constexpr int kTxGroups = (kTxReg + kTapGroup - 1) / kTapGroup;
+// item code: receive (bits 0-15), first group (16-19), end group (20-23),
+// last item of its receive (bit 28), not staged (bit 30)
+constexpr int kItemLast = 1 << 28;
+constexpr int kItemUnstaged = 1 << 30;
+
 // plan layout (int32 words): [0] status, [1] reserved, [2..3] pad, then per
 // tile a record of plan_tile_words(ntx, nrx) words:
-//   nlive | rx index per live receive (nrx) | rx lo,hi per live receive (2*nrx floats)
-//   | tx lo,hi per transmit (2*ntx floats)
+//   nitems | item code (imax) | receive lo,hi delay per item (2*imax floats)
+//   | transmit lo,hi delay (2*ntx floats),  imax = nrx * kTxGroups
 __host__ __device__ inline long long plan_tile_words(int ntx, int nrx) {
-    return 1 + (long long)nrx + 2LL * nrx + 2LL * ntx;
+    const long long imax = (long long)nrx * kTxGroups;
+    return 1 + imax + 2 * imax + 2LL * ntx;
 }
 constexpr int kPlanHeaderWords = 4;
 
@@ -150,16 +161,16 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
                                                              int *plan) {
     using E = typename StagedElem<KIND, T>::E;
     __shared__ float red[3][kBlock / 32];
-    __shared__ int s_any;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const long long tile = blockIdx.x;
     const long long i = tile * kBlock + tid;
     const bool valid = i < a.np;
     const int ntx = a.ntx, nrx = a.nrx;
+    const long long imax = (long long)nrx * kTxGroups;
     int *rec = plan + kPlanHeaderWords + tile * plan_tile_words(ntx, nrx);
-    int *rxidx = rec + 1;
-    float *rxlh = reinterpret_cast<float *>(rec + 1 + nrx);
-    float *txlh = rxlh + 2 * nrx;
+    int *codes = rec + 1;
+    float *rxlh = reinterpret_cast<float *>(rec + 1 + imax);
+    float *txlh = rxlh + 2 * imax;
     const float inf = __int_as_float(0x7f800000);
 
     auto block_minmax = [&](float lo, float hi, int any, float &blo, float &bhi, int &bany) {
@@ -186,6 +197,7 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
     };
 
     float amax = 0.f;
+    float txl = 0.f, txh = 0.f;  // this thread's transmit bounds (tid < ntx)
     for (int t = 0; t < ntx; ++t) {
         float tau = inf, taun = -inf;
         if (valid) {
@@ -195,13 +207,16 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
         float lo, hi;
         int any;
         block_minmax(tau == tau ? tau : inf, taun == taun ? taun : -inf, 0, lo, hi, any);
+        if (tid == t) {
+            txl = lo;
+            txh = hi;
+        }
         if (tid == 0) {
             txlh[2 * t] = lo;
             txlh[2 * t + 1] = hi;
         }
     }
-    __syncthreads();
-    int nlive = 0;
+    int nitems = 0;
     for (int r = 0; r < nrx; ++r) {
         float trx = 0.f, arx = 0.f;
         if (valid) {
@@ -212,28 +227,38 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
         float lo, hi;
         int any;
         block_minmax(live ? trx : inf, live ? trx : -inf, live ? 1 : 0, lo, hi, any);
-        if (!any) continue;
-        // staged only if all windows of this receive fit one stage
-        int bytes = 0;
-        if (tid < ntx) {
-            const float xlo = __fadd_rn(txlh[2 * tid], lo), xhi = __fadd_rn(txlh[2 * tid + 1], hi);
-            int e0, e1;
-            staged_window<KIND, T>(xlo, xhi, a, e0, e1);
-            bytes = (e1 - e0) * (int)sizeof(E);
+        if (!any) continue;  // block-uniform
+        if (w == 0) {
+            // window bytes of this thread's transmit, summed per transmit group
+            int bytes = 0;
+            if (lane < ntx) {
+                int e0, e1;
+                staged_window<KIND, T>(__fadd_rn(txl, lo), __fadd_rn(txh, hi), a, e0, e1);
+                bytes = (e1 - e0) * (int)sizeof(E);
+            }
+            for (int o = 1; o < kTapGroup; o <<= 1) bytes += __shfl_down_sync(0xffffffffu, bytes, o);
+            int gb[kTxGroups];
+            for (int g = 0; g < kTxGroups; ++g) gb[g] = __shfl_sync(0xffffffffu, bytes, g * kTapGroup);
+            if (lane == 0) {
+                const int ng = (ntx + kTapGroup - 1) / kTapGroup;
+                int g0 = 0;
+                while (g0 < ng) {
+                    int g1 = g0 + 1, tot = gb[g0];
+                    while (g1 < ng && tot + gb[g1] <= kStageBytes) tot += gb[g1++];
+                    int code = r | (g0 << 16) | (g1 << 20);
+                    if (tot > kStageBytes) code |= kItemUnstaged;
+                    if (g1 == ng) code |= kItemLast;
+                    codes[nitems] = code;
+                    rxlh[2 * nitems] = lo;
+                    rxlh[2 * nitems + 1] = hi;
+                    ++nitems;
+                    g0 = g1;
+                }
+            }
+            nitems = __shfl_sync(0xffffffffu, nitems, 0);
         }
-        for (int o = 16; o; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
-        if (w == 0 && lane == 0) s_any = bytes;
-        __syncthreads();
-        const bool staged = s_any <= kStageBytes;
-        if (tid == 0) {
-            rxidx[nlive] = staged ? r : (r | 0x40000000);
-            rxlh[2 * nlive] = lo;
-            rxlh[2 * nlive + 1] = hi;
-        }
-        ++nlive;
-        __syncthreads();
     }
-    if (tid == 0) rec[0] = nlive;
+    if (tid == 0) rec[0] = nitems;
 }
 
 // ---------------------------------------------------------------------------
@@ -251,8 +276,6 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
 // Warp 0 refills the slot of iteration it-1 at the end of iteration it, so it
 // waits only for warps that are a whole receive behind.
 // ---------------------------------------------------------------------------
-constexpr int kTapGroup = 4;
-
 // One group of kTapGroup taps of receive (trx, arx): index, gather, weight,
 // accumulate.  STAGED gathers from the shared-memory stage at clamped
 // indices, otherwise from global memory.  A tap whose quotient lies within
@@ -339,9 +362,6 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     __shared__ int sstaged[kStages];
     __shared__ float s_txlh[2 * kTxReg];
     __shared__ int s_failed;
-    // the tile's plan: live receive indices and their delay bounds
-    int *s_rx = reinterpret_cast<int *>(smem_raw + kStages * kStageBytes);
-    float *s_rxlh = reinterpret_cast<float *>(s_rx + a.nrx);
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const long long tile = blockIdx.x;
@@ -350,35 +370,41 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     const int f = blockIdx.y;
     const int ntx = a.ntx, nrx = a.nrx;
     const long long np = a.np;
+    const long long imax = (long long)nrx * kTxGroups;
     const int *rec = plan + kPlanHeaderWords + tile * plan_tile_words(ntx, nrx);
-    const int nlive = __ldg(rec);
+    const int nitems = __ldg(rec);
     const long long frame_ch = (long long)f * ntx * nrx;
     const long long chs = (long long)nrx * a.nt;
     const long long op = valid ? (a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i) : 0;
+    // the tile's work items and their receive delay bounds, after the stages
+    int *s_code = reinterpret_cast<int *>(smem_raw + kStages * kStageBytes);
+    float *s_rxlh = reinterpret_cast<float *>(s_code + imax);
 
     if (tid < kStages) {
         mbar_init(&full[tid], 1);
         mbar_init(&empty[tid], kWarps);
     }
     {
-        const float *txlh = reinterpret_cast<const float *>(rec + 1 + 3 * nrx);
+        const float *txlh = reinterpret_cast<const float *>(rec + 1 + 3 * imax);
         if (tid < 2 * ntx) s_txlh[tid] = __ldg(txlh + tid);
-        for (int k = tid; k < nlive; k += kBlock) s_rx[k] = __ldg(rec + 1 + k);
-        const float *rxlh = reinterpret_cast<const float *>(rec + 1 + nrx);
-        for (int k = tid; k < 2 * nlive; k += kBlock) s_rxlh[k] = __ldg(rxlh + k);
+        for (int k = tid; k < nitems; k += kBlock) s_code[k] = __ldg(rec + 1 + k);
+        const float *rxlh = reinterpret_cast<const float *>(rec + 1 + imax);
+        for (int k = tid; k < 2 * nitems; k += kBlock) s_rxlh[k] = __ldg(rxlh + k);
     }
     if (tid == 0) s_failed = 0;
     mbar_fence_init();
     __syncthreads();
 
-    // producer (warp 0): windows of live receive `it` into slot it % kStages
+    // producer (warp 0): windows of item `it` into slot it % kStages
     auto produce = [&](int it) {
         const int slot = it % kStages;
-        const int code = s_rx[it];
-        bool staged = !(code & 0x40000000);
-        const int r = code & 0x3fffffff;
+        const int code = s_code[it];
+        bool staged = !(code & kItemUnstaged);
+        const int r = code & 0xffff;
+        const int t0g = ((code >> 16) & 0xf) * kTapGroup, t1g = ((code >> 20) & 0xf) * kTapGroup;
+        const bool mine = lane >= t0g && lane < t1g && lane < ntx;
         int e0 = 0, e1 = 0;
-        if (staged && lane < ntx) {
+        if (staged && mine) {
             const float xlo = __fadd_rn(s_txlh[2 * lane], s_rxlh[2 * it]);
             const float xhi = __fadd_rn(s_txlh[2 * lane + 1], s_rxlh[2 * it + 1]);
             staged_window<KIND, T>(xlo, xhi, a, e0, e1);
@@ -392,22 +418,22 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         const int total = __shfl_sync(0xffffffffu, off, 31);
         off -= cnt;
         // the plan sized these windows to fit; a plan from other tables could
-        // not, and then this receive is gathered from global memory instead
+        // not, and then this item is gathered from global memory instead
         if ((long long)total * (long long)sizeof(E) > kStageBytes) staged = false;
-        if (lane < kTxReg) sbase[slot][lane] = (staged && lane < ntx) ? off - e0 : 0;
+        if (lane < kTxReg) sbase[slot][lane] = (staged && mine) ? off - e0 : 0;
         if (lane == 0) sstaged[slot] = staged ? 1 : 0;
         __syncwarp();
         if (lane == 0) mbar_arrive_expect_tx(&full[slot], staged ? (unsigned)(total * sizeof(E)) : 0u);
         __syncwarp();
-        if (staged && lane < ntx && cnt > 0) {
+        if (staged && mine && cnt > 0) {
             const E *src = static_cast<const E *>(a.data) + (frame_ch + (long long)lane * nrx + r) * a.nt + e0;
             E *dst = reinterpret_cast<E *>(smem_raw + (size_t)slot * kStageBytes) + off;
             tma_bulk_load(dst, src, (unsigned)(cnt * sizeof(E)), &full[slot]);
         }
     };
-    int produced = 0;  // iterations warp 0 has issued copies for
+    int produced = 0;  // items warp 0 has issued copies for
     if (w == 0)
-        for (int it = 0; it < kStages && it < nlive; ++it) produce(it), produced = it + 1;
+        for (int it = 0; it < kStages && it < nitems; ++it) produce(it), produced = it + 1;
 
     // transmit side of this pixel; slots past ntx carry zero weights
     float rtau[kTxReg], rapod[kTxReg];
@@ -423,25 +449,27 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         }
     }
 
-    float acc = 0.f, s1 = 0.f;
+    float acc = 0.f, s1 = 0.f, accr = 0.f;
     bool failed = false;
-    // receive-side values, fetched two receives ahead
+    // receive-side values, fetched two items ahead
     auto rx_load = [&](int it, float &trx, float &arx) {
-        const int r = s_rx[it] & 0x3fffffff;
+        const int r = s_code[it] & 0xffff;
         trx = valid ? __ldg(a.taurx + (long long)r * np + i) : 0.f;
         arx = valid ? __ldg(a.apodrx + (long long)r * np + i) : 0.f;
     };
     float trx1 = 0.f, arx1 = 0.f, trx2 = 0.f, arx2 = 0.f;
-    if (nlive > 0) rx_load(0, trx1, arx1);
-    if (nlive > 1) rx_load(1, trx2, arx2);
+    if (nitems > 0) rx_load(0, trx1, arx1);
+    if (nitems > 1) rx_load(1, trx2, arx2);
 
-    for (int it = 0; it < nlive; ++it) {
+    for (int it = 0; it < nitems; ++it) {
         const int slot = it % kStages;
-        const int r = s_rx[it] & 0x3fffffff;
+        const int code = s_code[it];
+        const int r = code & 0xffff;
+        const int g0 = (code >> 16) & 0xf, g1 = (code >> 20) & 0xf;
         const float trx = trx1, arx = arx1;
         trx1 = trx2;
         arx1 = arx2;
-        if (it + 2 < nlive) rx_load(it + 2, trx2, arx2);
+        if (it + 2 < nitems) rx_load(it + 2, trx2, arx2);
         if (!mbar_wait_bounded(&full[slot], (unsigned)(it / kStages) & 1u)) failed = true;
         if (failed || *(volatile int *)&s_failed) {
             failed = true;
@@ -450,14 +478,14 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         }
 
         const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh);
-        float accr = 0.f;
         if (live) {
             const long long ch_first = (frame_ch + r) * a.nt;
             if (sstaged[slot]) {
                 const E *stage = reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes);
 #pragma unroll
-                for (int g = 0; g < kTxReg; g += kTapGroup) {
-                    if (g < ntx) {
+                for (int gg = 0; gg < kTxGroups; ++gg) {
+                    if (gg >= g0 && gg < g1) {
+                        const int g = gg * kTapGroup;
                         const int4 b = *reinterpret_cast<const int4 *>(&sbase[slot][g]);
                         const int bk[kTapGroup] = {b.x, b.y, b.z, b.w};
                         accr = staged_group<KIND, T, true>(a, rtau + g, rapod + g, trx, arx, bk,
@@ -466,8 +494,9 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
                 }
             } else {
 #pragma unroll
-                for (int g = 0; g < kTxReg; g += kTapGroup) {
-                    if (g < ntx) {
+                for (int gg = 0; gg < kTxGroups; ++gg) {
+                    if (gg >= g0 && gg < g1) {
+                        const int g = gg * kTapGroup;
                         const int bk[kTapGroup] = {0, 0, 0, 0};
                         accr = staged_group<KIND, T, false>(a, rtau + g, rapod + g, trx, arx, bk,
                                                             nullptr, ch_first, chs, g, ntx, accr);
@@ -475,18 +504,21 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
                 }
             }
         }
-        if (SUM == PYCBF_GB_SUM_TX_AND_RX) acc += accr;
-        if (SUM == PYCBF_GB_SUM_TX_ONLY && valid) a.out[((long long)f * nrx + r) * np + op] = accr;
-        if (SUM == PYCBF_GB_SUM_DMAS_SSR || SUM == PYCBF_GB_SUM_DMAS_POWER) {
-            const float s = (SUM == PYCBF_GB_SUM_DMAS_SSR) ? copysignf(sqrtf(fabsf(accr)), accr) : accr;
-            acc = fmaf(s, s1, acc);
-            s1 += s;
+        if (code & kItemLast) {  // this receive is complete
+            if (SUM == PYCBF_GB_SUM_TX_AND_RX) acc += accr;
+            if (SUM == PYCBF_GB_SUM_TX_ONLY && valid) a.out[((long long)f * nrx + r) * np + op] = accr;
+            if (SUM == PYCBF_GB_SUM_DMAS_SSR || SUM == PYCBF_GB_SUM_DMAS_POWER) {
+                const float sv = (SUM == PYCBF_GB_SUM_DMAS_SSR) ? copysignf(sqrtf(fabsf(accr)), accr) : accr;
+                acc = fmaf(sv, s1, acc);
+                s1 += sv;
+            }
+            accr = 0.f;
         }
         // this warp is done with the slot
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[slot]);
-        // warp 0 refills the slot of the previous iteration once every warp left it
-        if (w == 0 && it >= 1 && it - 1 + kStages < nlive) {
+        // warp 0 refills the slot of the previous item once every warp left it
+        if (w == 0 && it >= 1 && it - 1 + kStages < nitems) {
             const int pit = it - 1;
             if (!mbar_wait_bounded(&empty[pit % kStages], (unsigned)(pit / kStages) & 1u)) {
                 failed = true;
@@ -520,7 +552,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
 }
 
 inline size_t staged_smem_bytes(int nrx) {
-    return (size_t)kStages * kStageBytes + sizeof(int) * 3 * (size_t)nrx;
+    return (size_t)kStages * kStageBytes + sizeof(int) * 3 * (size_t)nrx * kTxGroups;
 }
 
 template <int KIND, typename T>
