@@ -24,7 +24,9 @@
 namespace pgb {
 
 constexpr int kStages = 4;
-constexpr int kStageBytes = 12 * 1024;
+constexpr int kStageBytes = 12 * 1024;     // one stage: receive rows + channel windows
+constexpr int kRowBytes = 2 * kBlock * 4;  // the tile's taurx and apodrx of the receive
+constexpr int kWindowBytes = kStageBytes - kRowBytes;
 constexpr unsigned kWaitLimit = 1u << 16;
 
 // A tile's work is a list of items: one receive and a run of whole transmit
@@ -106,30 +108,30 @@ template <typename T> struct StagedElem<PYCBF_GB_INTERP_CUBIC, T> {
     static constexpr int kExtra = 0;
 };
 
-// First and one-past-last element of the window of delays [xlo, xhi], aligned
-// to 16 bytes (nt * sizeof(E) is a multiple of 16, checked on the host); empty
-// (e0 == e1) when no delay in the range can be in range.  The index rule is
-// the taps' own exact rule, and it is monotonic in the delay.
+// First and one-past-last element of a window that contains the sample index
+// of every delay in [xlo, xhi], aligned to 16 bytes (nt * sizeof(E) is a
+// multiple of 16, checked on the host); empty (e0 == e1) when no such delay
+// can be in range.  The reciprocal quotient is within 2 ulp of the IEEE one,
+// so its index, widened by one sample each way, bounds the taps' exact index,
+// which is monotonic in the delay.
 template <int KIND, typename T>
 __device__ __forceinline__ void staged_window(float xlo, float xhi, const DasArgs &a, int &e0,
                                               int &e1) {
     using E = typename StagedElem<KIND, T>::E;
     constexpr int per16 = 16 / (int)sizeof(E);
     e0 = e1 = 0;
-    if (xlo != xlo || xhi != xhi || xhi < xlo) return;
-    int i0, i1;
-    if (KIND == PYCBF_GB_INTERP_NEAREST) {
-        Kind<KIND, T>::index_exact(xlo, a, i0);
-        Kind<KIND, T>::index_exact(xhi, a, i1);
-        if (i1 < 0 || i0 >= a.nt) return;
-    } else {
-        if (xhi < a.t0 || xlo > a.xmax) return;
-        i0 = (xlo <= a.t0) ? 0 : (int)floorf(__fdiv_rn(__fsub_rn(xlo, a.t0), a.dt));
-        i1 = (xhi >= a.xmax) ? a.nt - 1 : (int)floorf(__fdiv_rn(__fsub_rn(xhi, a.t0), a.dt));
-    }
-    i0 = min(max(i0, 0), a.nt - 1);
-    i1 = min(max(i1 + StagedElem<KIND, T>::kExtra, 0), a.nt - 1);
-    if (i1 < i0) return;
+    if (!(xlo <= xhi)) return;  // also rejects NaN
+    const float q0 = __fmul_rn(__fsub_rn(xlo, a.t0), a.inv_dt);
+    const float q1 = __fmul_rn(__fsub_rn(xhi, a.t0), a.inv_dt);
+    const float h = (KIND == PYCBF_GB_INTERP_NEAREST) ? 0.5f : 0.f;
+    const float last = (float)(a.nt - 1);
+    const float f0 = fmaxf(floorf(q0 + h) - 1.f, 0.f);
+    // nearest truncates q + 0.5 toward zero, so q in (-1.5, -0.5) reads sample 0:
+    // one more sample of headroom above
+    const float up = (KIND == PYCBF_GB_INTERP_NEAREST) ? 2.f : 1.f + (float)StagedElem<KIND, T>::kExtra;
+    const float f1 = fminf(floorf(q1 + h) + up, last);
+    if (!(f0 <= f1)) return;  // window entirely before sample 0 or after the last
+    const int i0 = (int)f0, i1 = (int)f1;
     e0 = (i0 / per16) * per16;
     e1 = min(((i1 + per16) / per16) * per16, a.nt);
 }
@@ -244,9 +246,9 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
                 int g0 = 0;
                 while (g0 < ng) {
                     int g1 = g0 + 1, tot = gb[g0];
-                    while (g1 < ng && tot + gb[g1] <= kStageBytes) tot += gb[g1++];
+                    while (g1 < ng && tot + gb[g1] <= kWindowBytes) tot += gb[g1++];
                     int code = r | (g0 << 16) | (g1 << 20);
-                    if (tot > kStageBytes) code |= kItemUnstaged;
+                    if (tot > kWindowBytes) code |= kItemUnstaged;
                     if (g1 == ng) code |= kItemLast;
                     codes[nitems] = code;
                     rxlh[2 * nitems] = lo;
@@ -288,7 +290,7 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt,
                                               long long ch_first, long long chs, int g, int ntx,
                                               float accr) {
     using K = Kind<KIND, T>;
-    constexpr unsigned cap = kStageBytes / sizeof(typename StagedElem<KIND, T>::E);
+    constexpr unsigned cap = kWindowBytes / sizeof(typename StagedElem<KIND, T>::E);
     float xs[kTapGroup], ap[kTapGroup], fl[kTapGroup];
     bool ok[kTapGroup];
     bool nearb = false;
@@ -376,6 +378,8 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     const long long frame_ch = (long long)f * ntx * nrx;
     const long long chs = (long long)nrx * a.nt;
     const long long op = valid ? (a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i) : 0;
+    // bytes of one receive row of this tile (np % 4 == 0, checked on the host)
+    const unsigned row_bytes = (unsigned)(4 * min((long long)kBlock, np - tile * kBlock));
     // the tile's work items and their receive delay bounds, after the stages
     int *s_code = reinterpret_cast<int *>(smem_raw + kStages * kStageBytes);
     float *s_rxlh = reinterpret_cast<float *>(s_code + imax);
@@ -419,15 +423,23 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         off -= cnt;
         // the plan sized these windows to fit; a plan from other tables could
         // not, and then this item is gathered from global memory instead
-        if ((long long)total * (long long)sizeof(E) > kStageBytes) staged = false;
+        if ((long long)total * (long long)sizeof(E) > kWindowBytes) staged = false;
         if (lane < kTxReg) sbase[slot][lane] = (staged && mine) ? off - e0 : 0;
         if (lane == 0) sstaged[slot] = staged ? 1 : 0;
         __syncwarp();
-        if (lane == 0) mbar_arrive_expect_tx(&full[slot], staged ? (unsigned)(total * sizeof(E)) : 0u);
+        unsigned char *st = smem_raw + (size_t)slot * kStageBytes;
+        if (lane == 0)
+            mbar_arrive_expect_tx(&full[slot],
+                                  2u * row_bytes + (staged ? (unsigned)(total * sizeof(E)) : 0u));
         __syncwarp();
+        // the tile's receive rows (table columns of this tile are contiguous)
+        if (lane == 30) tma_bulk_load(st, a.taurx + (long long)r * np + tile * kBlock, row_bytes, &full[slot]);
+        if (lane == 31)
+            tma_bulk_load(st + kRowBytes / 2, a.apodrx + (long long)r * np + tile * kBlock, row_bytes,
+                          &full[slot]);
         if (staged && mine && cnt > 0) {
             const E *src = static_cast<const E *>(a.data) + (frame_ch + (long long)lane * nrx + r) * a.nt + e0;
-            E *dst = reinterpret_cast<E *>(smem_raw + (size_t)slot * kStageBytes) + off;
+            E *dst = reinterpret_cast<E *>(st + kRowBytes) + off;
             tma_bulk_load(dst, src, (unsigned)(cnt * sizeof(E)), &full[slot]);
         }
     };
@@ -451,37 +463,27 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
 
     float acc = 0.f, s1 = 0.f, accr = 0.f;
     bool failed = false;
-    // receive-side values, fetched two items ahead
-    auto rx_load = [&](int it, float &trx, float &arx) {
-        const int r = s_code[it] & 0xffff;
-        trx = valid ? __ldg(a.taurx + (long long)r * np + i) : 0.f;
-        arx = valid ? __ldg(a.apodrx + (long long)r * np + i) : 0.f;
-    };
-    float trx1 = 0.f, arx1 = 0.f, trx2 = 0.f, arx2 = 0.f;
-    if (nitems > 0) rx_load(0, trx1, arx1);
-    if (nitems > 1) rx_load(1, trx2, arx2);
 
     for (int it = 0; it < nitems; ++it) {
         const int slot = it % kStages;
         const int code = s_code[it];
         const int r = code & 0xffff;
         const int g0 = (code >> 16) & 0xf, g1 = (code >> 20) & 0xf;
-        const float trx = trx1, arx = arx1;
-        trx1 = trx2;
-        arx1 = arx2;
-        if (it + 2 < nitems) rx_load(it + 2, trx2, arx2);
         if (!mbar_wait_bounded(&full[slot], (unsigned)(it / kStages) & 1u)) failed = true;
         if (failed || *(volatile int *)&s_failed) {
             failed = true;
             s_failed = 1;
             break;
         }
+        const float *rows = reinterpret_cast<const float *>(smem_raw + (size_t)slot * kStageBytes);
+        const float trx = rows[tid], arx = rows[kBlock + tid];  // stale past the last pixel: unused
 
         const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh);
         if (live) {
             const long long ch_first = (frame_ch + r) * a.nt;
             if (sstaged[slot]) {
-                const E *stage = reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes);
+                const E *stage =
+                    reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes + kRowBytes);
 #pragma unroll
                 for (int gg = 0; gg < kTxGroups; ++gg) {
                     if (gg >= g0 && gg < g1) {
