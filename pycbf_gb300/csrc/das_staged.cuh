@@ -66,14 +66,14 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, u
 __device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-// try_wait suspends the thread until the phase completes or ~hint ns pass
+// try_wait: true once the phase with this parity has completed
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
     unsigned ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         " selp.u32 %0, 1, 0, p;\n}"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity), "r"(1000000u)
+        : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
     return ok != 0;
 }
@@ -88,6 +88,20 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsig
     }
     return false;
 }
+// asynchronous 16-byte / 4-byte copies global -> shared (LSU path)
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+// arrive on bar once this thread's earlier cp.async copies have landed (the
+// barrier's expected count includes this arrival)
+__device__ __forceinline__ void cp_async_arrive(unsigned long long *bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // 1-D bulk copy global -> shared (both 16-byte aligned, bytes a multiple of 16)
 __device__ __forceinline__ void tma_bulk_load(void *dst, const void *src, unsigned bytes,
                                               unsigned long long *bar) {
@@ -357,13 +371,17 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
                                                               int *status) {
     using E = typename StagedElem<KIND, T>::E;
     constexpr int kWarps = kBlock / 32;
+    constexpr int per16 = 16 / (int)sizeof(E);  // elements per 16-byte copy
+    constexpr int kAhead = kStages - 1;          // items staged ahead of the one consumed
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long full[kStages];
     __shared__ __align__(8) unsigned long long empty[kStages];
-    __shared__ __align__(16) int sbase[kStages][kTxReg];  // element base of each window - its e0
-    __shared__ int sstaged[kStages];
     __shared__ float s_txlh[2 * kTxReg];
     __shared__ int s_failed;
+    // per warp and slot: the stage base (offset - e0) of each transmit's window,
+    // written by the warp when it stages the item and read by it when it consumes
+    __shared__ __align__(16) int s_base[kStages][kBlock / 32][32];
+    __shared__ int s_staged[kStages][kBlock / 32];
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const long long tile = blockIdx.x;
@@ -378,14 +396,11 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     const long long frame_ch = (long long)f * ntx * nrx;
     const long long chs = (long long)nrx * a.nt;
     const long long op = valid ? (a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i) : 0;
-    // bytes of one receive row of this tile (np % 4 == 0, checked on the host)
-    const unsigned row_bytes = (unsigned)(4 * min((long long)kBlock, np - tile * kBlock));
-    // the tile's work items and their receive delay bounds, after the stages
     int *s_code = reinterpret_cast<int *>(smem_raw + kStages * kStageBytes);
     float *s_rxlh = reinterpret_cast<float *>(s_code + imax);
 
     if (tid < kStages) {
-        mbar_init(&full[tid], 1);
+        mbar_init(&full[tid], kBlock);  // one cp.async arrival per thread
         mbar_init(&empty[tid], kWarps);
     }
     {
@@ -399,12 +414,12 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     mbar_fence_init();
     __syncthreads();
 
-    // producer (warp 0): windows of item `it` into slot it % kStages
-    auto produce = [&](int it) {
-        const int slot = it % kStages;
+    // Window table of item `it` in this warp: lane t < ntx holds transmit t's
+    // first element e0 and, through the scan, its offset in the stage; returns
+    // the stage base (offset - e0) of the lane's transmit and its count.
+    auto windows = [&](int it, int &base, int &cnt, int &e0_out, bool &staged) {
         const int code = s_code[it];
-        bool staged = !(code & kItemUnstaged);
-        const int r = code & 0xffff;
+        staged = !(code & kItemUnstaged);
         const int t0g = ((code >> 16) & 0xf) * kTapGroup, t1g = ((code >> 20) & 0xf) * kTapGroup;
         const bool mine = lane >= t0g && lane < t1g && lane < ntx;
         int e0 = 0, e1 = 0;
@@ -413,7 +428,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             const float xhi = __fadd_rn(s_txlh[2 * lane + 1], s_rxlh[2 * it + 1]);
             staged_window<KIND, T>(xlo, xhi, a, e0, e1);
         }
-        const int cnt = e1 - e0;
+        cnt = e1 - e0;
         int off = cnt;
         for (int o = 1; o < 32; o <<= 1) {
             const int v = __shfl_up_sync(0xffffffffu, off, o);
@@ -421,31 +436,40 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         }
         const int total = __shfl_sync(0xffffffffu, off, 31);
         off -= cnt;
-        // the plan sized these windows to fit; a plan from other tables could
-        // not, and then this item is gathered from global memory instead
+        // the plan sized the windows to fit; a plan from other tables could not
         if ((long long)total * (long long)sizeof(E) > kWindowBytes) staged = false;
-        if (lane < kTxReg) sbase[slot][lane] = (staged && mine) ? off - e0 : 0;
-        if (lane == 0) sstaged[slot] = staged ? 1 : 0;
-        __syncwarp();
-        unsigned char *st = smem_raw + (size_t)slot * kStageBytes;
-        if (lane == 0)
-            mbar_arrive_expect_tx(&full[slot],
-                                  2u * row_bytes + (staged ? (unsigned)(total * sizeof(E)) : 0u));
-        __syncwarp();
-        // the tile's receive rows (table columns of this tile are contiguous)
-        if (lane == 30) tma_bulk_load(st, a.taurx + (long long)r * np + tile * kBlock, row_bytes, &full[slot]);
-        if (lane == 31)
-            tma_bulk_load(st + kRowBytes / 2, a.apodrx + (long long)r * np + tile * kBlock, row_bytes,
-                          &full[slot]);
-        if (staged && mine && cnt > 0) {
-            const E *src = static_cast<const E *>(a.data) + (frame_ch + (long long)lane * nrx + r) * a.nt + e0;
-            E *dst = reinterpret_cast<E *>(st + kRowBytes) + off;
-            tma_bulk_load(dst, src, (unsigned)(cnt * sizeof(E)), &full[slot]);
-        }
+        base = staged && mine ? off - e0 : 0;
+        e0_out = e0;
+        if (!staged) cnt = 0;
     };
-    int produced = 0;  // items warp 0 has issued copies for
-    if (w == 0)
-        for (int it = 0; it < kStages && it < nitems; ++it) produce(it), produced = it + 1;
+
+    // every warp stages its share of item `it`: the windows of transmits
+    // w, w+kWarps, ... and, per thread, its pixel's receive row entries
+    auto produce = [&](int it) {
+        const int slot = it % kStages;
+        unsigned char *st = smem_raw + (size_t)slot * kStageBytes;
+        const int r = s_code[it] & 0xffff;
+        if (valid) {
+            cp_async4(st + 4 * tid, a.taurx + (long long)r * np + i);
+            cp_async4(st + kRowBytes / 2 + 4 * tid, a.apodrx + (long long)r * np + i);
+        }
+        int base, cnt, e0;
+        bool staged;
+        windows(it, base, cnt, e0, staged);
+        s_base[slot][w][lane] = base;
+        if (lane == 0) s_staged[slot][w] = staged ? 1 : 0;
+        if (staged) {
+            E *stage = reinterpret_cast<E *>(st + kRowBytes);
+            for (int t = w; t < ntx; t += kWarps) {
+                const int ct = __shfl_sync(0xffffffffu, cnt, t);
+                const int et = __shfl_sync(0xffffffffu, e0, t);
+                const int bt = __shfl_sync(0xffffffffu, base, t);
+                const E *src = static_cast<const E *>(a.data) + (frame_ch + (long long)t * nrx + r) * a.nt + et;
+                for (int k = lane * per16; k < ct; k += 32 * per16) cp_async16(stage + bt + et + k, src + k);
+            }
+        }
+        cp_async_arrive(&full[slot]);
+    };
 
     // transmit side of this pixel; slots past ntx carry zero weights
     float rtau[kTxReg], rapod[kTxReg];
@@ -460,36 +484,50 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             amax = fmaxf(amax, fabsf(rapod[k]));
         }
     }
+    for (int it = 0; it < kAhead && it < nitems; ++it) produce(it);
 
     float acc = 0.f, s1 = 0.f, accr = 0.f;
     bool failed = false;
-
     for (int it = 0; it < nitems; ++it) {
         const int slot = it % kStages;
-        const int code = s_code[it];
-        const int r = code & 0xffff;
-        const int g0 = (code >> 16) & 0xf, g1 = (code >> 20) & 0xf;
+        // stage item it + kAhead into the slot item it - 1 used, once every warp left it
+        const int p = it + kAhead;
+        if (p < nitems) {
+            if (it >= 1 && !mbar_wait_bounded(&empty[(it - 1) % kStages], (unsigned)((it - 1) / kStages) & 1u))
+                failed = true;
+            if (failed || *(volatile int *)&s_failed) {
+                failed = true;
+                s_failed = 1;
+                break;
+            }
+            produce(p);
+        }
         if (!mbar_wait_bounded(&full[slot], (unsigned)(it / kStages) & 1u)) failed = true;
         if (failed || *(volatile int *)&s_failed) {
             failed = true;
             s_failed = 1;
             break;
         }
+        const int code = s_code[it];
+        const int r = code & 0xffff;
+        const int g0 = (code >> 16) & 0xf, g1 = (code >> 20) & 0xf;
         const float *rows = reinterpret_cast<const float *>(smem_raw + (size_t)slot * kStageBytes);
-        const float trx = rows[tid], arx = rows[kBlock + tid];  // stale past the last pixel: unused
+        const float trx = rows[tid], arx = rows[kBlock + tid];  // not copied past the last pixel: unused
 
+        __syncwarp();
+        const bool staged = s_staged[slot][w] != 0;
         const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh);
         if (live) {
             const long long ch_first = (frame_ch + r) * a.nt;
-            if (sstaged[slot]) {
+            if (staged) {
                 const E *stage =
                     reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes + kRowBytes);
 #pragma unroll
                 for (int gg = 0; gg < kTxGroups; ++gg) {
                     if (gg >= g0 && gg < g1) {
                         const int g = gg * kTapGroup;
-                        const int4 b = *reinterpret_cast<const int4 *>(&sbase[slot][g]);
-                        const int bk[kTapGroup] = {b.x, b.y, b.z, b.w};
+                        const int4 b4 = *reinterpret_cast<const int4 *>(&s_base[slot][w][g]);
+                        const int bk[kTapGroup] = {b4.x, b4.y, b4.z, b4.w};
                         accr = staged_group<KIND, T, true>(a, rtau + g, rapod + g, trx, arx, bk,
                                                            stage, ch_first, chs, g, ntx, accr);
                     }
@@ -516,31 +554,14 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             }
             accr = 0.f;
         }
-        // this warp is done with the slot
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[slot]);
-        // warp 0 refills the slot of the previous item once every warp left it
-        if (w == 0 && it >= 1 && it - 1 + kStages < nitems) {
-            const int pit = it - 1;
-            if (!mbar_wait_bounded(&empty[pit % kStages], (unsigned)(pit / kStages) & 1u)) {
-                failed = true;
-                s_failed = 1;
-                break;
-            }
-            produce(pit + kStages);
-            produced = pit + kStages + 1;
-        }
     }
+    // every thread's own copies are complete before the shared memory goes away
+    cp_async_wait_all();
     __syncthreads();
     if (s_failed) {
-        // drain the copies still in flight before the CTA's shared memory goes
-        // away: the latest phase of each slot is one of the last kStages issued
-        if (tid == 0) {
-            if (status) atomicExch(status, 1);
-            for (int j = max(0, produced - kStages); j < produced; ++j)
-                (void)mbar_wait_bounded(&full[j % kStages], (unsigned)(j / kStages) & 1u);
-        }
-        __syncthreads();
+        if (tid == 0 && status) atomicExch(status, 1);
         if (valid) {
             const float nan = __int_as_float(0x7fc00000);
             if (SUM == PYCBF_GB_SUM_TX_ONLY)
