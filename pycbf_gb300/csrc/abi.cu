@@ -77,7 +77,7 @@ bool das_shape_ok(int geom, int sumtype, long long ntx) {
 // receive; its 16-byte bulk copies need channel strides and the data base
 // aligned to 16 bytes.
 bool staged_ok(const pycbf_gb_rfinfo *rf, int interp, int sumtype, const void *data) {
-    if (rf->ntx > 12 || rf->nrx > 512 || interp > PYCBF_GB_INTERP_CUBIC) return false;
+    if (rf->ntx > 12 || rf->nrx > 4096 || interp > PYCBF_GB_INTERP_CUBIC) return false;
     if (sumtype != PYCBF_GB_SUM_TX_ONLY && sumtype != PYCBF_GB_SUM_TX_AND_RX &&
         sumtype != PYCBF_GB_SUM_DMAS_SSR && sumtype != PYCBF_GB_SUM_DMAS_POWER)
         return false;
@@ -86,15 +86,9 @@ bool staged_ok(const pycbf_gb_rfinfo *rf, int interp, int sumtype, const void *d
     return ((size_t)rf->nt * elem) % 16 == 0 && reinterpret_cast<uintptr_t>(data) % 16 == 0;
 }
 
-// the staged kernel also copies each tile's receive rows by TMA
-bool staged_tables_ok(long long np, const float *taurx, const float *apodrx) {
-    return np % 4 == 0 && reinterpret_cast<uintptr_t>(taurx) % 16 == 0 &&
-           reinterpret_cast<uintptr_t>(apodrx) % 16 == 0;
-}
-
 int launch_tabbed(const pycbf_gb_rfinfo *rf, DasArgs &a, int interp, int sumtype, const void *plan,
                   cudaStream_t s) {
-    if (plan && staged_ok(rf, interp, sumtype, a.data) && staged_tables_ok(a.np, a.taurx, a.apodrx)) {
+    if (plan && staged_ok(rf, interp, sumtype, a.data)) {
         if (sumtype == PYCBF_GB_SUM_TX_ONLY) {  // rows of receives no pixel of a tile uses stay 0
             const size_t bytes = sizeof(float) * (size_t)rf->nframes * rf->nrx * (size_t)a.np;
             int st = cuda_status(cudaMemsetAsync(a.out, 0, bytes, s));

@@ -24,28 +24,15 @@
 namespace pgb {
 
 constexpr int kStages = 4;
-constexpr int kStageBytes = 12 * 1024;     // one stage: receive rows + channel windows
-constexpr int kRowBytes = 2 * kBlock * 4;  // the tile's taurx and apodrx of the receive
-constexpr int kWindowBytes = kStageBytes - kRowBytes;
-constexpr unsigned kWaitLimit = 1u << 16;
-
-// A tile's work is a list of items: one receive and a run of whole transmit
-// groups (kTapGroup transmits each) whose windows fit one stage together; a
-// receive whose windows are too large for one stage becomes several items.
-constexpr int kTapGroup = 4;
-constexpr int kTxGroups = (kTxReg + kTapGroup - 1) / kTapGroup;
-// item code: receive (bits 0-15), first group (16-19), end group (20-23),
-// last item of its receive (bit 28), not staged (bit 30)
-constexpr int kItemLast = 1 << 28;
-constexpr int kItemUnstaged = 1 << 30;
+constexpr int kStageBytes = 12 * 1024;
+constexpr unsigned kWaitLimit = 1u << 30;  // polls; the ~1 s clock bound ends a wait first
 
 // plan layout (int32 words): [0] status, [1] reserved, [2..3] pad, then per
 // tile a record of plan_tile_words(ntx, nrx) words:
-//   nitems | item code (imax) | receive lo,hi delay per item (2*imax floats)
-//   | transmit lo,hi delay (2*ntx floats),  imax = nrx * kTxGroups
+//   nlive | rx index per live receive (nrx) | rx lo,hi per live receive (2*nrx floats)
+//   | tx lo,hi per transmit (2*ntx floats)
 __host__ __device__ inline long long plan_tile_words(int ntx, int nrx) {
-    const long long imax = (long long)nrx * kTxGroups;
-    return 1 + imax + 2 * imax + 2LL * ntx;
+    return 1 + (long long)nrx + 2LL * nrx + 2LL * ntx;
 }
 constexpr int kPlanHeaderWords = 4;
 
@@ -66,7 +53,8 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, u
 __device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-// try_wait: true once the phase with this parity has completed
+// try_wait: true once the phase with this parity has completed (a suspend-time
+// hint makes each wait ~500 cycles slower to wake, so none is given)
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
     unsigned ok;
     asm volatile(
@@ -88,20 +76,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsig
     }
     return false;
 }
-// asynchronous 16-byte / 4-byte copies global -> shared (LSU path)
-__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-// arrive on bar once this thread's earlier cp.async copies have landed (the
-// barrier's expected count includes this arrival)
-__device__ __forceinline__ void cp_async_arrive(unsigned long long *bar) {
-    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
 // 1-D bulk copy global -> shared (both 16-byte aligned, bytes a multiple of 16)
 __device__ __forceinline__ void tma_bulk_load(void *dst, const void *src, unsigned bytes,
                                               unsigned long long *bar) {
@@ -122,30 +96,30 @@ template <typename T> struct StagedElem<PYCBF_GB_INTERP_CUBIC, T> {
     static constexpr int kExtra = 0;
 };
 
-// First and one-past-last element of a window that contains the sample index
-// of every delay in [xlo, xhi], aligned to 16 bytes (nt * sizeof(E) is a
-// multiple of 16, checked on the host); empty (e0 == e1) when no such delay
-// can be in range.  The reciprocal quotient is within 2 ulp of the IEEE one,
-// so its index, widened by one sample each way, bounds the taps' exact index,
-// which is monotonic in the delay.
+// First and one-past-last element of the window of delays [xlo, xhi], aligned
+// to 16 bytes (nt * sizeof(E) is a multiple of 16, checked on the host); empty
+// (e0 == e1) when no delay in the range can be in range.  The index rule is
+// the taps' own exact rule, and it is monotonic in the delay.
 template <int KIND, typename T>
 __device__ __forceinline__ void staged_window(float xlo, float xhi, const DasArgs &a, int &e0,
                                               int &e1) {
     using E = typename StagedElem<KIND, T>::E;
     constexpr int per16 = 16 / (int)sizeof(E);
     e0 = e1 = 0;
-    if (!(xlo <= xhi)) return;  // also rejects NaN
-    const float q0 = __fmul_rn(__fsub_rn(xlo, a.t0), a.inv_dt);
-    const float q1 = __fmul_rn(__fsub_rn(xhi, a.t0), a.inv_dt);
-    const float h = (KIND == PYCBF_GB_INTERP_NEAREST) ? 0.5f : 0.f;
-    const float last = (float)(a.nt - 1);
-    const float f0 = fmaxf(floorf(q0 + h) - 1.f, 0.f);
-    // nearest truncates q + 0.5 toward zero, so q in (-1.5, -0.5) reads sample 0:
-    // one more sample of headroom above
-    const float up = (KIND == PYCBF_GB_INTERP_NEAREST) ? 2.f : 1.f + (float)StagedElem<KIND, T>::kExtra;
-    const float f1 = fminf(floorf(q1 + h) + up, last);
-    if (!(f0 <= f1)) return;  // window entirely before sample 0 or after the last
-    const int i0 = (int)f0, i1 = (int)f1;
+    if (xlo != xlo || xhi != xhi || xhi < xlo) return;
+    int i0, i1;
+    if (KIND == PYCBF_GB_INTERP_NEAREST) {
+        Kind<KIND, T>::index_exact(xlo, a, i0);
+        Kind<KIND, T>::index_exact(xhi, a, i1);
+        if (i1 < 0 || i0 >= a.nt) return;
+    } else {
+        if (xhi < a.t0 || xlo > a.xmax) return;
+        i0 = (xlo <= a.t0) ? 0 : (int)floorf(__fdiv_rn(__fsub_rn(xlo, a.t0), a.dt));
+        i1 = (xhi >= a.xmax) ? a.nt - 1 : (int)floorf(__fdiv_rn(__fsub_rn(xhi, a.t0), a.dt));
+    }
+    i0 = min(max(i0, 0), a.nt - 1);
+    i1 = min(max(i1 + StagedElem<KIND, T>::kExtra, 0), a.nt - 1);
+    if (i1 < i0) return;
     e0 = (i0 / per16) * per16;
     e1 = min(((i1 + per16) / per16) * per16, a.nt);
 }
@@ -177,16 +151,16 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
                                                              int *plan) {
     using E = typename StagedElem<KIND, T>::E;
     __shared__ float red[3][kBlock / 32];
+    __shared__ int s_any;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const long long tile = blockIdx.x;
     const long long i = tile * kBlock + tid;
     const bool valid = i < a.np;
     const int ntx = a.ntx, nrx = a.nrx;
-    const long long imax = (long long)nrx * kTxGroups;
     int *rec = plan + kPlanHeaderWords + tile * plan_tile_words(ntx, nrx);
-    int *codes = rec + 1;
-    float *rxlh = reinterpret_cast<float *>(rec + 1 + imax);
-    float *txlh = rxlh + 2 * imax;
+    int *rxidx = rec + 1;
+    float *rxlh = reinterpret_cast<float *>(rec + 1 + nrx);
+    float *txlh = rxlh + 2 * nrx;
     const float inf = __int_as_float(0x7f800000);
 
     auto block_minmax = [&](float lo, float hi, int any, float &blo, float &bhi, int &bany) {
@@ -213,7 +187,6 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
     };
 
     float amax = 0.f;
-    float txl = 0.f, txh = 0.f;  // this thread's transmit bounds (tid < ntx)
     for (int t = 0; t < ntx; ++t) {
         float tau = inf, taun = -inf;
         if (valid) {
@@ -223,16 +196,13 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
         float lo, hi;
         int any;
         block_minmax(tau == tau ? tau : inf, taun == taun ? taun : -inf, 0, lo, hi, any);
-        if (tid == t) {
-            txl = lo;
-            txh = hi;
-        }
         if (tid == 0) {
             txlh[2 * t] = lo;
             txlh[2 * t + 1] = hi;
         }
     }
-    int nitems = 0;
+    __syncthreads();
+    int nlive = 0;
     for (int r = 0; r < nrx; ++r) {
         float trx = 0.f, arx = 0.f;
         if (valid) {
@@ -243,38 +213,28 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
         float lo, hi;
         int any;
         block_minmax(live ? trx : inf, live ? trx : -inf, live ? 1 : 0, lo, hi, any);
-        if (!any) continue;  // block-uniform
-        if (w == 0) {
-            // window bytes of this thread's transmit, summed per transmit group
-            int bytes = 0;
-            if (lane < ntx) {
-                int e0, e1;
-                staged_window<KIND, T>(__fadd_rn(txl, lo), __fadd_rn(txh, hi), a, e0, e1);
-                bytes = (e1 - e0) * (int)sizeof(E);
-            }
-            for (int o = 1; o < kTapGroup; o <<= 1) bytes += __shfl_down_sync(0xffffffffu, bytes, o);
-            int gb[kTxGroups];
-            for (int g = 0; g < kTxGroups; ++g) gb[g] = __shfl_sync(0xffffffffu, bytes, g * kTapGroup);
-            if (lane == 0) {
-                const int ng = (ntx + kTapGroup - 1) / kTapGroup;
-                int g0 = 0;
-                while (g0 < ng) {
-                    int g1 = g0 + 1, tot = gb[g0];
-                    while (g1 < ng && tot + gb[g1] <= kWindowBytes) tot += gb[g1++];
-                    int code = r | (g0 << 16) | (g1 << 20);
-                    if (tot > kWindowBytes) code |= kItemUnstaged;
-                    if (g1 == ng) code |= kItemLast;
-                    codes[nitems] = code;
-                    rxlh[2 * nitems] = lo;
-                    rxlh[2 * nitems + 1] = hi;
-                    ++nitems;
-                    g0 = g1;
-                }
-            }
-            nitems = __shfl_sync(0xffffffffu, nitems, 0);
+        if (!any) continue;
+        // staged only if all windows of this receive fit one stage
+        int bytes = 0;
+        if (tid < ntx) {
+            const float xlo = __fadd_rn(txlh[2 * tid], lo), xhi = __fadd_rn(txlh[2 * tid + 1], hi);
+            int e0, e1;
+            staged_window<KIND, T>(xlo, xhi, a, e0, e1);
+            bytes = (e1 - e0) * (int)sizeof(E);
         }
+        for (int o = 16; o; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+        if (w == 0 && lane == 0) s_any = bytes;
+        __syncthreads();
+        const bool staged = s_any <= kStageBytes;
+        if (tid == 0) {
+            rxidx[nlive] = staged ? r : (r | 0x40000000);
+            rxlh[2 * nlive] = lo;
+            rxlh[2 * nlive + 1] = hi;
+        }
+        ++nlive;
+        __syncthreads();
     }
-    if (tid == 0) rec[0] = nitems;
+    if (tid == 0) rec[0] = nlive;
 }
 
 // ---------------------------------------------------------------------------
@@ -292,6 +252,8 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
 // Warp 0 refills the slot of iteration it-1 at the end of iteration it, so it
 // waits only for warps that are a whole receive behind.
 // ---------------------------------------------------------------------------
+constexpr int kTapGroup = 4;
+
 // One group of kTapGroup taps of receive (trx, arx): index, gather, weight,
 // accumulate.  STAGED gathers from the shared-memory stage at clamped
 // indices, otherwise from global memory.  A tap whose quotient lies within
@@ -304,7 +266,7 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt,
                                               long long ch_first, long long chs, int g, int ntx,
                                               float accr) {
     using K = Kind<KIND, T>;
-    constexpr unsigned cap = kWindowBytes / sizeof(typename StagedElem<KIND, T>::E);
+    constexpr unsigned cap = kStageBytes / sizeof(typename StagedElem<KIND, T>::E);
     float xs[kTapGroup], ap[kTapGroup], fl[kTapGroup];
     bool ok[kTapGroup];
     bool nearb = false;
@@ -371,17 +333,16 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
                                                               int *status) {
     using E = typename StagedElem<KIND, T>::E;
     constexpr int kWarps = kBlock / 32;
-    constexpr int per16 = 16 / (int)sizeof(E);  // elements per 16-byte copy
-    constexpr int kAhead = kStages - 1;          // items staged ahead of the one consumed
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long full[kStages];
     __shared__ __align__(8) unsigned long long empty[kStages];
+    __shared__ __align__(16) int sbase[kStages][kTxReg];  // element base of each window - its e0
+    __shared__ int sstaged[kStages];
     __shared__ float s_txlh[2 * kTxReg];
     __shared__ int s_failed;
-    // per warp and slot: the stage base (offset - e0) of each transmit's window,
-    // written by the warp when it stages the item and read by it when it consumes
-    __shared__ __align__(16) int s_base[kStages][kBlock / 32][32];
-    __shared__ int s_staged[kStages][kBlock / 32];
+    // the tile's plan: live receive indices and their delay bounds
+    int *s_rx = reinterpret_cast<int *>(smem_raw + kStages * kStageBytes);
+    float *s_rxlh = reinterpret_cast<float *>(s_rx + a.nrx);
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const long long tile = blockIdx.x;
@@ -390,45 +351,40 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     const int f = blockIdx.y;
     const int ntx = a.ntx, nrx = a.nrx;
     const long long np = a.np;
-    const long long imax = (long long)nrx * kTxGroups;
     const int *rec = plan + kPlanHeaderWords + tile * plan_tile_words(ntx, nrx);
-    const int nitems = __ldg(rec);
+    const int nlive = __ldg(rec);
     const long long frame_ch = (long long)f * ntx * nrx;
     const long long chs = (long long)nrx * a.nt;
     const long long op = valid ? (a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i) : 0;
-    int *s_code = reinterpret_cast<int *>(smem_raw + kStages * kStageBytes);
-    float *s_rxlh = reinterpret_cast<float *>(s_code + imax);
 
     if (tid < kStages) {
-        mbar_init(&full[tid], kBlock);  // one cp.async arrival per thread
+        mbar_init(&full[tid], 1);
         mbar_init(&empty[tid], kWarps);
     }
     {
-        const float *txlh = reinterpret_cast<const float *>(rec + 1 + 3 * imax);
+        const float *txlh = reinterpret_cast<const float *>(rec + 1 + 3 * nrx);
         if (tid < 2 * ntx) s_txlh[tid] = __ldg(txlh + tid);
-        for (int k = tid; k < nitems; k += kBlock) s_code[k] = __ldg(rec + 1 + k);
-        const float *rxlh = reinterpret_cast<const float *>(rec + 1 + imax);
-        for (int k = tid; k < 2 * nitems; k += kBlock) s_rxlh[k] = __ldg(rxlh + k);
+        for (int k = tid; k < nlive; k += kBlock) s_rx[k] = __ldg(rec + 1 + k);
+        const float *rxlh = reinterpret_cast<const float *>(rec + 1 + nrx);
+        for (int k = tid; k < 2 * nlive; k += kBlock) s_rxlh[k] = __ldg(rxlh + k);
     }
     if (tid == 0) s_failed = 0;
     mbar_fence_init();
     __syncthreads();
 
-    // Window table of item `it` in this warp: lane t < ntx holds transmit t's
-    // first element e0 and, through the scan, its offset in the stage; returns
-    // the stage base (offset - e0) of the lane's transmit and its count.
-    auto windows = [&](int it, int &base, int &cnt, int &e0_out, bool &staged) {
-        const int code = s_code[it];
-        staged = !(code & kItemUnstaged);
-        const int t0g = ((code >> 16) & 0xf) * kTapGroup, t1g = ((code >> 20) & 0xf) * kTapGroup;
-        const bool mine = lane >= t0g && lane < t1g && lane < ntx;
+    // producer (warp 0): windows of live receive `it` into slot it % kStages
+    auto produce = [&](int it) {
+        const int slot = it % kStages;
+        const int code = s_rx[it];
+        bool staged = !(code & 0x40000000);
+        const int r = code & 0x3fffffff;
         int e0 = 0, e1 = 0;
-        if (staged && mine) {
+        if (staged && lane < ntx) {
             const float xlo = __fadd_rn(s_txlh[2 * lane], s_rxlh[2 * it]);
             const float xhi = __fadd_rn(s_txlh[2 * lane + 1], s_rxlh[2 * it + 1]);
             staged_window<KIND, T>(xlo, xhi, a, e0, e1);
         }
-        cnt = e1 - e0;
+        const int cnt = e1 - e0;
         int off = cnt;
         for (int o = 1; o < 32; o <<= 1) {
             const int v = __shfl_up_sync(0xffffffffu, off, o);
@@ -436,40 +392,23 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         }
         const int total = __shfl_sync(0xffffffffu, off, 31);
         off -= cnt;
-        // the plan sized the windows to fit; a plan from other tables could not
-        if ((long long)total * (long long)sizeof(E) > kWindowBytes) staged = false;
-        base = staged && mine ? off - e0 : 0;
-        e0_out = e0;
-        if (!staged) cnt = 0;
-    };
-
-    // every warp stages its share of item `it`: the windows of transmits
-    // w, w+kWarps, ... and, per thread, its pixel's receive row entries
-    auto produce = [&](int it) {
-        const int slot = it % kStages;
-        unsigned char *st = smem_raw + (size_t)slot * kStageBytes;
-        const int r = s_code[it] & 0xffff;
-        if (valid) {
-            cp_async4(st + 4 * tid, a.taurx + (long long)r * np + i);
-            cp_async4(st + kRowBytes / 2 + 4 * tid, a.apodrx + (long long)r * np + i);
+        // the plan sized these windows to fit; a plan from other tables could
+        // not, and then this receive is gathered from global memory instead
+        if ((long long)total * (long long)sizeof(E) > kStageBytes) staged = false;
+        if (lane < kTxReg) sbase[slot][lane] = (staged && lane < ntx) ? off - e0 : 0;
+        if (lane == 0) sstaged[slot] = staged ? 1 : 0;
+        __syncwarp();
+        if (lane == 0) mbar_arrive_expect_tx(&full[slot], staged ? (unsigned)(total * sizeof(E)) : 0u);
+        __syncwarp();
+        if (staged && lane < ntx && cnt > 0) {
+            const E *src = static_cast<const E *>(a.data) + (frame_ch + (long long)lane * nrx + r) * a.nt + e0;
+            E *dst = reinterpret_cast<E *>(smem_raw + (size_t)slot * kStageBytes) + off;
+            tma_bulk_load(dst, src, (unsigned)(cnt * sizeof(E)), &full[slot]);
         }
-        int base, cnt, e0;
-        bool staged;
-        windows(it, base, cnt, e0, staged);
-        s_base[slot][w][lane] = base;
-        if (lane == 0) s_staged[slot][w] = staged ? 1 : 0;
-        if (staged) {
-            E *stage = reinterpret_cast<E *>(st + kRowBytes);
-            for (int t = w; t < ntx; t += kWarps) {
-                const int ct = __shfl_sync(0xffffffffu, cnt, t);
-                const int et = __shfl_sync(0xffffffffu, e0, t);
-                const int bt = __shfl_sync(0xffffffffu, base, t);
-                const E *src = static_cast<const E *>(a.data) + (frame_ch + (long long)t * nrx + r) * a.nt + et;
-                for (int k = lane * per16; k < ct; k += 32 * per16) cp_async16(stage + bt + et + k, src + k);
-            }
-        }
-        cp_async_arrive(&full[slot]);
     };
+    int produced = 0;  // iterations warp 0 has issued copies for
+    if (w == 0)
+        for (int it = 0; it < kStages && it < nlive; ++it) produce(it), produced = it + 1;
 
     // transmit side of this pixel; slots past ntx carry zero weights
     float rtau[kTxReg], rapod[kTxReg];
@@ -484,59 +423,52 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             amax = fmaxf(amax, fabsf(rapod[k]));
         }
     }
-    for (int it = 0; it < kAhead && it < nitems; ++it) produce(it);
 
-    float acc = 0.f, s1 = 0.f, accr = 0.f;
+    float acc = 0.f, s1 = 0.f;
     bool failed = false;
-    for (int it = 0; it < nitems; ++it) {
+    // receive-side values, fetched two receives ahead
+    auto rx_load = [&](int it, float &trx, float &arx) {
+        const int r = s_rx[it] & 0x3fffffff;
+        trx = valid ? __ldg(a.taurx + (long long)r * np + i) : 0.f;
+        arx = valid ? __ldg(a.apodrx + (long long)r * np + i) : 0.f;
+    };
+    float trx1 = 0.f, arx1 = 0.f, trx2 = 0.f, arx2 = 0.f;
+    if (nlive > 0) rx_load(0, trx1, arx1);
+    if (nlive > 1) rx_load(1, trx2, arx2);
+
+    for (int it = 0; it < nlive; ++it) {
         const int slot = it % kStages;
-        // stage item it + kAhead into the slot item it - 1 used, once every warp left it
-        const int p = it + kAhead;
-        if (p < nitems) {
-            if (it >= 1 && !mbar_wait_bounded(&empty[(it - 1) % kStages], (unsigned)((it - 1) / kStages) & 1u))
-                failed = true;
-            if (failed || *(volatile int *)&s_failed) {
-                failed = true;
-                s_failed = 1;
-                break;
-            }
-            produce(p);
-        }
+        const int r = s_rx[it] & 0x3fffffff;
+        const float trx = trx1, arx = arx1;
+        trx1 = trx2;
+        arx1 = arx2;
+        if (it + 2 < nlive) rx_load(it + 2, trx2, arx2);
         if (!mbar_wait_bounded(&full[slot], (unsigned)(it / kStages) & 1u)) failed = true;
         if (failed || *(volatile int *)&s_failed) {
             failed = true;
             s_failed = 1;
             break;
         }
-        const int code = s_code[it];
-        const int r = code & 0xffff;
-        const int g0 = (code >> 16) & 0xf, g1 = (code >> 20) & 0xf;
-        const float *rows = reinterpret_cast<const float *>(smem_raw + (size_t)slot * kStageBytes);
-        const float trx = rows[tid], arx = rows[kBlock + tid];  // not copied past the last pixel: unused
 
-        __syncwarp();
-        const bool staged = s_staged[slot][w] != 0;
         const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh);
+        float accr = 0.f;
         if (live) {
             const long long ch_first = (frame_ch + r) * a.nt;
-            if (staged) {
-                const E *stage =
-                    reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes + kRowBytes);
+            if (sstaged[slot]) {
+                const E *stage = reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes);
 #pragma unroll
-                for (int gg = 0; gg < kTxGroups; ++gg) {
-                    if (gg >= g0 && gg < g1) {
-                        const int g = gg * kTapGroup;
-                        const int4 b4 = *reinterpret_cast<const int4 *>(&s_base[slot][w][g]);
-                        const int bk[kTapGroup] = {b4.x, b4.y, b4.z, b4.w};
+                for (int g = 0; g < kTxReg; g += kTapGroup) {
+                    if (g < ntx) {
+                        const int4 b = *reinterpret_cast<const int4 *>(&sbase[slot][g]);
+                        const int bk[kTapGroup] = {b.x, b.y, b.z, b.w};
                         accr = staged_group<KIND, T, true>(a, rtau + g, rapod + g, trx, arx, bk,
                                                            stage, ch_first, chs, g, ntx, accr);
                     }
                 }
             } else {
 #pragma unroll
-                for (int gg = 0; gg < kTxGroups; ++gg) {
-                    if (gg >= g0 && gg < g1) {
-                        const int g = gg * kTapGroup;
+                for (int g = 0; g < kTxReg; g += kTapGroup) {
+                    if (g < ntx) {
                         const int bk[kTapGroup] = {0, 0, 0, 0};
                         accr = staged_group<KIND, T, false>(a, rtau + g, rapod + g, trx, arx, bk,
                                                             nullptr, ch_first, chs, g, ntx, accr);
@@ -544,24 +476,38 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
                 }
             }
         }
-        if (code & kItemLast) {  // this receive is complete
-            if (SUM == PYCBF_GB_SUM_TX_AND_RX) acc += accr;
-            if (SUM == PYCBF_GB_SUM_TX_ONLY && valid) a.out[((long long)f * nrx + r) * np + op] = accr;
-            if (SUM == PYCBF_GB_SUM_DMAS_SSR || SUM == PYCBF_GB_SUM_DMAS_POWER) {
-                const float sv = (SUM == PYCBF_GB_SUM_DMAS_SSR) ? copysignf(sqrtf(fabsf(accr)), accr) : accr;
-                acc = fmaf(sv, s1, acc);
-                s1 += sv;
-            }
-            accr = 0.f;
+        if (SUM == PYCBF_GB_SUM_TX_AND_RX) acc += accr;
+        if (SUM == PYCBF_GB_SUM_TX_ONLY && valid) a.out[((long long)f * nrx + r) * np + op] = accr;
+        if (SUM == PYCBF_GB_SUM_DMAS_SSR || SUM == PYCBF_GB_SUM_DMAS_POWER) {
+            const float s = (SUM == PYCBF_GB_SUM_DMAS_SSR) ? copysignf(sqrtf(fabsf(accr)), accr) : accr;
+            acc = fmaf(s, s1, acc);
+            s1 += s;
         }
+        // this warp is done with the slot
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[slot]);
+        // warp 0 refills the slot of the previous iteration once every warp left it
+        if (w == 0 && it >= 1 && it - 1 + kStages < nlive) {
+            const int pit = it - 1;
+            if (!mbar_wait_bounded(&empty[pit % kStages], (unsigned)(pit / kStages) & 1u)) {
+                failed = true;
+                s_failed = 1;
+                break;
+            }
+            produce(pit + kStages);
+            produced = pit + kStages + 1;
+        }
     }
-    // every thread's own copies are complete before the shared memory goes away
-    cp_async_wait_all();
     __syncthreads();
     if (s_failed) {
-        if (tid == 0 && status) atomicExch(status, 1);
+        // drain the copies still in flight before the CTA's shared memory goes
+        // away: the latest phase of each slot is one of the last kStages issued
+        if (tid == 0) {
+            if (status) atomicExch(status, 1);
+            for (int j = max(0, produced - kStages); j < produced; ++j)
+                (void)mbar_wait_bounded(&full[j % kStages], (unsigned)(j / kStages) & 1u);
+        }
+        __syncthreads();
         if (valid) {
             const float nan = __int_as_float(0x7fc00000);
             if (SUM == PYCBF_GB_SUM_TX_ONLY)
@@ -575,7 +521,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
 }
 
 inline size_t staged_smem_bytes(int nrx) {
-    return (size_t)kStages * kStageBytes + sizeof(int) * 3 * (size_t)nrx * kTxGroups;
+    return (size_t)kStages * kStageBytes + sizeof(int) * 3 * (size_t)nrx;
 }
 
 template <int KIND, typename T>
