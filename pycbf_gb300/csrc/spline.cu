@@ -7,8 +7,9 @@
 // contract by |0.5/p| -> 2 - sqrt(3) = 0.268 per step, so a lane can start
 // either sweep 32 samples before its chunk from zero: the start error has
 // shrunk by 0.268^32 ~ 5e-19 when the chunk begins.  Each of the 32 lanes
-// owns a contiguous chunk of the channel; the channel, u and y2 sit in shared
-// memory.  Output per sample j: (y_j, y_j+1, z_j, z_j+1), z = y2 dx^2 / 6,
+// owns a contiguous chunk of the channel (of odd length, so that the lanes'
+// sequential sweeps fall in distinct shared-memory banks); the channel, u and
+// y2 sit in shared memory.  Output per sample j: (y_j, y_j+1, z_j, z_j+1), z = y2 dx^2 / 6,
 // with y_nt = z_nt = 0, so the forward kernel does one 16-byte (or 8-byte)
 // load per tap.
 #include <algorithm>
@@ -73,7 +74,8 @@ spline_coef_kernel(const T *__restrict__ rf, typename CoefRec<T>::raw *__restric
     const float inv_dt = 1.0f / dt;
     const float cscale = 6.0f / (2.0f * dt);
     const float zscale = dt * dt / 6.0f;
-    const int C = (nt + 31) >> 5;
+    // chunk length odd: lane l then reads word l*C + i, a distinct bank per lane
+    const int C = ((nt + 31) >> 5) | 1;
     const int s = lane * C;
     const int e = min(s + C, nt);
 
