@@ -228,6 +228,30 @@ int pycbf_gb_slsc(const float *im, const unsigned char *mask, long long nframes,
                   int nz, int nlag, int nkern, float *out, void *stream);
 
 /* ---------------------------------------------------------------------- */
+/* Cubic Tabbed delay-and-sum that allocates nothing (no counterpart in    */
+/* the reference).  For callers that cannot call cudaMalloc -- a language  */
+/* runtime reaching CUDA only through this C ABI, a service whose device   */
+/* memory is fixed at start-up, code that must not trigger the implicit    */
+/* synchronisation of an allocation -- and so cannot provide the workspace */
+/* pycbf_gb_das_tabbed needs for cubic interpolation.  The spline          */
+/* coefficients live in a device array of PYCBF_GB_NOALLOC_SCRATCH_BYTES   */
+/* inside this library, held by every GPU that loads it until the process */
+/* exits.  Channel data whose coefficients                                 */
+/* (pycbf_gb_workspace_bytes(rf, PYCBF_GB_INTERP_CUBIC)) exceed it are      */
+/* rejected with PYCBF_GB_ERANGE.  The first call on a device looks up the */
+/* array's address on that device; make it before any stream capture.     */
+/* All calls share the array: calls whose work overlaps on the GPU (other  */
+/* streams, other host threads) race on it.  Other arguments and results   */
+/* are those of pycbf_gb_das_tabbed with interp = cubic and no plan.       */
+/* ---------------------------------------------------------------------- */
+#define PYCBF_GB_NOALLOC_SCRATCH_BYTES (64u << 20)
+int pycbf_gb_das_tabbed_cubic_noalloc(const pycbf_gb_rfinfo *rf, const void *rfdata,
+                                      const float *tautx, const float *apodtx,
+                                      const float *taurx, const float *apodrx, long long np,
+                                      const int *pixel_index, float thresh, int sumtype,
+                                      float *out, void *stream);
+
+/* ---------------------------------------------------------------------- */
 /* Measurement utility (no counterpart in the reference): blocks x 256    */
 /* threads each run iters rounds of 8 independent float32 FMAs and store  */
 /* one float to out[blocks*256].  FLOPs = blocks*256*iters*16.  Gives the */
