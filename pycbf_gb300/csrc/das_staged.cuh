@@ -340,6 +340,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     __shared__ int sstaged[kStages];
     __shared__ float s_txlh[2 * kTxReg];
     __shared__ int s_failed;
+    __shared__ int s_produced;  // receives whose copies have been issued
     // the tile's plan: live receive indices and their delay bounds
     int *s_rx = reinterpret_cast<int *>(smem_raw + kStages * kStageBytes);
     float *s_rxlh = reinterpret_cast<float *>(s_rx + a.nrx);
@@ -368,11 +369,14 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         const float *rxlh = reinterpret_cast<const float *>(rec + 1 + nrx);
         for (int k = tid; k < 2 * nlive; k += kBlock) s_rxlh[k] = __ldg(rxlh + k);
     }
-    if (tid == 0) s_failed = 0;
+    if (tid == 0) {
+        s_failed = 0;
+        s_produced = 0;
+    }
     mbar_fence_init();
     __syncthreads();
 
-    // producer (warp 0): windows of live receive `it` into slot it % kStages
+    // producer: windows of live receive `it` into slot it % kStages
     auto produce = [&](int it) {
         const int slot = it % kStages;
         const int code = s_rx[it];
@@ -406,9 +410,13 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             tma_bulk_load(dst, src, (unsigned)(cnt * sizeof(E)), &full[slot]);
         }
     };
-    int produced = 0;  // iterations warp 0 has issued copies for
-    if (w == 0)
-        for (int it = 0; it < kStages && it < nlive; ++it) produce(it), produced = it + 1;
+    // warp 0 stages the first kStages receives; after that the producer role
+    // rotates over the warps (a bulk copy costs ~100 cycles to issue, and one
+    // warp issuing every receive's copies starved the others)
+    if (w == 0) {
+        for (int it = 0; it < kStages && it < nlive; ++it) produce(it);
+        if (lane == 0) atomicMax(&s_produced, min(kStages, nlive));
+    }
 
     // transmit side of this pixel; slots past ntx carry zero weights
     float rtau[kTxReg], rapod[kTxReg];
@@ -486,8 +494,9 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         // this warp is done with the slot
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[slot]);
-        // warp 0 refills the slot of the previous iteration once every warp left it
-        if (w == 0 && it >= 1 && it - 1 + kStages < nlive) {
+        // warp it % kWarps refills the slot of the previous iteration once every
+        // warp left it
+        if (w == it % kWarps && it >= 1 && it - 1 + kStages < nlive) {
             const int pit = it - 1;
             if (!mbar_wait_bounded(&empty[pit % kStages], (unsigned)(pit / kStages) & 1u)) {
                 failed = true;
@@ -495,7 +504,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
                 break;
             }
             produce(pit + kStages);
-            produced = pit + kStages + 1;
+            if (lane == 0) atomicMax(&s_produced, pit + kStages + 1);
         }
     }
     __syncthreads();
@@ -504,6 +513,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         // away: the latest phase of each slot is one of the last kStages issued
         if (tid == 0) {
             if (status) atomicExch(status, 1);
+            const int produced = *(volatile int *)&s_produced;
             for (int j = max(0, produced - kStages); j < produced; ++j)
                 (void)mbar_wait_bounded(&full[j % kStages], (unsigned)(j / kStages) & 1u);
         }
