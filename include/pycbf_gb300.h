@@ -252,6 +252,46 @@ int pycbf_gb_das_tabbed_cubic_noalloc(const pycbf_gb_rfinfo *rf, const void *rfd
                                       float *out, void *stream);
 
 /* ---------------------------------------------------------------------- */
+/* Differentiable cubic delay-and-sum (no counterpart in the reference,   */
+/* whose beamformers are forward-only).  Inputs are spline coefficients    */
+/* from pycbf_gb_spline_coefficients; sumtype is PYCBF_GB_SUM_TX_AND_RX    */
+/* (gradient and image (nframes, np)) or PYCBF_GB_SUM_TX_ONLY ((nframes,   */
+/* nrx, np)); ntx <= 128.                                                  */
+/*                                                                        */
+/* The Synthetic form replaces 1/c0 by a slowness per pixel s[i] (s/m, in  */
+/* table-column order): every delay is its path length times s[i] (plus    */
+/* t0tx for the focused transmits), with the masks of                      */
+/* pycbf_gb_das_synthetic.  geo->c0 is not used.                           */
+/*                                                                        */
+/* The adjoints take the upstream gradient grad_out (shaped like the       */
+/* image, indexed through pixel_index like it) and write, each only when   */
+/* its pointer is not NULL:                                                */
+/*   grad_rf     (nframes, ntx, nrx, nt) float32 whatever the storage;     */
+/*               needs pycbf_gb_adjoint_workspace_bytes of workspace       */
+/*   grad_tautx  (ntx, np), grad_taurx (nrx, np): Tabbed, summed over      */
+/*               frames, table-column order                                */
+/*   grad_slow   (np): Synthetic, summed over frames                       */
+/* All outputs are overwritten; every sum has a fixed order, so results    */
+/* are bitwise reproducible.  Apodization is not differentiated.           */
+/* ---------------------------------------------------------------------- */
+int pycbf_gb_das_synthetic_slowness(const pycbf_gb_rfinfo *rf, const void *coef,
+                                    const pycbf_gb_synthetic *geo, const float *slowness,
+                                    const int *pixel_index, int sumtype, float *out,
+                                    void *stream);
+size_t pycbf_gb_adjoint_workspace_bytes(const pycbf_gb_rfinfo *rf, long long np);
+int pycbf_gb_das_tabbed_adjoint(const pycbf_gb_rfinfo *rf, const void *coef,
+                                const float *tautx, const float *apodtx, const float *taurx,
+                                const float *apodrx, long long np, const int *pixel_index,
+                                float thresh, int sumtype, const float *grad_out,
+                                float *grad_rf, float *grad_tautx, float *grad_taurx,
+                                void *workspace, size_t workspace_bytes, void *stream);
+int pycbf_gb_das_synthetic_adjoint(const pycbf_gb_rfinfo *rf, const void *coef,
+                                   const pycbf_gb_synthetic *geo, const float *slowness,
+                                   const int *pixel_index, int sumtype, const float *grad_out,
+                                   float *grad_rf, float *grad_slow, void *workspace,
+                                   size_t workspace_bytes, void *stream);
+
+/* ---------------------------------------------------------------------- */
 /* Measurement utility (no counterpart in the reference): blocks x 256    */
 /* threads each run iters rounds of 8 independent float32 FMAs and store  */
 /* one float to out[blocks*256].  FLOPs = blocks*256*iters*16.  Gives the */

@@ -27,7 +27,9 @@ EXPORTS = (
     "pycbf_gb_das_tabbed_prefiltered", "pycbf_gb_tabbed_plan_bytes", "pycbf_gb_tabbed_plan",
     "pycbf_gb_das_synthetic", "pycbf_gb_tap_census_tabbed", "pycbf_gb_tap_census_synthetic",
     "pycbf_gb_synthetic_rx_mask", "pycbf_gb_dmas", "pycbf_gb_slsc", "pycbf_gb_fp32_probe",
-    "pycbf_gb_das_tabbed_cubic_noalloc",
+    "pycbf_gb_das_tabbed_cubic_noalloc", "pycbf_gb_das_synthetic_slowness",
+    "pycbf_gb_adjoint_workspace_bytes", "pycbf_gb_das_tabbed_adjoint",
+    "pycbf_gb_das_synthetic_adjoint",
 )
 NOALLOC_SCRATCH_BYTES = 64 << 20
 
@@ -90,10 +92,18 @@ def load() -> ct.CDLL:
         L.pycbf_gb_fp32_probe.argtypes = [vp, i, i, vp]
         L.pycbf_gb_das_tabbed_cubic_noalloc.argtypes = [P(RFInfo), vp, vp, vp, vp, vp, ll, vp, f, i,
                                                         vp, vp]
+        L.pycbf_gb_das_synthetic_slowness.argtypes = [P(RFInfo), vp, P(SyntheticGeom), vp, vp, i,
+                                                      vp, vp]
+        L.pycbf_gb_adjoint_workspace_bytes.argtypes = [P(RFInfo), ll]
+        L.pycbf_gb_adjoint_workspace_bytes.restype = sz
+        L.pycbf_gb_das_tabbed_adjoint.argtypes = [P(RFInfo), vp, vp, vp, vp, vp, ll, vp, f, i, vp,
+                                                  vp, vp, vp, vp, sz, vp]
+        L.pycbf_gb_das_synthetic_adjoint.argtypes = [P(RFInfo), vp, P(SyntheticGeom), vp, vp, i,
+                                                     vp, vp, vp, vp, sz, vp]
         for name in EXPORTS:
             if name not in ("pycbf_gb_abi_version", "pycbf_gb_status_string",
                             "pycbf_gb_last_cuda_error", "pycbf_gb_workspace_bytes",
-                            "pycbf_gb_tabbed_plan_bytes"):
+                            "pycbf_gb_tabbed_plan_bytes", "pycbf_gb_adjoint_workspace_bytes"):
                 getattr(L, name).restype = i
         _lib = L
         return L

@@ -325,6 +325,14 @@ class _GPUBeamformer(Beamformer):
     def _launch(self, rf, info, out, sumtype_code):
         raise NotImplementedError
 
+    def _autograd_input(self, txrxt):
+        if not isinstance(txrxt, torch.Tensor):
+            raise BeamformerException("the differentiable path takes torch tensors")
+        if txrxt.ndim not in (3, 4) or tuple(txrxt.shape[-3:]) != (self.ntx, self.nrx, self.nt):
+            raise BeamformerException(
+                f"'txrxt' must be ({self.ntx}, {self.nrx}, {self.nt}) or 4-D with those last axes")
+        return txrxt.to(device="cuda", dtype=self._torch_dtype)
+
     def _beamform(self, txrxt, buffer=None, sumtype=None):
         rf, nframes = self._prepare_input(txrxt)
         info = self._rfinfo(nframes, getattr(self, "ndimp", 0) if isinstance(self, Synthetic) else 0)
@@ -385,6 +393,31 @@ class TabbedBeamformer(Tabbed, _GPUBeamformer):
             self.nop, _ptr(self._pixel_index), self._interp_code, float(np.float32(self.thresh)),
             sumtype_code, _ptr(self._plan), _ptr(out), _ptr(ws), nws, _stream_ptr())
         _lib.check(st, "pycbf_gb_das_tabbed")
+
+    def differentiable(self, txrxt, tautx=None, taurx=None, sumtype=None):
+        """Cubic delay-and-sum through torch autograd (pycbf_gb300.adjoint.das_tabbed).
+
+        txrxt: torch CUDA tensor (ntx, nrx, nt) or (nframes, ntx, nrx, nt);
+        tautx / taurx: optional (ntx, nop) / (nrx, nop) tensors in the
+        original pixel order replacing the constructor's tables (e.g.
+        learnable delays).  sumtype 'tx_and_rx' or 'tx_only'.  Returns a CUDA
+        float32 tensor of the usual output shape, differentiable with respect
+        to txrxt and the given delay tables.
+        """
+        from . import adjoint
+        if self._interp_code != _lib.INTERP["cubic"]:
+            raise BeamformerException("the differentiable path interpolates with the cubic spline")
+        rf = self._autograd_input(txrxt)
+        ktx, kap_tx, krx, kap_rx = self._tables
+        perm = None if self._pixel_index is None else self._pixel_index.long()
+        order = (lambda t: t) if perm is None else (lambda t: t[:, perm])
+        if tautx is not None:
+            ktx = order(tautx.to(device="cuda", dtype=torch.float32))
+        if taurx is not None:
+            krx = order(taurx.to(device="cuda", dtype=torch.float32))
+        return adjoint.das_tabbed(rf, ktx, krx, kap_tx, kap_rx, t0=self.t0, dt=self.dt,
+                                  thresh=self.thresh, sumtype=sumtype or self.sumtype,
+                                  pixel_index=self._pixel_index)
 
     def kernel_status(self) -> int:
         """0, or 1 if a staged launch gave up a bounded wait (its outputs are NaN)."""
@@ -466,6 +499,25 @@ class SyntheticBeamformer(Synthetic, _GPUBeamformer):
             ct.byref(info), _ptr(rf), ct.byref(self._geom), _ptr(self._pixel_index),
             self._interp_code, sumtype_code, _ptr(out), _ptr(ws), nws, _stream_ptr())
         _lib.check(st, "pycbf_gb_das_synthetic")
+
+    def differentiable(self, txrxt, slowness=None, sumtype=None):
+        """Cubic delay-and-sum with a slowness per pixel, through torch autograd
+        (pycbf_gb300.adjoint.das_synthetic_slowness).
+
+        slowness: (nop,) tensor in the original point order, s/m; default
+        1/c0 everywhere.  Every delay is path length x slowness (plus t0tx
+        for focused transmits).  Returns a CUDA float32 tensor of the usual
+        output shape for sumtype 'tx_and_rx' or 'tx_only', differentiable with
+        respect to txrxt and slowness.
+        """
+        from . import adjoint
+        if self._interp_code != _lib.INTERP["cubic"]:
+            raise BeamformerException("the differentiable path interpolates with the cubic spline")
+        rf = self._autograd_input(txrxt)
+        if slowness is None:
+            slowness = torch.full((self.nop,), 1.0 / float(self.c0), dtype=torch.float32,
+                                  device="cuda")
+        return adjoint.das_synthetic_slowness(rf, slowness, self, sumtype=sumtype or self.sumtype)
 
     def tap_census(self):
         info = self._rfinfo(1, self.ndimp)

@@ -358,3 +358,117 @@ int pycbf_gb_slsc(const float *im, const unsigned char *mask, long long nframes,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// differentiable cubic delay-and-sum
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr long long kMaxAdjTx = 128;  // three shared-memory columns per transmit (192 KB)
+
+int check_adjoint_common(const pycbf_gb_rfinfo *rf, const void *coef, int sumtype, bool synthetic) {
+    int st = check_rf(rf, synthetic);
+    if (st) return st;
+    if (!coef || reinterpret_cast<uintptr_t>(coef) % 16) return PYCBF_GB_EINVAL;
+    if (sumtype != PYCBF_GB_SUM_TX_AND_RX && sumtype != PYCBF_GB_SUM_TX_ONLY)
+        return PYCBF_GB_EUNSUPPORTED;
+    if (rf->ntx > kMaxAdjTx || rf->nt > kMaxNtSpline || !adjoint_rows_warps(rf->nt))
+        return PYCBF_GB_ERANGE;
+    return PYCBF_GB_OK;
+}
+
+int run_adjoint(const pycbf_gb_rfinfo *rf, AdjArgs &g, void *workspace, size_t workspace_bytes,
+                cudaStream_t s) {
+    if (g.grad_rf) {
+        const size_t need = pycbf_gb_adjoint_workspace_bytes(rf, g.d.np);
+        if (!workspace || workspace_bytes < need || reinterpret_cast<uintptr_t>(workspace) % 16)
+            return PYCBF_GB_EWORKSPACE;
+        g.partial = static_cast<float *>(workspace);
+    }
+    return cuda_status(launch_adjoint(g, rf->dtype, s));
+}
+
+}  // namespace
+
+extern "C" {
+
+int pycbf_gb_das_synthetic_slowness(const pycbf_gb_rfinfo *rf, const void *coef,
+                                    const pycbf_gb_synthetic *geo, const float *slowness,
+                                    const int *pixel_index, int sumtype, float *out,
+                                    void *stream) {
+    int st = check_adjoint_common(rf, coef, sumtype, true);
+    if (st) return st;
+    if (!geo_ok(geo) || !slowness || !out) return PYCBF_GB_EINVAL;
+    if (!das_shape_ok(GEOM_SYNTH, sumtype, rf->ntx)) return PYCBF_GB_ERANGE;
+    DasArgs a = {};
+    fill_time_axis(a, rf);
+    a.data = coef;
+    a.geo = *geo;
+    a.ndim = rf->ndim;
+    a.pixel_index = pixel_index;
+    a.out = out;
+    a.np = geo->np;
+    a.slow = slowness;
+    return cuda_status(launch_das_synth_slow(a, sumtype, rf->dtype, static_cast<cudaStream_t>(stream)));
+}
+
+size_t pycbf_gb_adjoint_workspace_bytes(const pycbf_gb_rfinfo *rf, long long np) {
+    if (!rf || np <= 0 || rf->ntx <= 0 || rf->nrx <= 0 || rf->nt <= 0 || rf->nframes <= 0) return 0;
+    return adjoint_workspace_bytes(rf->nframes * rf->ntx * rf->nrx, np, rf->nt);
+}
+
+int pycbf_gb_das_tabbed_adjoint(const pycbf_gb_rfinfo *rf, const void *coef,
+                                const float *tautx, const float *apodtx, const float *taurx,
+                                const float *apodrx, long long np, const int *pixel_index,
+                                float thresh, int sumtype, const float *grad_out,
+                                float *grad_rf, float *grad_tautx, float *grad_taurx,
+                                void *workspace, size_t workspace_bytes, void *stream) {
+    int st = check_adjoint_common(rf, coef, sumtype, false);
+    if (st) return st;
+    if (!tautx || !apodtx || !taurx || !apodrx || !grad_out || std::isnan(thresh))
+        return PYCBF_GB_EINVAL;
+    if (np <= 0 || np >= (1LL << 31)) return np == 0 ? PYCBF_GB_OK : PYCBF_GB_ERANGE;
+    AdjArgs g = {};
+    fill_time_axis(g.d, rf);
+    g.d.data = coef;
+    g.d.tautx = tautx;
+    g.d.apodtx = apodtx;
+    g.d.taurx = taurx;
+    g.d.apodrx = apodrx;
+    g.d.pixel_index = pixel_index;
+    g.d.np = np;
+    g.d.thresh = thresh;
+    g.geom = GEOM_TABBED;
+    g.sumtype = sumtype;
+    g.gout = grad_out;
+    g.grad_rf = grad_rf;
+    g.grad_tautx = grad_tautx;
+    g.grad_taurx = grad_taurx;
+    return run_adjoint(rf, g, workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
+}
+
+int pycbf_gb_das_synthetic_adjoint(const pycbf_gb_rfinfo *rf, const void *coef,
+                                   const pycbf_gb_synthetic *geo, const float *slowness,
+                                   const int *pixel_index, int sumtype, const float *grad_out,
+                                   float *grad_rf, float *grad_slow, void *workspace,
+                                   size_t workspace_bytes, void *stream) {
+    int st = check_adjoint_common(rf, coef, sumtype, true);
+    if (st) return st;
+    if (!geo_ok(geo) || !slowness || !grad_out) return PYCBF_GB_EINVAL;
+    AdjArgs g = {};
+    fill_time_axis(g.d, rf);
+    g.d.data = coef;
+    g.d.geo = *geo;
+    g.d.ndim = rf->ndim;
+    g.d.pixel_index = pixel_index;
+    g.d.np = geo->np;
+    g.d.slow = slowness;
+    g.geom = GEOM_SYNTH_SLOW;
+    g.sumtype = sumtype;
+    g.gout = grad_out;
+    g.grad_rf = grad_rf;
+    g.grad_slow = grad_slow;
+    return run_adjoint(rf, g, workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,436 @@
+// Gradients of the cubic delay-and-sum (no reference counterpart).
+//
+// Forward (per frame f, pixel p, summed over the taps that contribute):
+//   img[p] += w * S_ch(x),  x = tau_tx(p) + tau_rx(p),  ch = (f, tx, rx)
+//   S(x) = a y_j + b y_j+1 + (a^3 - a) z_j + (b^3 - b) z_j+1
+// with the knot j, fractions a, b and the records (y, z) of the spline
+// prefilter, z = 1/2 T^-1 D y (T = tridiag(0.5, 2, 0.5) on the interior
+// samples, D the second difference; natural ends z_0 = z_nt-1 = 0).
+//
+// Three kernels, all deterministic (no atomics; every sum has a fixed order):
+//   adj_delay_kernel    one thread per pixel: dL/dx = g w S'(x) summed into
+//                       dL/dtau_tx (ntx, np) and dL/dtau_rx (nrx, np) for
+//                       Tabbed tables, or into dL/ds (np) for the Synthetic
+//                       slowness form (x = (D_tx + D_rx) s + t0).
+//   adj_scatter_kernel  one CTA per (channel, part of the pixel range): the
+//                       transpose of the interpolation.  Each warp owns two
+//                       shared-memory rows (dL/dy, dL/dz) of the channel; the
+//                       taps of one warp step are grouped by knot with
+//                       match.any and each group's weights are summed in lane
+//                       order by its lowest lane, which alone updates the rows
+//                       (so no two lanes ever touch one word together).  The
+//                       warp rows are added in warp order into the part's row.
+//   adj_finalize_kernel one warp per channel: adds the parts in order, then
+//                       the adjoint of the prefilter, dL/drf = dL/dy +
+//                       1/2 D^T T^-1 dL/dz (T is symmetric: the same chunked
+//                       Thomas recurrences as the forward prefilter).
+// Delays are recomputed from the tables or the geometry, never stored per tap;
+// the tap decisions (range, threshold, correctly rounded knot) are the forward's.
+#include <algorithm>
+
+#include "das_impl.cuh"
+
+namespace pgb {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kWarmAdj = 32;  // warm-up of the chunked recurrences (0.268^32 ~ 5e-19)
+constexpr size_t kRowSmemMax = 160 * 1024;
+
+// The forward's decisions for one cubic tap; fractions only where it is in range.
+__device__ __forceinline__ bool cubic_tap(float x, const DasArgs &a, int &j, float &am, float &b) {
+    using K = Kind<PYCBF_GB_INTERP_CUBIC, float>;
+    int idx;
+    bool fix;
+    bool inr = K::index(x, a, idx, fix);
+    if (fix) inr = K::index_exact(x, a, idx);
+    j = idx;
+    am = b = 0.f;
+    if (inr) knot_fractions(x, (float)idx, a, am, b);
+    return inr;
+}
+
+// dS/dx: d(a)/dx = -1/dt, d(b)/dx = 1/dt
+__device__ __forceinline__ float cubic_slope(const float4 &c, float am, float b, float inv_dt) {
+    const float da = fmaf(3.f * am, am, -1.f);
+    const float db = fmaf(3.f * b, b, -1.f);
+    return (c.y - c.x + fmaf(db, c.w, -da * c.z)) * inv_dt;
+}
+
+__device__ __forceinline__ float upstream(const AdjArgs &g, int sum, int f, int r, long long op) {
+    const DasArgs &a = g.d;
+    return sum == PYCBF_GB_SUM_TX_AND_RX ? __ldg(g.gout + (long long)f * a.np + op)
+                                         : __ldg(g.gout + ((long long)f * a.nrx + r) * a.np + op);
+}
+
+// ---------------------------------------------------------------------------
+// delays / slowness: gather per pixel
+// ---------------------------------------------------------------------------
+template <int GEOM, int SUM, typename T>
+__global__ void __launch_bounds__(kBlock) adj_delay_kernel(const __grid_constant__ AdjArgs g) {
+    using rec = typename CoefRec<T>::raw;
+    const DasArgs &a = g.d;
+    extern __shared__ float sm[];
+    const int tid = threadIdx.x;
+    const long long i = (long long)blockIdx.x * kBlock + tid;
+    if (i >= a.np) return;
+    const long long np = a.np;
+    const int ntx = a.ntx, nrx = a.nrx, nfr = a.nframes, nt = a.nt;
+    const long long op = a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i;
+    const rec *coef = static_cast<const rec *>(a.data);
+    // this thread's columns: transmit delay, apodization (Tabbed) or path
+    // length (Synthetic), and the dL/dtau_tx accumulator
+    float *stau = sm + tid;
+    float *sw = stau + (size_t)ntx * kBlock;
+    float *sg = sw + (size_t)ntx * kBlock;
+
+    float pnt[3] = {0.f, 0.f, 0.f};
+    float slow = 0.f;
+    if (GEOM == GEOM_SYNTH_SLOW) {
+        for (int k = 0; k < a.ndim; ++k) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
+        slow = __ldg(a.slow + i);
+    }
+    for (int t = 0; t < ntx; ++t) {
+        if (GEOM == GEOM_TABBED) {
+            stau[(size_t)t * kBlock] = __ldg(a.tautx + (long long)t * np + i);
+            sw[(size_t)t * kBlock] = __ldg(a.apodtx + (long long)t * np + i);
+            sg[(size_t)t * kBlock] = 0.f;
+        } else {
+            float D, t0add;
+            const bool ok = synth_tx_path(a, t, pnt, D, t0add);
+            stau[(size_t)t * kBlock] = slow_delay(ok, D, slow, t0add);
+            sw[(size_t)t * kBlock] = D;
+        }
+    }
+
+    float gs = 0.f;
+    for (int r = 0; r < nrx; ++r) {
+        float trx, arx = 1.f, Drx = 0.f;
+        if (GEOM == GEOM_TABBED) {
+            trx = __ldg(a.taurx + (long long)r * np + i);
+            arx = __ldg(a.apodrx + (long long)r * np + i);
+        } else {
+            const bool ok = synth_rx_path(a, r, pnt, Drx);
+            if (!ok) continue;
+            trx = slow_delay(true, Drx, slow, 0.f);
+        }
+        float grx = 0.f;
+        for (int t = 0; t < ntx; ++t) {
+            const float x = __fadd_rn(stau[(size_t)t * kBlock], trx);
+            float apod = 1.f;
+            if (GEOM == GEOM_TABBED) {
+                apod = __fmul_rn(sw[(size_t)t * kBlock], arx);
+                if (!(fabsf(apod) >= a.thresh)) continue;
+            }
+            int j;
+            float am, b;
+            if (!cubic_tap(x, a, j, am, b)) continue;
+            float sum = 0.f;
+            for (int f = 0; f < nfr; ++f) {
+                const float gp = upstream(g, SUM, f, r, op);
+                const float4 c =
+                    CoefRec<T>::load(coef + (((long long)f * ntx + t) * nrx + r) * nt + j);
+                sum = fmaf(gp, cubic_slope(c, am, b, a.inv_dt), sum);
+            }
+            if (GEOM == GEOM_TABBED) {
+                const float d = apod * sum;
+                sg[(size_t)t * kBlock] += d;
+                grx += d;
+            } else {
+                gs = fmaf(sum, sw[(size_t)t * kBlock] + Drx, gs);  // dx/ds = D_tx + D_rx
+            }
+        }
+        if (GEOM == GEOM_TABBED && g.grad_taurx) g.grad_taurx[(long long)r * np + i] = grx;
+    }
+    if (GEOM == GEOM_TABBED && g.grad_tautx)
+        for (int t = 0; t < ntx; ++t) g.grad_tautx[(long long)t * np + i] = sg[(size_t)t * kBlock];
+    if (GEOM == GEOM_SYNTH_SLOW && g.grad_slow) g.grad_slow[i] = gs;
+}
+
+// ---------------------------------------------------------------------------
+// channel data: transpose of the interpolation, per (channel, part)
+// ---------------------------------------------------------------------------
+template <int GEOM, int SUM>
+__global__ void __launch_bounds__(128) adj_scatter_kernel(const __grid_constant__ AdjArgs g,
+                                                          long long part_len, int Lp) {
+    const DasArgs &a = g.d;
+    extern __shared__ float rows[];  // [warp][2][Lp]: dL/dy, dL/dz
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const long long np = a.np;
+    const int ntx = a.ntx, nrx = a.nrx;
+    const long long nch = (long long)a.nframes * ntx * nrx;
+    const long long c = blockIdx.x;  // channel ((f * ntx + t) * nrx + r)
+    const int q = blockIdx.y;        // part
+    const int r = (int)(c % nrx);
+    const int t = (int)((c / nrx) % ntx);
+    const int f = (int)(c / ((long long)nrx * ntx));
+    float *ry = rows + (size_t)w * 2 * Lp;
+    float *rz = ry + Lp;
+    for (int n = lane; n < 2 * Lp; n += 32) ry[n] = 0.f;
+    __syncwarp();
+
+    const long long i0 = (long long)q * part_len;
+    const long long i1 = min(np, i0 + part_len);
+    for (long long base = i0; base < i1; base += blockDim.x) {
+        const long long i = base + threadIdx.x;
+        bool hit = false;
+        int j = 0;
+        float am = 0.f, b = 0.f, v = 0.f;
+        if (i < i1) {
+            float x = 0.f, apod = 1.f;
+            bool live;
+            if (GEOM == GEOM_TABBED) {
+                apod = __fmul_rn(__ldg(a.apodtx + (long long)t * np + i),
+                                 __ldg(a.apodrx + (long long)r * np + i));
+                live = fabsf(apod) >= a.thresh;
+                if (live)
+                    x = __fadd_rn(__ldg(a.tautx + (long long)t * np + i),
+                                  __ldg(a.taurx + (long long)r * np + i));
+            } else {
+                float pnt[3] = {0.f, 0.f, 0.f};
+                for (int k = 0; k < a.ndim; ++k) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
+                const float slow = __ldg(a.slow + i);
+                float Dt, t0add, Dr;
+                const bool okt = synth_tx_path(a, t, pnt, Dt, t0add);
+                const bool okr = synth_rx_path(a, r, pnt, Dr);
+                live = okt && okr;
+                if (live) x = __fadd_rn(slow_delay(true, Dt, slow, t0add), slow_delay(true, Dr, slow, 0.f));
+            }
+            if (live && cubic_tap(x, a, j, am, b)) {
+                hit = true;
+                const long long op = a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i;
+                v = upstream(g, SUM, f, r, op);
+                if (GEOM == GEOM_TABBED) v *= apod;
+            }
+        }
+        if (!__any_sync(kFull, hit)) continue;
+        // group the warp's taps by knot; the lowest lane of a group sums the
+        // group's weights in lane order
+        const unsigned grp = __match_any_sync(kFull, hit ? j : -1);
+        const int n = __popc(grp);
+        const int nmax = (int)__reduce_max_sync(kFull, hit ? (unsigned)n : 0u);
+        const float wa = v * am, wb = v * b;
+        const float wc = v * fmaf(am * am, am, -am), wd = v * fmaf(b * b, b, -b);
+        float A = wa, B = wb, C = wc, D = wd;
+        unsigned rest = grp & (grp - 1u);
+        for (int k = 1; k < nmax; ++k) {
+            const int src = rest ? __ffs(rest) - 1 : lane;
+            rest &= rest - 1u;
+            const float xa = __shfl_sync(kFull, wa, src), xb = __shfl_sync(kFull, wb, src);
+            const float xc = __shfl_sync(kFull, wc, src), xd = __shfl_sync(kFull, wd, src);
+            if (k < n) {
+                A += xa;
+                B += xb;
+                C += xc;
+                D += xd;
+            }
+        }
+        const bool leader = hit && (lane == __ffs(grp) - 1);
+        if (leader) {
+            ry[j] += A;
+            rz[j] += C;
+        }
+        __syncwarp();
+        if (leader) {
+            ry[j + 1] += B;
+            rz[j + 1] += D;
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    float *dst = g.partial + ((size_t)q * nch + c) * 2 * Lp;
+    for (int m = threadIdx.x; m < 2 * Lp; m += blockDim.x) {
+        float s = rows[m];
+        for (int k = 1; k < nw; ++k) s += rows[(size_t)k * 2 * Lp + m];
+        dst[m] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// adjoint of the prefilter, one warp per channel
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+adj_finalize_kernel(const float *__restrict__ partial, int nparts, long long nch, int nt, int Lp,
+                    float *__restrict__ grad_rf, const __grid_constant__ SplineTable tab) {
+    extern __shared__ float smem[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const long long ch = (long long)blockIdx.x * wpb + w;
+    if (ch >= nch) return;
+    const int stride = (nt + 4) & ~3;
+    float *gy = smem + (size_t)w * 4 * stride;
+    float *gz = gy + stride;
+    float *u = gz + stride;
+    float *v = u + stride;
+    for (int n = lane; n < nt; n += 32) {
+        float sy = 0.f, sz = 0.f;
+        for (int q = 0; q < nparts; ++q) {
+            const float *p = partial + ((size_t)q * nch + ch) * 2 * Lp;
+            sy += p[n];
+            sz += p[Lp + n];
+        }
+        gy[n] = sy;
+        gz[n] = sz;
+    }
+    if (lane == 0) {
+        u[0] = 0.f;
+        v[0] = 0.f;
+        v[nt - 1] = 0.f;
+    }
+    __syncwarp();
+    // T v = dL/dz on the interior samples 1..nt-2 (v_0 = v_nt-1 = 0)
+    const int C = ((nt + 31) >> 5) | 1;
+    const int s = lane * C;
+    const int e = min(s + C, nt);
+    {
+        const int ib = max(s, 1), ie = min(e, nt - 1);
+        if (ib < ie) {
+            float up = 0.f;
+            for (int k = max(1, ib - kWarmAdj); k < ie; ++k) {
+                const float uk = fmaf(-0.5f, up, gz[k]) * tab.invp[min(k, kSplineTab - 1)];
+                if (k >= ib) u[k] = uk;
+                up = uk;
+            }
+        }
+    }
+    __syncwarp();
+    {
+        const int kb = max(s, 1), ke = min(e, nt - 1);
+        if (kb < ke) {
+            float vn = 0.f;
+            for (int k = min(nt - 2, ke - 1 + kWarmAdj); k >= kb; --k) {
+                const float vk = fmaf(tab.c[min(k, kSplineTab - 1)], vn, u[k]);
+                if (k < ke) v[k] = vk;
+                vn = vk;
+            }
+        }
+    }
+    __syncwarp();
+    float *dst = grad_rf + ch * (long long)nt;
+    for (int n = lane; n < nt; n += 32) {
+        const float vm = n >= 1 ? v[n - 1] : 0.f;
+        const float vp = n + 1 < nt ? v[n + 1] : 0.f;
+        dst[n] = fmaf(0.5f, vm - 2.f * v[n] + vp, gy[n]);
+    }
+}
+
+size_t delay_smem_bytes(int ntx) { return 3 * (size_t)ntx * kBlock * sizeof(float); }
+
+template <int GEOM, int SUM, typename T>
+cudaError_t launch_delay_one(const AdjArgs &g, cudaStream_t s) {
+    auto kern = adj_delay_kernel<GEOM, SUM, T>;
+    const size_t smem = delay_smem_bytes(g.d.ntx);
+    if (smem > 48 * 1024) {
+        cudaError_t err =
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return err;
+    }
+    const long long bx = (g.d.np + kBlock - 1) / kBlock;
+    kern<<<(unsigned)bx, kBlock, smem, s>>>(g);
+    return cudaGetLastError();
+}
+
+template <int GEOM, int SUM>
+cudaError_t launch_scatter_one(const AdjArgs &g, cudaStream_t s) {
+    const DasArgs &a = g.d;
+    const long long nch = (long long)a.nframes * a.ntx * a.nrx;
+    const int nparts = adjoint_parts(nch, a.np);
+    const int nw = adjoint_rows_warps(a.nt);
+    if (nw == 0) return cudaErrorInvalidValue;
+    const int Lp = (a.nt + 1 + 3) & ~3;
+    const long long per = (a.np + nparts - 1) / nparts;
+    const long long part_len = (per + 127) / 128 * 128;
+    const size_t smem = (size_t)nw * 2 * Lp * sizeof(float);
+    auto kern = adj_scatter_kernel<GEOM, SUM>;
+    cudaError_t err =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    kern<<<dim3((unsigned)nch, (unsigned)nparts), 32 * nw, smem, s>>>(g, part_len, Lp);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+
+    static SplineTable tab = [] {
+        SplineTable t;
+        make_spline_table(&t);
+        return t;
+    }();
+    const size_t per_warp = sizeof(float) * 4 * (size_t)((a.nt + 4) & ~3);
+    const int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (96 * 1024) / per_warp));
+    const size_t fsmem = per_warp * wpb;
+    err = cudaFuncSetAttribute(adj_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)fsmem);
+    if (err != cudaSuccess) return err;
+    const long long blocks = (nch + wpb - 1) / wpb;
+    adj_finalize_kernel<<<(unsigned)blocks, 32 * wpb, fsmem, s>>>(g.partial, nparts, nch, a.nt, Lp,
+                                                                  g.grad_rf, tab);
+    return cudaGetLastError();
+}
+
+template <int GEOM, int SUM, typename T>
+cudaError_t launch_adjoint_gs(const AdjArgs &g, cudaStream_t s) {
+    if (g.grad_tautx || g.grad_taurx || g.grad_slow) {
+        cudaError_t err = launch_delay_one<GEOM, SUM, T>(g, s);
+        if (err != cudaSuccess) return err;
+    }
+    if (g.grad_rf) return launch_scatter_one<GEOM, SUM>(g, s);
+    return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t launch_adjoint_t(const AdjArgs &g, cudaStream_t s) {
+    const bool both = g.sumtype == PYCBF_GB_SUM_TX_AND_RX;
+    if (g.geom == GEOM_TABBED)
+        return both ? launch_adjoint_gs<GEOM_TABBED, PYCBF_GB_SUM_TX_AND_RX, T>(g, s)
+                    : launch_adjoint_gs<GEOM_TABBED, PYCBF_GB_SUM_TX_ONLY, T>(g, s);
+    return both ? launch_adjoint_gs<GEOM_SYNTH_SLOW, PYCBF_GB_SUM_TX_AND_RX, T>(g, s)
+                : launch_adjoint_gs<GEOM_SYNTH_SLOW, PYCBF_GB_SUM_TX_ONLY, T>(g, s);
+}
+
+}  // namespace
+
+int adjoint_parts(long long nch, long long np) {
+    // enough (channel, part) CTAs to fill the GPU several times over, parts of >= 2048 pixels
+    long long p = (2048 + nch - 1) / nch;
+    p = std::min<long long>(p, std::max<long long>(1, np / 2048));
+    return (int)std::max<long long>(1, std::min<long long>(p, 64));
+}
+
+int adjoint_rows_warps(int nt) {
+    const size_t row = 2 * (size_t)((nt + 1 + 3) & ~3) * sizeof(float);
+    for (int nw = 4; nw >= 1; nw >>= 1)
+        if (nw * row <= kRowSmemMax) return nw;
+    return 0;
+}
+
+size_t adjoint_workspace_bytes(long long nch, long long np, int nt) {
+    const size_t Lp = (size_t)((nt + 1 + 3) & ~3);
+    return (size_t)adjoint_parts(nch, np) * (size_t)nch * 2 * Lp * sizeof(float);
+}
+
+cudaError_t launch_adjoint(const AdjArgs &g, int dtype, cudaStream_t s) {
+    switch (dtype) {
+        case PYCBF_GB_F32: return launch_adjoint_t<float>(g, s);
+        case PYCBF_GB_F16: return launch_adjoint_t<__half>(g, s);
+        case PYCBF_GB_BF16: return launch_adjoint_t<__nv_bfloat16>(g, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_das_synth_slow(const DasArgs &a, int sumtype, int dtype, cudaStream_t s) {
+    constexpr int CU = PYCBF_GB_INTERP_CUBIC;
+    const bool both = sumtype == PYCBF_GB_SUM_TX_AND_RX;
+    switch (dtype) {
+        case PYCBF_GB_F32:
+            return both ? launch_das_one<GEOM_SYNTH_SLOW, CU, PYCBF_GB_SUM_TX_AND_RX, float, false>(a, s)
+                        : launch_das_one<GEOM_SYNTH_SLOW, CU, PYCBF_GB_SUM_TX_ONLY, float, false>(a, s);
+        case PYCBF_GB_F16:
+            return both ? launch_das_one<GEOM_SYNTH_SLOW, CU, PYCBF_GB_SUM_TX_AND_RX, __half, false>(a, s)
+                        : launch_das_one<GEOM_SYNTH_SLOW, CU, PYCBF_GB_SUM_TX_ONLY, __half, false>(a, s);
+        case PYCBF_GB_BF16:
+            return both ? launch_das_one<GEOM_SYNTH_SLOW, CU, PYCBF_GB_SUM_TX_AND_RX, __nv_bfloat16, false>(a, s)
+                        : launch_das_one<GEOM_SYNTH_SLOW, CU, PYCBF_GB_SUM_TX_ONLY, __nv_bfloat16, false>(a, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace pgb

@@ -98,7 +98,9 @@ cudaError_t launch_spline(const SplineArgs &a, int dtype, cudaStream_t s);
 // ---------------------------------------------------------------------------
 // delay-and-sum
 // ---------------------------------------------------------------------------
-enum Geom { GEOM_TABBED = 0, GEOM_SYNTH = 1 };
+// GEOM_SYNTH_SLOW: synthetic geometry whose delays are path length x a
+// per-pixel slowness (the differentiable form) instead of path length / c0
+enum Geom { GEOM_TABBED = 0, GEOM_SYNTH = 1, GEOM_SYNTH_SLOW = 2 };
 
 struct DasArgs {
     // channel data (or spline coefficients for cubic), (nframes, ntx, nrx, nt)
@@ -114,6 +116,7 @@ struct DasArgs {
     long long np;
     int ntx, nrx, nt, ndim, nframes;
     float t0, dt, inv_dt, xmax, xend, thresh, eps;
+    const float *slow;  // GEOM_SYNTH_SLOW: slowness per pixel (s/m), kernel pixel order
 };
 cudaError_t launch_das(const DasArgs &a, int geom, int interp, int sumtype, int dtype, bool census,
                        cudaStream_t s);
@@ -123,6 +126,28 @@ long long tabbed_plan_words(long long np, int ntx, int nrx);
 cudaError_t launch_tabbed_plan(const DasArgs &a, int interp, int dtype, int *plan, cudaStream_t s);
 cudaError_t launch_das_staged(const DasArgs &a, int interp, int sumtype, int dtype, const int *plan,
                               int *status, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// adjoint (gradients of the cubic delay-and-sum; no reference counterpart)
+// ---------------------------------------------------------------------------
+struct AdjArgs {
+    DasArgs d;            // the forward's arguments (d.data = coefficient records)
+    int geom;             // GEOM_TABBED or GEOM_SYNTH_SLOW
+    int sumtype;          // PYCBF_GB_SUM_TX_AND_RX or PYCBF_GB_SUM_TX_ONLY
+    const float *gout;    // upstream gradient, shaped like the forward's output
+    float *grad_rf;       // (nframes, ntx, nrx, nt) float32, or NULL
+    float *grad_tautx;    // Tabbed (ntx, np), or NULL
+    float *grad_taurx;    // Tabbed (nrx, np), or NULL
+    float *grad_slow;     // Synthetic (np), or NULL
+    float *partial;       // workspace: per-part sums of the spline-record adjoints
+};
+// parts of the pixel range whose channel adjoints are summed separately, and
+// the workspace they need
+int adjoint_parts(long long nch, long long np);
+size_t adjoint_workspace_bytes(long long nch, long long np, int nt);
+int adjoint_rows_warps(int nt);  // warps (private accumulation rows) per scatter CTA, 0 = nt too large
+cudaError_t launch_adjoint(const AdjArgs &a, int dtype, cudaStream_t s);
+cudaError_t launch_das_synth_slow(const DasArgs &a, int sumtype, int dtype, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // coherence

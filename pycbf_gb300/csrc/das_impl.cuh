@@ -206,6 +206,45 @@ __device__ __forceinline__ float synth_tx_delay(const DasArgs &a, int t, const f
     return __fdiv_rn(proj, c0);
 }
 
+// The same geometry as path lengths for the slowness form: a transmit delay
+// is D*s + t0add, a receive delay D*s; false where the element masks the point.
+__device__ __forceinline__ bool synth_tx_path(const DasArgs &a, int t, const float *p, float &D,
+                                              float &t0add) {
+    const int nd = a.ndim;
+    float mag, proj;
+    synth_dist(a.geo.ovectx + t * nd, a.geo.nvectx + t * nd, p, nd, mag, proj);
+    const float ala = __ldg(a.geo.alatx + t);
+    t0add = 0.f;
+    D = proj;
+    if (ala == 0.f) return true;
+    t0add = __ldg(a.geo.t0tx + t);
+    const float sgn = (proj > 0.f) ? 1.f : -1.f;
+    const float cosala = __ldg(a.geo.cosalatx + t);
+    if (__ldg(a.geo.doftx + t) != 0.f) {
+        if ((fabsf(proj) > kDxMin) && (mag > kDxMin) && (fabsf(__fdiv_rn(proj, mag)) >= cosala)) {
+            D = sgn * mag;
+            return true;
+        }
+        const float lat = __fsqrt_rn(fabsf(__fsub_rn(__fmul_rn(mag, mag), __fmul_rn(proj, proj))));
+        D = __fmul_rn(proj, __ldg(a.geo.secalatx + t));
+        return lat < __ldg(a.geo.halfdofsintx + t);
+    }
+    D = (fabsf(proj) > kDxMin) ? sgn * mag : 0.f;
+    return !((mag > kDxMin) && (fabsf(__fdiv_rn(proj, mag)) < cosala));
+}
+
+__device__ __forceinline__ bool synth_rx_path(const DasArgs &a, int r, const float *p, float &D) {
+    const int nd = a.ndim;
+    float mag, proj;
+    synth_dist(a.geo.ovecrx + r * nd, a.geo.nvecrx + r * nd, p, nd, mag, proj);
+    D = mag;
+    return !((mag > kDxMin) && (__fdiv_rn(proj, mag) < __ldg(a.geo.cosalarx + r)));
+}
+
+__device__ __forceinline__ float slow_delay(bool ok, float D, float s, float t0add) {
+    return ok ? __fadd_rn(__fmul_rn(D, s), t0add) : __int_as_float(0x7f800000);
+}
+
 __device__ __forceinline__ float synth_rx_delay(const DasArgs &a, int r, const float *p) {
     const int nd = a.ndim;
     float mag, proj;
@@ -235,8 +274,9 @@ __global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ 
     const long long chs = (long long)nrx * a.nt;  // channel stride between transmits
 
     float pnt[3] = {0.f, 0.f, 0.f};
-    if (GEOM == GEOM_SYNTH)
+    if (GEOM != GEOM_TABBED)
         for (int k = 0; k < a.ndim; ++k) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
+    const float slow = (GEOM == GEOM_SYNTH_SLOW) ? __ldg(a.slow + i) : 0.f;
 
     // transmit side: registers (ntx <= kTxReg) or this thread's column of shared memory.
     // Synthetic masks travel as +inf delays, which the range test rejects.
@@ -250,8 +290,13 @@ __global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ 
             tau = __ldg(a.tautx + (long long)t * np + i);
             apod = __ldg(a.apodtx + (long long)t * np + i);
             amax = fmaxf(amax, fabsf(apod));
-        } else {
+        } else if (GEOM == GEOM_SYNTH) {
             tau = synth_tx_delay(a, t, pnt);
+            apod = 1.f;
+        } else {
+            float D, t0add;
+            const bool ok = synth_tx_path(a, t, pnt, D, t0add);
+            tau = slow_delay(ok, D, slow, t0add);
             apod = 1.f;
         }
     };
@@ -284,8 +329,13 @@ __global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ 
         if (GEOM == GEOM_TABBED) {
             trx = __ldg(a.taurx + (long long)r * np + i);
             arx = __ldg(a.apodrx + (long long)r * np + i);
-        } else {
+        } else if (GEOM == GEOM_SYNTH) {
             trx = synth_rx_delay(a, r, pnt);
+            arx = 1.f;
+        } else {
+            float D;
+            const bool ok = synth_rx_path(a, r, pnt, D);
+            trx = slow_delay(ok, D, slow, 0.f);
             arx = 1.f;
         }
     };

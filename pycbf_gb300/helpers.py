@@ -78,3 +78,21 @@ def pw_synthetic_points(steers, ctx, cm, xele, fnum, rpw: float = -10.0):
     alarx = np.arctan2(0.5, fnum) * np.ones(nrx)
     return dict(ovectx=ovectx, nvectx=nvectx, t0tx=t0tx, doftx=doftx, alatx=alatx,
                 ovecrx=ovecrx, nvecrx=nvecrx, alarx=alarx)
+
+
+def pw_synthetic_planewaves(steers, xele, fnum):
+    """True plane waves in the synthetic-point form: alatx = 0, so a transmit
+    delay is (p - o) . n / c with o the array edge the wave leaves first (the
+    geometry of pw_tx_tables), and receive elements with the F-number mask
+    (pycbf/gpu/__engines__.cu:382-470: the ala == 0 branch of
+    calc_tautx_apodtx has no mask and no t0)."""
+    steers = np.asarray(steers, np.float64)
+    orig = np.stack([np.where(steers <= 0, xele[-1], xele[0]), np.zeros_like(steers)], axis=1)
+    nvectx = np.stack([np.sin(steers), np.cos(steers)], axis=1)
+    z = np.zeros(len(steers))
+    nrx = len(xele)
+    ovecrx = np.stack([xele, np.zeros(nrx)], axis=1)
+    nvecrx = np.stack([np.zeros(nrx), np.ones(nrx)], axis=1)
+    alarx = np.arctan2(0.5, fnum) * np.ones(nrx)
+    return dict(ovectx=orig, nvectx=nvectx, t0tx=z, doftx=z.copy(), alatx=z.copy(),
+                ovecrx=ovecrx, nvecrx=nvecrx, alarx=alarx)

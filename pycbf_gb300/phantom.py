@@ -177,3 +177,49 @@ def linear_pw_synthetic(nele=192, pitch=0.2e-3, nsteer=75, max_deg=18.0, fs=31.2
     return SyntheticWorkload(name, rf.cpu().numpy(), geo, t0, dt, nt, (nx, nz),
                              dict(nele=nele, pitch=pitch, nsteer=nsteer, fs=fs, fc=fc, c=c,
                                   fnum=fnum, seed=seed, xout=xout, zout=zout))
+
+
+def layered_slowness(z, c_top=1450.0, c_bottom=1560.0, z_interface=15e-3):
+    """Mean slowness (s/m) along a straight path from depth 0 to depth z through
+    a layer of speed c_top above z_interface and c_bottom below it."""
+    z = np.maximum(np.asarray(z, np.float64), 1e-9)
+    return (np.minimum(z, z_interface) / c_top + np.maximum(z - z_interface, 0.0) / c_bottom) / z
+
+
+def two_layer_pw_synthetic(nele=128, pitch=0.3e-3, nsteer=11, max_deg=10.0, fs=25e6, fc=5e6,
+                           bw=0.6, nt=2048, nx=256, nz=512, xlim=(-19e-3, 19e-3),
+                           zlim=(5e-3, 45e-3), n_speckle=5000, n_points=20, fnum=1.5,
+                           noise_db=-40.0, c_top=1450.0, c_bottom=1560.0, z_interface=15e-3,
+                           c_nominal=1540.0, seed=2468, device=None,
+                           name="two_layer") -> SyntheticWorkload:
+    """Plane-wave synthetic workload in a two-layer medium (defaults: the
+    128-element, 11-angle geometry; 1450 m/s to 15 mm, 1560 m/s below).
+
+    Every echo delay is its straight path length times the mean slowness of
+    the layers down to the scatterer's depth (layered_slowness), the model the
+    slowness form of the delay-and-sum inverts.  meta['slowness_true'] holds
+    that slowness at every pixel; geometry['c0'] is the nominal speed.
+    """
+    dev = _device(device)
+    xele = helpers.element_positions(nele, pitch)
+    steers = np.radians(np.linspace(-max_deg, max_deg, nsteer))
+    xout = np.linspace(xlim[0], xlim[1], nx)
+    zout = np.linspace(zlim[0], zlim[1], nz)
+    geo = helpers.pw_synthetic_planewaves(steers, xele, fnum)
+    pnts = helpers.pixel_grid(xout, zout)
+    pos, amp = scatterers(seed, n_speckle, n_points, xlim, zlim)
+    s_true = layered_slowness(pos[:, 1], c_top, c_bottom, z_interface)
+    proj = np.sum((pos[None, :, :] - geo["ovectx"][:, None, :]) * geo["nvectx"][:, None, :], -1)
+    tt = proj * s_true[None, :]
+    tr = np.linalg.norm(pos[None, :, :] - geo["ovecrx"][:, None, :], axis=-1) * s_true[None, :]
+    t0, dt = 0.0, 1.0 / fs
+    rf = simulate_channels(torch.tensor(tt, device=dev), torch.tensor(tr, device=dev),
+                           torch.tensor(amp, device=dev), t0, dt, nt, fc, bw, noise_db, seed)
+    geo = dict(geo)
+    geo["c0"] = c_nominal
+    geo["pnts"] = pnts
+    return SyntheticWorkload(name, rf.cpu().numpy(), geo, t0, dt, nt, (nx, nz),
+                             dict(nele=nele, pitch=pitch, nsteer=nsteer, fs=fs, fc=fc, c=c_nominal,
+                                  fnum=fnum, seed=seed, xout=xout, zout=zout,
+                                  slowness_true=layered_slowness(pnts[:, 1], c_top, c_bottom,
+                                                                 z_interface)))

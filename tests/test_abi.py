@@ -120,3 +120,39 @@ def test_synthetic_and_coherence_validation():
     assert L.pycbf_gb_slsc(p, p, 1, 8, 4, 4, 40, 2, p, None) == _lib.ERANGE
     assert L.pycbf_gb_slsc(p, p, 1, 8, 4, 4, 4, 40, p, None) == _lib.ERANGE
     assert L.pycbf_gb_slsc(p, None, 1, 8, 4, 4, 4, 2, p, None) == _lib.EINVAL
+
+
+def test_adjoint_workspace_bytes():
+    L = _lib.load()
+    info = _info(ntx=2, nrx=3, nt=16, nframes=2)
+    nch = 2 * 2 * 3
+    # parts: enough (channel, part) blocks to fill the GPU, >= 2048 pixels per part
+    n = L.pycbf_gb_adjoint_workspace_bytes(ct.byref(info), 100000)
+    lp = (16 + 1 + 3) & ~3
+    assert n % (nch * 2 * lp * 4) == 0 and n // (nch * 2 * lp * 4) == min(48, (2048 + nch - 1) // nch)
+    assert L.pycbf_gb_adjoint_workspace_bytes(ct.byref(info), 100) == nch * 2 * lp * 4
+    assert L.pycbf_gb_adjoint_workspace_bytes(ct.byref(info), 0) == 0
+
+
+def test_adjoint_entry_points_validate_first():
+    L = _lib.load()
+    p = ct.c_void_p(16)
+    info = _info()
+    tab = lambda **kw: L.pycbf_gb_das_tabbed_adjoint(
+        ct.byref(kw.get("info", info)), kw.get("coef", p), p, p, p, p, 10, None, 0.01,
+        kw.get("sum", 3), kw.get("gout", p), kw.get("grf", None), p, p, kw.get("ws", None),
+        kw.get("wsb", 0), None)
+    assert tab(sum=0) == _lib.EUNSUPPORTED
+    assert tab(sum=5) == _lib.EUNSUPPORTED
+    assert tab(gout=None) == _lib.EINVAL
+    assert tab(coef=ct.c_void_p(8)) == _lib.EINVAL          # coefficients 16-byte aligned
+    assert tab(info=_info(ntx=129)) == _lib.ERANGE
+    assert tab(info=_info(nt=20000)) == _lib.ERANGE
+    assert tab(grf=p) == _lib.EWORKSPACE                    # grad_rf needs the workspace
+    assert tab(grf=p, ws=p, wsb=1) == _lib.EWORKSPACE
+    geo = _lib.SyntheticGeom()
+    sinfo = _info(ndim=2)
+    assert L.pycbf_gb_das_synthetic_adjoint(ct.byref(sinfo), p, ct.byref(geo), p, None, 3, p,
+                                            None, p, None, 0, None) == _lib.EINVAL
+    assert L.pycbf_gb_das_synthetic_slowness(ct.byref(_info(ndim=4)), p, ct.byref(geo), p, None,
+                                             3, p, None) == _lib.EINVAL
