@@ -378,6 +378,111 @@ def run_variants(a, w, dev, taps):
         res[name] = {"value": taps * nf / statistics.mean(times), "unit": UNIT,
                      "ms_per_call": 1e3 * statistics.mean(times), "frames_per_call": nf,
                      "storage": storage, "interp": kind}
+    res.update(run_adjoint_variants(a, w, dev, taps))
+    return res
+
+
+def _event_time(fn, reps, flush, stream):
+    import torch
+    times = []
+    for _ in range(reps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    return statistics.mean(times)
+
+
+def run_adjoint_variants(a, w, dev, taps):
+    """Forward + adjoint against the plain forward.
+
+    fwd_adj_tabbed: the workload above through the differentiable path,
+    gradients with respect to the channel data and both delay tables.
+    fwd_adj_sos: the same array and grid as Synthetic beamforming in a
+    two-layer medium (1450 m/s to 15 mm, 1560 m/s below), per-element images
+    with a slowness per pixel, gradients with respect to the channel data and
+    the slowness; plus one optimisation step of a global c + 32 x 64 slowness
+    map on the lag-1 coherence + sharpness loss.
+    """
+    import torch
+
+    import pycbf_gb300 as pg
+    from pycbf_gb300 import phantom, sos
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    reps = max(3, a.steps // 2)
+    res = {}
+
+    bf = pg.TabbedBeamformer(tautx=w.tautx, taurx=w.taurx, apodtx=w.apodtx, apodrx=w.apodrx,
+                             t0=w.t0, dt=w.dt, nt=w.nt, interp={"kind": "cubic"})
+    rf = torch.as_tensor(w.rf, device=dev)
+    tautx = torch.as_tensor(w.tautx, device=dev)
+    taurx = torch.as_tensor(w.taurx, device=dev)
+    gout = torch.randn((bf.nop,), device=dev)
+
+    def fwd_tab():
+        with torch.no_grad():
+            bf.differentiable(rf)
+
+    def fwd_adj_tab():
+        r = rf.detach().requires_grad_(True)
+        t1, t2 = tautx.detach().requires_grad_(True), taurx.detach().requires_grad_(True)
+        bf.differentiable(r, tautx=t1, taurx=t2).backward(gout)
+
+    for _ in range(2):
+        fwd_tab(), fwd_adj_tab()
+    t_f = _event_time(fwd_tab, reps, flush, stream)
+    t_fa = _event_time(fwd_adj_tab, reps, flush, stream)
+    res["fwd_adj_tabbed"] = {"value": taps / t_fa, "unit": UNIT, "ms_per_call": 1e3 * t_fa,
+                             "forward_ms": 1e3 * t_f, "forward_value": taps / t_f,
+                             "grads": ["rf", "tautx", "taurx"], "interp": "cubic",
+                             "sumtype": "tx_and_rx"}
+
+    sw = phantom.two_layer_pw_synthetic(device=dev)
+    g = sw.geometry
+    sbf = pg.SyntheticBeamformer(ovectx=g["ovectx"], nvectx=g["nvectx"], doftx=g["doftx"],
+                                 alatx=g["alatx"], t0tx=g["t0tx"], ovecrx=g["ovecrx"],
+                                 nvecrx=g["nvecrx"], alarx=g["alarx"], c0=g["c0"],
+                                 pnts=g["pnts"], t0=sw.t0, dt=sw.dt, nt=sw.nt,
+                                 interp={"kind": "cubic"}, sumtype="tx_only")
+    srf = torch.as_tensor(sw.rf, device=dev)
+    staps = sbf.ntx * sbf.nrx * sbf.nop
+    model = sos.SlownessModel(sw.grid, map_shape=(32, 64), c_init=1540.0, device=dev)
+    mask = sbf.rx_mask()
+    s_fixed = model().detach()
+    gimg = torch.randn((sbf.nrx, sbf.nop), device=dev)
+
+    def fwd_s():
+        with torch.no_grad():
+            sbf.differentiable(srf, slowness=s_fixed)
+
+    def fwd_adj_s():
+        r = srf.detach().requires_grad_(True)
+        s = s_fixed.detach().requires_grad_(True)
+        sbf.differentiable(r, slowness=s).backward(gimg)
+
+    opt = torch.optim.Adam(model.parameters(), lr=1e-6)
+
+    def train_step():
+        opt.zero_grad(set_to_none=True)
+        loss = sos.sos_loss(sbf.differentiable(srf, slowness=model()), mask, sw.grid, nkern=2)
+        loss.backward()
+        opt.step()
+
+    for _ in range(2):
+        fwd_s(), fwd_adj_s(), train_step()
+    t_f = _event_time(fwd_s, reps, flush, stream)
+    t_fa = _event_time(fwd_adj_s, reps, flush, stream)
+    t_tr = _event_time(train_step, reps, flush, stream)
+    res["fwd_adj_sos"] = {"value": staps / t_fa, "unit": UNIT, "ms_per_call": 1e3 * t_fa,
+                          "forward_ms": 1e3 * t_f, "forward_value": staps / t_f,
+                          "train_step_ms": 1e3 * t_tr, "grads": ["rf", "slowness"],
+                          "workload": "synthetic two-layer 128el 11pw 2048s 256x512, per-element "
+                                      "images, 32x64 slowness map + global c",
+                          "interp": "cubic", "sumtype": "tx_only"}
     return res
 
 

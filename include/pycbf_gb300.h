@@ -266,13 +266,14 @@ int pycbf_gb_das_tabbed_cubic_noalloc(const pycbf_gb_rfinfo *rf, const void *rfd
 /* The adjoints take the upstream gradient grad_out (shaped like the       */
 /* image, indexed through pixel_index like it) and write, each only when   */
 /* its pointer is not NULL:                                                */
-/*   grad_rf     (nframes, ntx, nrx, nt) float32 whatever the storage;     */
-/*               needs pycbf_gb_adjoint_workspace_bytes of workspace       */
+/*   grad_rf     (nframes, ntx, nrx, nt) float32 whatever the storage      */
 /*   grad_tautx  (ntx, np), grad_taurx (nrx, np): Tabbed, summed over      */
 /*               frames, table-column order                                */
 /*   grad_slow   (np): Synthetic, summed over frames                       */
 /* All outputs are overwritten; every sum has a fixed order, so results    */
 /* are bitwise reproducible.  Apodization is not differentiated.           */
+/* workspace: pycbf_gb_adjoint_workspace_bytes bytes, 16-byte aligned;     */
+/* it may be NULL only when grad_rf and pixel_index are both NULL.         */
 /* ---------------------------------------------------------------------- */
 int pycbf_gb_das_synthetic_slowness(const pycbf_gb_rfinfo *rf, const void *coef,
                                     const pycbf_gb_synthetic *geo, const float *slowness,

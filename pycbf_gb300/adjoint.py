@@ -122,7 +122,7 @@ class _TabbedDAS(torch.autograd.Function):
         g_ttx = torch.empty_like(tautx) if need_ttx else None
         g_trx = torch.empty_like(taurx) if need_trx else None
         ws, nws = None, 0
-        if need_rf:
+        if need_rf or ctx.pixel_index is not None:
             nws = L.pycbf_gb_adjoint_workspace_bytes(ct.byref(info), np_)
             ws = torch.empty(nws, dtype=torch.uint8, device=dev)
         if need_rf or need_ttx or need_trx:
@@ -171,7 +171,7 @@ class _SyntheticDAS(torch.autograd.Function):
         g_rf = torch.empty(shape, dtype=torch.float32, device=dev) if need_rf else None
         g_s = torch.empty_like(slowness) if need_s else None
         ws, nws = None, 0
-        if need_rf:
+        if need_rf or ctx.pixel_index is not None:
             nws = L.pycbf_gb_adjoint_workspace_bytes(ct.byref(info), slowness.shape[0])
             ws = torch.empty(nws, dtype=torch.uint8, device=dev)
         if need_rf or need_s:

@@ -379,11 +379,13 @@ int check_adjoint_common(const pycbf_gb_rfinfo *rf, const void *coef, int sumtyp
 
 int run_adjoint(const pycbf_gb_rfinfo *rf, AdjArgs &g, void *workspace, size_t workspace_bytes,
                 cudaStream_t s) {
-    if (g.grad_rf) {
+    if (g.grad_rf || g.d.pixel_index) {
         const size_t need = pycbf_gb_adjoint_workspace_bytes(rf, g.d.np);
         if (!workspace || workspace_bytes < need || reinterpret_cast<uintptr_t>(workspace) % 16)
             return PYCBF_GB_EWORKSPACE;
-        g.partial = static_cast<float *>(workspace);
+        g.gk_buf = static_cast<float *>(workspace);
+        g.partial = reinterpret_cast<float *>(static_cast<char *>(workspace) +
+                                              adjoint_grad_bytes(rf->nframes, rf->nrx, g.d.np));
     }
     return cuda_status(launch_adjoint(g, rf->dtype, s));
 }
@@ -414,7 +416,7 @@ int pycbf_gb_das_synthetic_slowness(const pycbf_gb_rfinfo *rf, const void *coef,
 
 size_t pycbf_gb_adjoint_workspace_bytes(const pycbf_gb_rfinfo *rf, long long np) {
     if (!rf || np <= 0 || rf->ntx <= 0 || rf->nrx <= 0 || rf->nt <= 0 || rf->nframes <= 0) return 0;
-    return adjoint_workspace_bytes(rf->nframes * rf->ntx * rf->nrx, np, rf->nt);
+    return adjoint_workspace_bytes(rf->nframes, rf->ntx, rf->nrx, np, rf->nt);
 }
 
 int pycbf_gb_das_tabbed_adjoint(const pycbf_gb_rfinfo *rf, const void *coef,

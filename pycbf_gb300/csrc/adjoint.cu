@@ -58,10 +58,18 @@ __device__ __forceinline__ float cubic_slope(const float4 &c, float am, float b,
     return (c.y - c.x + fmaf(db, c.w, -da * c.z)) * inv_dt;
 }
 
-__device__ __forceinline__ float upstream(const AdjArgs &g, int sum, int f, int r, long long op) {
-    const DasArgs &a = g.d;
-    return sum == PYCBF_GB_SUM_TX_AND_RX ? __ldg(g.gout + (long long)f * a.np + op)
-                                         : __ldg(g.gout + ((long long)f * a.nrx + r) * a.np + op);
+// the upstream gradient of (frame f, receive r) at kernel-order pixel i (g.gk
+// holds it in kernel order: gathered through pixel_index when there is one)
+__device__ __forceinline__ long long grad_row(int sum, int f, int r, int nrx) {
+    return sum == PYCBF_GB_SUM_TX_AND_RX ? (long long)f : (long long)f * nrx + r;
+}
+
+__global__ void adj_gather_kernel(const float *__restrict__ gout, const int *__restrict__ pidx,
+                                  long long rows, long long np, float *__restrict__ gk) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= rows * np) return;
+    const long long row = n / np, i = n - row * np;
+    gk[n] = __ldg(gout + row * np + __ldg(pidx + i));
 }
 
 // ---------------------------------------------------------------------------
@@ -70,6 +78,7 @@ __device__ __forceinline__ float upstream(const AdjArgs &g, int sum, int f, int 
 template <int GEOM, int SUM, typename T>
 __global__ void __launch_bounds__(kBlock) adj_delay_kernel(const __grid_constant__ AdjArgs g) {
     using rec = typename CoefRec<T>::raw;
+    constexpr int G = 6;  // taps whose record loads are in flight together
     const DasArgs &a = g.d;
     extern __shared__ float sm[];
     const int tid = threadIdx.x;
@@ -77,7 +86,6 @@ __global__ void __launch_bounds__(kBlock) adj_delay_kernel(const __grid_constant
     if (i >= a.np) return;
     const long long np = a.np;
     const int ntx = a.ntx, nrx = a.nrx, nfr = a.nframes, nt = a.nt;
-    const long long op = a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i;
     const rec *coef = static_cast<const rec *>(a.data);
     // this thread's columns: transmit delay, apodization (Tabbed) or path
     // length (Synthetic), and the dL/dtau_tx accumulator
@@ -116,29 +124,53 @@ __global__ void __launch_bounds__(kBlock) adj_delay_kernel(const __grid_constant
             trx = slow_delay(true, Drx, slow, 0.f);
         }
         float grx = 0.f;
-        for (int t = 0; t < ntx; ++t) {
-            const float x = __fadd_rn(stau[(size_t)t * kBlock], trx);
-            float apod = 1.f;
-            if (GEOM == GEOM_TABBED) {
-                apod = __fmul_rn(sw[(size_t)t * kBlock], arx);
-                if (!(fabsf(apod) >= a.thresh)) continue;
+        for (int t0 = 0; t0 < ntx; t0 += G) {
+            bool hit[G];
+            int jj[G];
+            float am[G], bb[G], ap[G], sum[G];
+            bool any = false;
+#pragma unroll
+            for (int k = 0; k < G; ++k) {
+                const int t = t0 + k;
+                hit[k] = false;
+                jj[k] = 0;
+                am[k] = bb[k] = sum[k] = 0.f;
+                ap[k] = 1.f;
+                if (t < ntx) {
+                    const float x = __fadd_rn(stau[(size_t)t * kBlock], trx);
+                    bool ok = true;
+                    if (GEOM == GEOM_TABBED) {
+                        ap[k] = __fmul_rn(sw[(size_t)t * kBlock], arx);
+                        ok = fabsf(ap[k]) >= a.thresh;
+                    }
+                    hit[k] = ok && cubic_tap(x, a, jj[k], am[k], bb[k]);
+                    any |= hit[k];
+                }
             }
-            int j;
-            float am, b;
-            if (!cubic_tap(x, a, j, am, b)) continue;
-            float sum = 0.f;
+            if (!any) continue;
             for (int f = 0; f < nfr; ++f) {
-                const float gp = upstream(g, SUM, f, r, op);
-                const float4 c =
-                    CoefRec<T>::load(coef + (((long long)f * ntx + t) * nrx + r) * nt + j);
-                sum = fmaf(gp, cubic_slope(c, am, b, a.inv_dt), sum);
+                const float gp = __ldg(g.gk + grad_row(SUM, f, r, nrx) * np + i);
+                float4 c[G];
+#pragma unroll
+                for (int k = 0; k < G; ++k)
+                    if (hit[k])
+                        c[k] = CoefRec<T>::load(coef + (((long long)f * ntx + t0 + k) * nrx + r) * nt +
+                                                jj[k]);
+#pragma unroll
+                for (int k = 0; k < G; ++k)
+                    if (hit[k]) sum[k] = fmaf(gp, cubic_slope(c[k], am[k], bb[k], a.inv_dt), sum[k]);
             }
-            if (GEOM == GEOM_TABBED) {
-                const float d = apod * sum;
-                sg[(size_t)t * kBlock] += d;
-                grx += d;
-            } else {
-                gs = fmaf(sum, sw[(size_t)t * kBlock] + Drx, gs);  // dx/ds = D_tx + D_rx
+#pragma unroll
+            for (int k = 0; k < G; ++k) {
+                if (!hit[k]) continue;
+                const int t = t0 + k;
+                if (GEOM == GEOM_TABBED) {
+                    const float d = ap[k] * sum[k];
+                    sg[(size_t)t * kBlock] += d;
+                    grx += d;
+                } else {
+                    gs = fmaf(sum[k], sw[(size_t)t * kBlock] + Drx, gs);  // dx/ds = D_tx + D_rx
+                }
             }
         }
         if (GEOM == GEOM_TABBED && g.grad_taurx) g.grad_taurx[(long long)r * np + i] = grx;
@@ -172,8 +204,31 @@ __global__ void __launch_bounds__(128) adj_scatter_kernel(const __grid_constant_
 
     const long long i0 = (long long)q * part_len;
     const long long i1 = min(np, i0 + part_len);
+    const float *grow = g.gk + grad_row(SUM, f, r, nrx) * np;
+    // this pixel's inputs, fetched one step ahead: Tabbed apodtx, apodrx,
+    // tautx, taurx; Synthetic the point and its slowness; the upstream gradient
+    struct In {
+        float v[4];
+        float gp;
+    };
+    auto fetch = [&](long long i, In &in) {
+        if (i >= i1) return;
+        if (GEOM == GEOM_TABBED) {
+            in.v[0] = __ldg(a.apodtx + (long long)t * np + i);
+            in.v[1] = __ldg(a.apodrx + (long long)r * np + i);
+            in.v[2] = __ldg(a.tautx + (long long)t * np + i);
+            in.v[3] = __ldg(a.taurx + (long long)r * np + i);
+        } else {
+            for (int k = 0; k < a.ndim; ++k) in.v[k] = __ldg(a.geo.pnts + i * a.ndim + k);
+            in.v[3] = __ldg(a.slow + i);
+        }
+        in.gp = __ldg(grow + i);
+    };
+    In cur = {{0.f, 0.f, 0.f, 0.f}, 0.f}, nxt = cur;
+    fetch(i0 + threadIdx.x, cur);
     for (long long base = i0; base < i1; base += blockDim.x) {
         const long long i = base + threadIdx.x;
+        fetch(i + blockDim.x, nxt);
         bool hit = false;
         int j = 0;
         float am = 0.f, b = 0.f, v = 0.f;
@@ -181,29 +236,24 @@ __global__ void __launch_bounds__(128) adj_scatter_kernel(const __grid_constant_
             float x = 0.f, apod = 1.f;
             bool live;
             if (GEOM == GEOM_TABBED) {
-                apod = __fmul_rn(__ldg(a.apodtx + (long long)t * np + i),
-                                 __ldg(a.apodrx + (long long)r * np + i));
+                apod = __fmul_rn(cur.v[0], cur.v[1]);
                 live = fabsf(apod) >= a.thresh;
-                if (live)
-                    x = __fadd_rn(__ldg(a.tautx + (long long)t * np + i),
-                                  __ldg(a.taurx + (long long)r * np + i));
+                x = __fadd_rn(cur.v[2], cur.v[3]);
             } else {
-                float pnt[3] = {0.f, 0.f, 0.f};
-                for (int k = 0; k < a.ndim; ++k) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
-                const float slow = __ldg(a.slow + i);
+                const float pnt[3] = {cur.v[0], cur.v[1], cur.v[2]};
                 float Dt, t0add, Dr;
                 const bool okt = synth_tx_path(a, t, pnt, Dt, t0add);
                 const bool okr = synth_rx_path(a, r, pnt, Dr);
                 live = okt && okr;
-                if (live) x = __fadd_rn(slow_delay(true, Dt, slow, t0add), slow_delay(true, Dr, slow, 0.f));
+                x = __fadd_rn(slow_delay(true, Dt, cur.v[3], t0add),
+                              slow_delay(true, Dr, cur.v[3], 0.f));
             }
             if (live && cubic_tap(x, a, j, am, b)) {
                 hit = true;
-                const long long op = a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i;
-                v = upstream(g, SUM, f, r, op);
-                if (GEOM == GEOM_TABBED) v *= apod;
+                v = (GEOM == GEOM_TABBED) ? cur.gp * apod : cur.gp;
             }
         }
+        cur = nxt;
         if (!__any_sync(kFull, hit)) continue;
         // group the warp's taps by knot; the lowest lane of a group sums the
         // group's weights in lane order
@@ -258,25 +308,16 @@ adj_finalize_kernel(const float *__restrict__ partial, int nparts, long long nch
     const long long ch = (long long)blockIdx.x * wpb + w;
     if (ch >= nch) return;
     const int stride = (nt + 4) & ~3;
-    float *gy = smem + (size_t)w * 4 * stride;
-    float *gz = gy + stride;
-    float *u = gz + stride;
-    float *v = u + stride;
+    float *zv = smem + (size_t)w * 2 * stride;  // dL/dz, then v = T^-1 dL/dz in place
+    float *u = zv + stride;
+    const float *p0 = partial + (size_t)ch * 2 * Lp;
+    const size_t pstride = (size_t)nch * 2 * Lp;  // between parts
     for (int n = lane; n < nt; n += 32) {
-        float sy = 0.f, sz = 0.f;
-        for (int q = 0; q < nparts; ++q) {
-            const float *p = partial + ((size_t)q * nch + ch) * 2 * Lp;
-            sy += p[n];
-            sz += p[Lp + n];
-        }
-        gy[n] = sy;
-        gz[n] = sz;
+        float sz = 0.f;
+        for (int q = 0; q < nparts; ++q) sz += p0[q * pstride + Lp + n];
+        zv[n] = sz;
     }
-    if (lane == 0) {
-        u[0] = 0.f;
-        v[0] = 0.f;
-        v[nt - 1] = 0.f;
-    }
+    if (lane == 0) u[0] = 0.f;
     __syncwarp();
     // T v = dL/dz on the interior samples 1..nt-2 (v_0 = v_nt-1 = 0)
     const int C = ((nt + 31) >> 5) | 1;
@@ -287,30 +328,37 @@ adj_finalize_kernel(const float *__restrict__ partial, int nparts, long long nch
         if (ib < ie) {
             float up = 0.f;
             for (int k = max(1, ib - kWarmAdj); k < ie; ++k) {
-                const float uk = fmaf(-0.5f, up, gz[k]) * tab.invp[min(k, kSplineTab - 1)];
+                const float uk = fmaf(-0.5f, up, zv[k]) * tab.invp[min(k, kSplineTab - 1)];
                 if (k >= ib) u[k] = uk;
                 up = uk;
             }
         }
     }
-    __syncwarp();
+    __syncwarp();  // every lane is past its reads of dL/dz
     {
         const int kb = max(s, 1), ke = min(e, nt - 1);
         if (kb < ke) {
             float vn = 0.f;
             for (int k = min(nt - 2, ke - 1 + kWarmAdj); k >= kb; --k) {
                 const float vk = fmaf(tab.c[min(k, kSplineTab - 1)], vn, u[k]);
-                if (k < ke) v[k] = vk;
+                if (k < ke) zv[k] = vk;
                 vn = vk;
             }
         }
     }
     __syncwarp();
+    if (lane == 0) {
+        zv[0] = 0.f;
+        zv[nt - 1] = 0.f;
+    }
+    __syncwarp();
     float *dst = grad_rf + ch * (long long)nt;
     for (int n = lane; n < nt; n += 32) {
-        const float vm = n >= 1 ? v[n - 1] : 0.f;
-        const float vp = n + 1 < nt ? v[n + 1] : 0.f;
-        dst[n] = fmaf(0.5f, vm - 2.f * v[n] + vp, gy[n]);
+        float sy = 0.f;
+        for (int q = 0; q < nparts; ++q) sy += p0[q * pstride + n];
+        const float vm = n >= 1 ? zv[n - 1] : 0.f;
+        const float vp = n + 1 < nt ? zv[n + 1] : 0.f;
+        dst[n] = fmaf(0.5f, vm - 2.f * zv[n] + vp, sy);
     }
 }
 
@@ -354,8 +402,8 @@ cudaError_t launch_scatter_one(const AdjArgs &g, cudaStream_t s) {
         make_spline_table(&t);
         return t;
     }();
-    const size_t per_warp = sizeof(float) * 4 * (size_t)((a.nt + 4) & ~3);
-    const int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (96 * 1024) / per_warp));
+    const size_t per_warp = sizeof(float) * 2 * (size_t)((a.nt + 4) & ~3);
+    const int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (112 * 1024) / per_warp));
     const size_t fsmem = per_warp * wpb;
     err = cudaFuncSetAttribute(adj_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)fsmem);
@@ -377,8 +425,19 @@ cudaError_t launch_adjoint_gs(const AdjArgs &g, cudaStream_t s) {
 }
 
 template <typename T>
-cudaError_t launch_adjoint_t(const AdjArgs &g, cudaStream_t s) {
+cudaError_t launch_adjoint_t(const AdjArgs &g0, cudaStream_t s) {
+    AdjArgs g = g0;
     const bool both = g.sumtype == PYCBF_GB_SUM_TX_AND_RX;
+    g.gk = g.gout;
+    if (g.d.pixel_index) {
+        const long long rows = (long long)g.d.nframes * (both ? 1 : g.d.nrx);
+        const long long n = rows * g.d.np;
+        adj_gather_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g.gout, g.d.pixel_index, rows,
+                                                                     g.d.np, g.gk_buf);
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+        g.gk = g.gk_buf;
+    }
     if (g.geom == GEOM_TABBED)
         return both ? launch_adjoint_gs<GEOM_TABBED, PYCBF_GB_SUM_TX_AND_RX, T>(g, s)
                     : launch_adjoint_gs<GEOM_TABBED, PYCBF_GB_SUM_TX_ONLY, T>(g, s);
@@ -402,9 +461,16 @@ int adjoint_rows_warps(int nt) {
     return 0;
 }
 
-size_t adjoint_workspace_bytes(long long nch, long long np, int nt) {
+size_t adjoint_grad_bytes(long long nframes, long long nrx, long long np) {
+    return ((size_t)nframes * (size_t)nrx * (size_t)np * sizeof(float) + 255) & ~(size_t)255;
+}
+
+size_t adjoint_workspace_bytes(long long nframes, long long ntx, long long nrx, long long np,
+                               int nt) {
+    const long long nch = nframes * ntx * nrx;
     const size_t Lp = (size_t)((nt + 1 + 3) & ~3);
-    return (size_t)adjoint_parts(nch, np) * (size_t)nch * 2 * Lp * sizeof(float);
+    return adjoint_grad_bytes(nframes, nrx, np) +
+           (size_t)adjoint_parts(nch, np) * (size_t)nch * 2 * Lp * sizeof(float);
 }
 
 cudaError_t launch_adjoint(const AdjArgs &g, int dtype, cudaStream_t s) {

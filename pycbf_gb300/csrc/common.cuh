@@ -139,12 +139,17 @@ struct AdjArgs {
     float *grad_tautx;    // Tabbed (ntx, np), or NULL
     float *grad_taurx;    // Tabbed (nrx, np), or NULL
     float *grad_slow;     // Synthetic (np), or NULL
+    float *gk_buf;        // workspace: grad_out gathered into kernel pixel order
     float *partial;       // workspace: per-part sums of the spline-record adjoints
+    const float *gk;      // set by launch_adjoint: gk_buf, or grad_out without pixel_index
 };
 // parts of the pixel range whose channel adjoints are summed separately, and
-// the workspace they need
+// the workspace: [gathered gradient (nframes * nrx * np floats, 256-byte
+// rounded)][partial sums (parts * nch * 2 * Lp floats)]
 int adjoint_parts(long long nch, long long np);
-size_t adjoint_workspace_bytes(long long nch, long long np, int nt);
+size_t adjoint_grad_bytes(long long nframes, long long nrx, long long np);
+size_t adjoint_workspace_bytes(long long nframes, long long ntx, long long nrx, long long np,
+                               int nt);
 int adjoint_rows_warps(int nt);  // warps (private accumulation rows) per scatter CTA, 0 = nt too large
 cudaError_t launch_adjoint(const AdjArgs &a, int dtype, cudaStream_t s);
 cudaError_t launch_das_synth_slow(const DasArgs &a, int sumtype, int dtype, cudaStream_t s);

@@ -127,10 +127,12 @@ def test_adjoint_workspace_bytes():
     info = _info(ntx=2, nrx=3, nt=16, nframes=2)
     nch = 2 * 2 * 3
     # parts: enough (channel, part) blocks to fill the GPU, >= 2048 pixels per part
-    n = L.pycbf_gb_adjoint_workspace_bytes(ct.byref(info), 100000)
     lp = (16 + 1 + 3) & ~3
-    assert n % (nch * 2 * lp * 4) == 0 and n // (nch * 2 * lp * 4) == min(48, (2048 + nch - 1) // nch)
-    assert L.pycbf_gb_adjoint_workspace_bytes(ct.byref(info), 100) == nch * 2 * lp * 4
+    grad = lambda np_: (2 * 3 * np_ * 4 + 255) // 256 * 256  # gathered upstream gradient
+    n = L.pycbf_gb_adjoint_workspace_bytes(ct.byref(info), 100000)
+    parts = min(48, (2048 + nch - 1) // nch)
+    assert n == grad(100000) + parts * nch * 2 * lp * 4
+    assert L.pycbf_gb_adjoint_workspace_bytes(ct.byref(info), 100) == grad(100) + nch * 2 * lp * 4
     assert L.pycbf_gb_adjoint_workspace_bytes(ct.byref(info), 0) == 0
 
 
