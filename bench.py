@@ -379,6 +379,46 @@ def run_variants(a, w, dev, taps):
                      "ms_per_call": 1e3 * statistics.mean(times), "frames_per_call": nf,
                      "storage": storage, "interp": kind}
     res.update(run_adjoint_variants(a, w, dev, taps))
+    res.update(run_batch_variants(a, dev))
+    return res
+
+
+def run_batch_variants(a, dev):
+    """64 seeded uneven frames (ntx 1..75, nrx 64..192, nt 1024..4096, grids
+    128x128..512x1024, Tabbed and Synthetic) in one persistent launch replayed
+    as a CUDA graph, launch shape autotuned, for float32 / float16 / bfloat16
+    channel data; the 16-bit images are compared with the float32 ones."""
+    import numpy as np
+    import torch
+
+    from pycbf_gb300 import phantom
+    from pycbf_gb300.batch import BatchBeamformer, beamformers_for
+    frames = phantom.batch_frames(n=64, device=dev)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    reps = max(3, a.steps // 2)
+    res, images32 = {}, None
+    for storage in ("float32", "float16", "bfloat16"):
+        t0 = time.perf_counter()
+        bb = BatchBeamformer(beamformers_for(frames, storage))
+        tune_s = time.perf_counter() - t0
+        outs = bb([f["rf"] for f in frames])
+        t = _event_time(bb.replay, reps, flush, stream)
+        entry = {"value": bb.taps / t, "unit": UNIT, "ms_per_call": 1e3 * t, "frames_per_call": 64,
+                 "storage": storage, "taps_per_call": bb.taps, "launches_per_call": 2,
+                 "config": bb.config.__dict__, "configs_timed": len(bb.timings),
+                 "setup_and_autotune_s": tune_s,
+                 "kinds": {k: sum(f["kind"] == k for f in frames) for k in ("tabbed", "synthetic")}}
+        if storage == "float32":
+            images32 = [o.clone() for o in outs]
+        else:
+            rel = [float(torch.linalg.norm((o - i).double()) / torch.linalg.norm(i.double()))
+                   for o, i in zip(outs, images32)]
+            entry["rel_l2_vs_float32_per_frame"] = {"median": float(np.median(rel)),
+                                                    "max": float(np.max(rel))}
+        res[f"batch64_{storage}"] = entry
+        del bb, outs
+        torch.cuda.empty_cache()
     return res
 
 

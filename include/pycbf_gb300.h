@@ -293,6 +293,61 @@ int pycbf_gb_das_synthetic_adjoint(const pycbf_gb_rfinfo *rf, const void *coef,
                                    size_t workspace_bytes, void *stream);
 
 /* ---------------------------------------------------------------------- */
+/* Uneven batches (no counterpart in the reference): many frames of        */
+/* Tabbed and Synthetic beamformers of any size and storage type,          */
+/* prefiltered and beamformed (cubic, summed over transmits and receives)  */
+/* by two launches -- one batched prefilter, one persistent delay-and-sum  */
+/* that takes (frame, pixel tile) work items from a queue -- so the whole  */
+/* batch can be captured in one CUDA graph.                                */
+/*                                                                        */
+/* Each job is one frame: rf.nframes = 1, rfdata (ntx, nrx, nt); coef its  */
+/* own pycbf_gb_workspace_bytes(&rf, PYCBF_GB_INTERP_CUBIC) bytes          */
+/* (16-byte aligned); out (np) float32.  Tabbed jobs give the tables, np   */
+/* and thresh (geo NULL); Synthetic jobs give geo (np from geo->np; delays */
+/* and masks of pycbf_gb_das_synthetic).  Several jobs may share tables,   */
+/* geometry or pixel_index.                                                */
+/*                                                                        */
+/* pycbf_gb_batch_plan validates every job and writes, into the caller's   */
+/* device buffer plan (pycbf_gb_batch_plan_bytes, 16-byte aligned), the    */
+/* job descriptors and the work items: runs of tiles_per_item (1..8) tiles */
+/* of 128 pixels, in job order (order 0) or largest estimated cost first   */
+/* (order 1).  It fills *info, which pycbf_gb_batch_run needs.             */
+/* pycbf_gb_batch_run queues the prefilter and the delay-and-sum on the   */
+/* stream: tx_chunk (4, 8 or 12) transmits are held in registers at a      */
+/* time; ctas CTAs of 128 threads serve the queue.  With ntx <= tx_chunk   */
+/* a job's image is bitwise the one pycbf_gb_das_tabbed /                  */
+/* pycbf_gb_das_synthetic give for its frame.  run allocates nothing and   */
+/* makes no host-blocking call, so it can be captured in a CUDA graph once */
+/* plan has run; rerunning it (or the graph) reuses the plan's buffers.    */
+/* ---------------------------------------------------------------------- */
+typedef struct pycbf_gb_batch_job {
+    int geom;                       /* 0 Tabbed, 1 Synthetic                          */
+    pycbf_gb_rfinfo rf;
+    const void *rfdata;
+    void *coef;
+    const float *tautx, *apodtx, *taurx, *apodrx;   /* Tabbed                      */
+    long long np;                   /* Tabbed                                         */
+    float thresh;                   /* Tabbed                                         */
+    const pycbf_gb_synthetic *geo;  /* Synthetic (host pointer, copied by plan)       */
+    const int *pixel_index;
+    float *out;
+} pycbf_gb_batch_job;
+
+typedef struct pycbf_gb_batch_info {
+    long long nitems;
+    long long nchannels;
+    int njobs;
+    int max_nt;
+    int tiles_per_item;
+} pycbf_gb_batch_info;
+
+size_t pycbf_gb_batch_plan_bytes(const pycbf_gb_batch_job *jobs, int njobs, int tiles_per_item);
+int pycbf_gb_batch_plan(const pycbf_gb_batch_job *jobs, int njobs, int tiles_per_item, int order,
+                        void *plan, size_t plan_bytes, pycbf_gb_batch_info *info, void *stream);
+int pycbf_gb_batch_run(const void *plan, const pycbf_gb_batch_info *info, int tx_chunk, int ctas,
+                       void *stream);
+
+/* ---------------------------------------------------------------------- */
 /* Measurement utility (no counterpart in the reference): blocks x 256    */
 /* threads each run iters rounds of 8 independent float32 FMAs and store  */
 /* one float to out[blocks*256].  FLOPs = blocks*256*iters*16.  Gives the */

@@ -343,3 +343,51 @@ def max_abs_rel_peak(a, b) -> float:
     b = np.asarray(b, np.float64).ravel()
     peak = np.max(np.abs(b))
     return float(np.max(np.abs(a - b)) / peak) if peak > 0 else float(np.max(np.abs(a - b)))
+
+
+def spline_z64(rf):
+    """Float64 natural-spline records z = y'' dt^2 / 6 of every channel (last axis),
+    the same system as pycbf.c:114-166 (0.5 z_i-1 + 2 z_i + 0.5 z_i+1 =
+    (y_i+1 - 2 y_i + y_i-1) / 2, z_0 = z_n-1 = 0), by a banded solve."""
+    from scipy.linalg import solve_banded
+
+    rf = np.asarray(rf, np.float64)
+    n = rf.shape[-1]
+    flat = rf.reshape(-1, n).T
+    z = np.zeros_like(flat)
+    if n >= 3:
+        d = flat[2:] - 2.0 * flat[1:-1] + flat[:-2]
+        ab = np.zeros((3, n - 2))
+        ab[0, 1:] = 0.5
+        ab[1, :] = 2.0
+        ab[2, :-1] = 0.5
+        z[1:-1] = solve_banded((1, 1), ab, 0.5 * d)
+    return z.T.reshape(rf.shape)
+
+
+def das_fp64_columns(rf, tautx, apodtx, taurx, apodrx, t0, dt, thresh=1e-2, z=None):
+    """Float64 'tx_and_rx' image of the given table columns (any subset of the
+    pixels): natural cubic spline in double, taps decided as in float32
+    (|fl(apodtx apodrx)| >= thresh, t0 <= fl(tautx + taurx) <= xmax,
+    pycbf.c:68-105, 179-207), values at the float64 delay sum."""
+    rf64 = np.asarray(rf, np.float64)
+    ntx, nrx, nt = rf64.shape
+    z = spline_z64(rf64) if z is None else z
+    ttx32, atx32, trx32, arx32 = map(_c32, (tautx, apodtx, taurx, apodrx))
+    x32 = ttx32[:, None, :] + trx32[None, :, :]
+    apod32 = atx32[:, None, :] * arx32[None, :, :]
+    xmax32 = lib().orc_xmax(float(t0), float(dt), int(nt))
+    with np.errstate(invalid="ignore"):
+        ok = (np.abs(apod32) >= np.float32(thresh)) & (x32 >= np.float32(t0)) & (x32 <= xmax32)
+    x = ttx32.astype(np.float64)[:, None, :] + trx32.astype(np.float64)[None, :, :]
+    q = np.where(ok, (x - float(np.float32(t0))) / float(np.float32(dt)), 0.0)
+    j = np.clip(np.floor(q), 0, max(nt - 2, 0)).astype(np.int64)
+    a = (j + 1) - q
+    b = q - j
+    t_i = np.arange(ntx)[:, None, None]
+    r_i = np.arange(nrx)[None, :, None]
+    j1 = np.minimum(j + 1, nt - 1)
+    s = (a * rf64[t_i, r_i, j] + b * rf64[t_i, r_i, j1] + (a ** 3 - a) * z[t_i, r_i, j]
+         + (b ** 3 - b) * z[t_i, r_i, j1])
+    apod = atx32.astype(np.float64)[:, None, :] * arx32.astype(np.float64)[None, :, :]
+    return np.where(ok, apod * s, 0.0).sum(axis=(0, 1))

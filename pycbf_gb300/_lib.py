@@ -29,7 +29,8 @@ EXPORTS = (
     "pycbf_gb_synthetic_rx_mask", "pycbf_gb_dmas", "pycbf_gb_slsc", "pycbf_gb_fp32_probe",
     "pycbf_gb_das_tabbed_cubic_noalloc", "pycbf_gb_das_synthetic_slowness",
     "pycbf_gb_adjoint_workspace_bytes", "pycbf_gb_das_tabbed_adjoint",
-    "pycbf_gb_das_synthetic_adjoint",
+    "pycbf_gb_das_synthetic_adjoint", "pycbf_gb_batch_plan_bytes", "pycbf_gb_batch_plan",
+    "pycbf_gb_batch_run",
 )
 NOALLOC_SCRATCH_BYTES = 64 << 20
 
@@ -46,6 +47,21 @@ class SyntheticGeom(ct.Structure):
     _fields_ = [(n, ct.c_void_p) for n in (
         "ovectx", "nvectx", "t0tx", "alatx", "doftx", "cosalatx", "secalatx", "halfdofsintx",
         "ovecrx", "nvecrx", "cosalarx", "pnts")] + [("np", ct.c_longlong), ("c0", ct.c_float)]
+
+
+class BatchJob(ct.Structure):
+    """pycbf_gb_batch_job: one frame of one beamformer in an uneven batch."""
+    _fields_ = [("geom", ct.c_int), ("rf", RFInfo), ("rfdata", ct.c_void_p), ("coef", ct.c_void_p),
+                ("tautx", ct.c_void_p), ("apodtx", ct.c_void_p), ("taurx", ct.c_void_p),
+                ("apodrx", ct.c_void_p), ("np", ct.c_longlong), ("thresh", ct.c_float),
+                ("geo", ct.POINTER(SyntheticGeom)), ("pixel_index", ct.c_void_p),
+                ("out", ct.c_void_p)]
+
+
+class BatchInfo(ct.Structure):
+    """pycbf_gb_batch_info: what pycbf_gb_batch_run needs from the plan."""
+    _fields_ = [("nitems", ct.c_longlong), ("nchannels", ct.c_longlong), ("njobs", ct.c_int),
+                ("max_nt", ct.c_int), ("tiles_per_item", ct.c_int)]
 
 
 class GPUError(RuntimeError):
@@ -100,10 +116,15 @@ def load() -> ct.CDLL:
                                                   vp, vp, vp, vp, sz, vp]
         L.pycbf_gb_das_synthetic_adjoint.argtypes = [P(RFInfo), vp, P(SyntheticGeom), vp, vp, i,
                                                      vp, vp, vp, vp, sz, vp]
+        L.pycbf_gb_batch_plan_bytes.argtypes = [P(BatchJob), i, i]
+        L.pycbf_gb_batch_plan_bytes.restype = sz
+        L.pycbf_gb_batch_plan.argtypes = [P(BatchJob), i, i, i, vp, sz, P(BatchInfo), vp]
+        L.pycbf_gb_batch_run.argtypes = [vp, P(BatchInfo), i, i, vp]
         for name in EXPORTS:
             if name not in ("pycbf_gb_abi_version", "pycbf_gb_status_string",
                             "pycbf_gb_last_cuda_error", "pycbf_gb_workspace_bytes",
-                            "pycbf_gb_tabbed_plan_bytes", "pycbf_gb_adjoint_workspace_bytes"):
+                            "pycbf_gb_tabbed_plan_bytes", "pycbf_gb_adjoint_workspace_bytes",
+                            "pycbf_gb_batch_plan_bytes"):
                 getattr(L, name).restype = i
         _lib = L
         return L

@@ -1,8 +1,10 @@
 // The C ABI (include/pycbf_gb300.h): host-side validation, then stream-ordered
 // launches.  No allocation, no synchronisation, no mutable shared state.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <limits>
+#include <vector>
 
 #include "common.cuh"
 
@@ -471,6 +473,154 @@ int pycbf_gb_das_synthetic_adjoint(const pycbf_gb_rfinfo *rf, const void *coef,
     g.grad_rf = grad_rf;
     g.grad_slow = grad_slow;
     return run_adjoint(rf, g, workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// uneven batches
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kBatchHeader = 16;  // the work-queue head, padded
+
+long long job_np(const pycbf_gb_batch_job &j) { return j.geom == 0 ? j.np : (j.geo ? j.geo->np : 0); }
+
+long long job_items(const pycbf_gb_batch_job &j, int tiles_per_item) {
+    const long long tiles = (job_np(j) + kBlock - 1) / kBlock;
+    return (tiles + tiles_per_item - 1) / tiles_per_item;
+}
+
+int check_batch_job(const pycbf_gb_batch_job &j) {
+    if (j.geom != 0 && j.geom != 1) return PYCBF_GB_EINVAL;
+    int st = check_rf(&j.rf, j.geom == 1);
+    if (st) return st;
+    if (j.rf.nframes != 1) return PYCBF_GB_EINVAL;
+    if (!j.rfdata || !j.coef || !j.out) return PYCBF_GB_EINVAL;
+    if (reinterpret_cast<uintptr_t>(j.coef) % 16) return PYCBF_GB_EINVAL;
+    if (j.rf.nt > kMaxNtSpline) return PYCBF_GB_ERANGE;
+    if (j.geom == 0) {
+        if (!j.tautx || !j.apodtx || !j.taurx || !j.apodrx || std::isnan(j.thresh))
+            return PYCBF_GB_EINVAL;
+        if (j.np <= 0 || j.np >= (1LL << 31)) return PYCBF_GB_ERANGE;
+    } else {
+        if (!geo_ok(j.geo)) return PYCBF_GB_EINVAL;
+    }
+    return PYCBF_GB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t pycbf_gb_batch_plan_bytes(const pycbf_gb_batch_job *jobs, int njobs, int tiles_per_item) {
+    if (!jobs || njobs <= 0 || tiles_per_item < 1 || tiles_per_item > 8) return 0;
+    long long items = 0;
+    for (int k = 0; k < njobs; ++k) items += job_items(jobs[k], tiles_per_item);
+    return kBatchHeader + sizeof(BatchJob) * (size_t)njobs + sizeof(int2) * (size_t)items;
+}
+
+int pycbf_gb_batch_plan(const pycbf_gb_batch_job *jobs, int njobs, int tiles_per_item, int order,
+                        void *plan, size_t plan_bytes, pycbf_gb_batch_info *info, void *stream) {
+    if (!jobs || njobs <= 0 || !plan || !info) return PYCBF_GB_EINVAL;
+    if (tiles_per_item < 1 || tiles_per_item > 8 || (order != 0 && order != 1))
+        return PYCBF_GB_EINVAL;
+    for (int k = 0; k < njobs; ++k) {
+        int st = check_batch_job(jobs[k]);
+        if (st) return st;
+    }
+    const size_t need = pycbf_gb_batch_plan_bytes(jobs, njobs, tiles_per_item);
+    if (plan_bytes < need || reinterpret_cast<uintptr_t>(plan) % 16) return PYCBF_GB_EWORKSPACE;
+
+    std::vector<BatchJob> desc((size_t)njobs);
+    std::vector<int2> items;
+    std::vector<double> cost;
+    long long ch0 = 0;
+    int max_nt = 1;
+    for (int k = 0; k < njobs; ++k) {
+        const pycbf_gb_batch_job &j = jobs[k];
+        BatchJob &b = desc[(size_t)k];
+        b = BatchJob{};
+        fill_time_axis(b.a, &j.rf);
+        b.a.data = j.coef;
+        b.a.pixel_index = j.pixel_index;
+        b.a.out = j.out;
+        b.a.np = job_np(j);
+        if (j.geom == 0) {
+            b.a.tautx = j.tautx;
+            b.a.apodtx = j.apodtx;
+            b.a.taurx = j.taurx;
+            b.a.apodrx = j.apodrx;
+            b.a.thresh = j.thresh;
+        } else {
+            b.a.geo = *j.geo;
+            b.a.ndim = j.rf.ndim;
+            b.a.thresh = 0.01f;
+        }
+        b.rf = j.rfdata;
+        b.ch0 = ch0;
+        b.geom = j.geom == 0 ? GEOM_TABBED : GEOM_SYNTH;
+        b.dtype = j.rf.dtype;
+        ch0 += j.rf.ntx * j.rf.nrx;
+        max_nt = std::max(max_nt, j.rf.nt);
+        const long long n = job_items(j, tiles_per_item);
+        // relative cost of an item: its taps, synthetic delays weighted up
+        const double c = (double)j.rf.ntx * (double)j.rf.nrx * (j.geom == 1 ? 1.3 : 1.0);
+        for (long long t = 0; t < n; ++t) {
+            items.push_back(make_int2(k, (int)t));
+            cost.push_back(c);
+        }
+    }
+    if (order == 1) {
+        std::vector<size_t> idx(items.size());
+        for (size_t q = 0; q < idx.size(); ++q) idx[q] = q;
+        std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) { return cost[x] > cost[y]; });
+        std::vector<int2> sorted(items.size());
+        for (size_t q = 0; q < idx.size(); ++q) sorted[q] = items[idx[q]];
+        items.swap(sorted);
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    char *base = static_cast<char *>(plan);
+    int st = cuda_status(cudaMemsetAsync(base, 0, kBatchHeader, s));
+    if (st) return st;
+    st = cuda_status(cudaMemcpyAsync(base + kBatchHeader, desc.data(), sizeof(BatchJob) * desc.size(),
+                                     cudaMemcpyHostToDevice, s));
+    if (st) return st;
+    if (!items.empty()) {
+        st = cuda_status(cudaMemcpyAsync(base + kBatchHeader + sizeof(BatchJob) * desc.size(),
+                                         items.data(), sizeof(int2) * items.size(),
+                                         cudaMemcpyHostToDevice, s));
+        if (st) return st;
+    }
+    info->nitems = (long long)items.size();
+    info->nchannels = ch0;
+    info->njobs = njobs;
+    info->max_nt = max_nt;
+    info->tiles_per_item = tiles_per_item;
+    // shared-memory size of the batched prefilter, set outside any capture
+    return cuda_status(launch_batch_spline(reinterpret_cast<const BatchJob *>(base + kBatchHeader),
+                                           njobs, 0, max_nt, s, true));
+}
+
+int pycbf_gb_batch_run(const void *plan, const pycbf_gb_batch_info *info, int tx_chunk, int ctas,
+                       void *stream) {
+    if (!plan || !info || info->njobs <= 0 || info->nitems < 0 || info->max_nt <= 0)
+        return PYCBF_GB_EINVAL;
+    if (tx_chunk != 4 && tx_chunk != 8 && tx_chunk != 12) return PYCBF_GB_EINVAL;
+    if (ctas < 1 || ctas > (1 << 20) || info->tiles_per_item < 1 || info->tiles_per_item > 8)
+        return PYCBF_GB_EINVAL;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const char *base = static_cast<const char *>(plan);
+    const BatchJob *jobs = reinterpret_cast<const BatchJob *>(base + kBatchHeader);
+    const int2 *items = reinterpret_cast<const int2 *>(base + kBatchHeader +
+                                                       sizeof(BatchJob) * (size_t)info->njobs);
+    unsigned long long *counter =
+        reinterpret_cast<unsigned long long *>(const_cast<char *>(base));
+    int st = cuda_status(launch_batch_spline(jobs, info->njobs, info->nchannels, info->max_nt, s,
+                                             false));
+    if (st) return st;
+    return cuda_status(launch_batch_das(jobs, items, info->nitems, info->tiles_per_item, counter,
+                                        tx_chunk, ctas, s));
 }
 
 }  // extern "C"

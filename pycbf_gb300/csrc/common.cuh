@@ -98,6 +98,9 @@ cudaError_t launch_spline(const SplineArgs &a, int dtype, cudaStream_t s);
 // ---------------------------------------------------------------------------
 // delay-and-sum
 // ---------------------------------------------------------------------------
+// pixels (threads) per CTA of the delay-and-sum kernels: one table column each
+constexpr int kBlock = 128;
+
 // GEOM_SYNTH_SLOW: synthetic geometry whose delays are path length x a
 // per-pixel slowness (the differentiable form) instead of path length / c0
 enum Geom { GEOM_TABBED = 0, GEOM_SYNTH = 1, GEOM_SYNTH_SLOW = 2 };
@@ -126,6 +129,24 @@ long long tabbed_plan_words(long long np, int ntx, int nrx);
 cudaError_t launch_tabbed_plan(const DasArgs &a, int interp, int dtype, int *plan, cudaStream_t s);
 cudaError_t launch_das_staged(const DasArgs &a, int interp, int sumtype, int dtype, const int *plan,
                               int *status, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// uneven batches: one frame of one beamformer per job, all in one launch
+// ---------------------------------------------------------------------------
+struct BatchJob {
+    DasArgs a;            // a.data: this frame's coefficient records; a.out: its image (np)
+    const void *rf;       // this frame's channel data (ntx, nrx, nt), storage type
+    long long ch0;        // first channel of this job in the batch's channel numbering
+    int geom;             // GEOM_TABBED or GEOM_SYNTH
+    int dtype;            // storage type
+};
+cudaError_t launch_batch_spline(const BatchJob *jobs, int njobs, long long nch_total, int max_nt,
+                                cudaStream_t s, bool set_attr);
+// items: (job, first tile / tiles_per_item) pairs in processing order; counter:
+// the work-queue head (zero before the launch)
+cudaError_t launch_batch_das(const BatchJob *jobs, const int2 *items, long long nitems,
+                             int tiles_per_item, unsigned long long *counter, int tx_chunk,
+                             int ctas, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // adjoint (gradients of the cubic delay-and-sum; no reference counterpart)

@@ -25,7 +25,6 @@
 
 namespace pgb {
 
-constexpr int kBlock = 128;
 constexpr int kTxReg = 12;
 constexpr float kDxMin = 1e-12f;
 

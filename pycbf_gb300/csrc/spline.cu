@@ -33,23 +33,19 @@ void make_spline_table(SplineTable *t) {
     }
 }
 
+// One channel by one warp: src (nt samples) -> dst (nt records); smem holds
+// three arrays of (nt + 4) & ~3 floats.
 template <typename T>
-__global__ void __launch_bounds__(256)
-spline_coef_kernel(const T *__restrict__ rf, typename CoefRec<T>::raw *__restrict__ coef,
-                   long long nch, int nt, float dt, const __grid_constant__ SplineTable tab) {
-    extern __shared__ float smem[];
+__device__ __forceinline__ void spline_channel(const T *__restrict__ src,
+                                               typename CoefRec<T>::raw *__restrict__ dst, int nt,
+                                               float dt, const SplineTable &tab, float *smem) {
     const int lane = threadIdx.x & 31;
-    const int w = threadIdx.x >> 5;
-    const int wpb = blockDim.x >> 5;
-    const long long ch = (long long)blockIdx.x * wpb + w;
-    if (ch >= nch) return;
     const int stride = (nt + 4) & ~3;  // >= nt+1, keeps every array 16-byte aligned
-    float *y = smem + (size_t)w * 3 * stride;
+    float *y = smem;
     float *u = y + stride;
     float *z = u + stride;
 
     // stage the channel: 16-byte vector loads, several in flight per lane
-    const T *src = rf + ch * (long long)nt;
     constexpr int V = 16 / sizeof(T);
     if ((nt % V) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
         const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
@@ -108,8 +104,58 @@ spline_coef_kernel(const T *__restrict__ rf, typename CoefRec<T>::raw *__restric
         }
     }
     __syncwarp();
-    typename CoefRec<T>::raw *dst = coef + ch * (long long)nt;
     for (int k = lane; k < nt; k += 32) dst[k] = CoefRec<T>::pack(y[k], y[k + 1], z[k], z[k + 1]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+spline_coef_kernel(const T *__restrict__ rf, typename CoefRec<T>::raw *__restrict__ coef,
+                   long long nch, int nt, float dt, const __grid_constant__ SplineTable tab) {
+    extern __shared__ float smem[];
+    const int w = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    const long long ch = (long long)blockIdx.x * wpb + w;
+    if (ch >= nch) return;
+    const int stride = (nt + 4) & ~3;
+    spline_channel<T>(rf + ch * (long long)nt, coef + ch * (long long)nt, nt, dt, tab,
+                      smem + (size_t)w * 3 * stride);
+}
+
+// Batched: one warp per channel of any job (jobs' channels numbered
+// consecutively from BatchJob::ch0); smem per warp sized for the longest.
+template <typename T>
+__device__ __forceinline__ void batch_spline_one(const BatchJob &j, long long ch, float *sm,
+                                                 const SplineTable &tab) {
+    using raw = typename CoefRec<T>::raw;
+    const int nt = j.a.nt;
+    spline_channel<T>(static_cast<const T *>(j.rf) + ch * (long long)nt,
+                      static_cast<raw *>(const_cast<void *>(j.a.data)) + ch * (long long)nt, nt,
+                      j.a.dt, tab, sm);
+}
+
+__global__ void __launch_bounds__(256)
+batch_spline_kernel(const BatchJob *__restrict__ jobs, int njobs, long long nch_total,
+                    int max_stride, const __grid_constant__ SplineTable tab) {
+    extern __shared__ float smem[];
+    const int w = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    const long long gc = (long long)blockIdx.x * wpb + w;
+    if (gc >= nch_total) return;
+    // the job whose channel range holds gc (jobs sorted by ch0)
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].ch0 <= gc) lo = mid;
+        else hi = mid - 1;
+    }
+    const BatchJob &j = jobs[lo];
+    const long long ch = gc - j.ch0;
+    float *sm = smem + (size_t)w * 3 * max_stride;
+    switch (j.dtype) {
+        case PYCBF_GB_F32: batch_spline_one<float>(j, ch, sm, tab); break;
+        case PYCBF_GB_F16: batch_spline_one<__half>(j, ch, sm, tab); break;
+        default: batch_spline_one<__nv_bfloat16>(j, ch, sm, tab); break;
+    }
 }
 
 template <typename T>
@@ -131,6 +177,30 @@ static cudaError_t launch_spline_t(const SplineArgs &a, cudaStream_t s) {
     spline_coef_kernel<T><<<(unsigned)blocks, 32 * wpb, smem, s>>>(
         static_cast<const T *>(a.rf), static_cast<typename CoefRec<T>::raw *>(a.coef), a.nch, a.nt,
         a.dt, tab);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_spline(const BatchJob *jobs, int njobs, long long nch_total, int max_nt,
+                                cudaStream_t s, bool set_attr) {
+    const int stride = (max_nt + 4) & ~3;
+    const size_t per_warp = sizeof(float) * 3 * (size_t)stride;
+    const int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (96 * 1024) / per_warp));
+    const size_t smem = per_warp * wpb;
+    if (smem > 227 * 1024) return cudaErrorInvalidValue;
+    static SplineTable tab = [] {
+        SplineTable t;
+        make_spline_table(&t);
+        return t;
+    }();
+    if (set_attr) {
+        cudaError_t err = cudaFuncSetAttribute(batch_spline_kernel,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return err;
+    }
+    if (nch_total <= 0) return cudaSuccess;
+    const long long blocks = (nch_total + wpb - 1) / wpb;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    batch_spline_kernel<<<(unsigned)blocks, 32 * wpb, smem, s>>>(jobs, njobs, nch_total, stride, tab);
     return cudaGetLastError();
 }
 

@@ -223,3 +223,78 @@ def two_layer_pw_synthetic(nele=128, pitch=0.3e-3, nsteer=11, max_deg=10.0, fs=2
                                   fnum=fnum, seed=seed, xout=xout, zout=zout,
                                   slowness_true=layered_slowness(pnts[:, 1], c_top, c_bottom,
                                                                  z_interface)))
+
+
+def pw_tabbed_tables_torch(steers, xele, xout, zout, c, fnum, device):
+    """The plane-wave tables of helpers.pw_tx_tables(ones=True) / rx_tables(hann=True),
+    built with torch on the device (float32 results, float64 arithmetic)."""
+    dev = _device(device)
+    f64 = dict(dtype=torch.float64, device=dev)
+    st = torch.as_tensor(np.asarray(steers, np.float64), **f64)
+    xe = torch.as_tensor(np.asarray(xele, np.float64), **f64)
+    X, Z = torch.meshgrid(torch.as_tensor(xout, **f64), torch.as_tensor(zout, **f64), indexing="ij")
+    X, Z = X.reshape(-1), Z.reshape(-1)
+    O = torch.where(st <= 0, xe[-1], xe[0])
+    tautx = ((X[None] - O[:, None]) * torch.sin(st)[:, None] + Z[None] * torch.cos(st)[:, None]) / c
+    dx = X[None] - xe[:, None]
+    taurx = torch.sqrt(dx * dx + Z[None] * Z[None]) / c
+    half = torch.clamp(Z[None] / (2 * fnum), min=1e-30)
+    inside = dx.abs() - Z[None] / (2 * fnum) < 0
+    w = torch.cos(0.5 * math.pi * torch.clamp(dx / half, -1.0, 1.0)) ** 2
+    apodrx = torch.where(inside, w, torch.zeros_like(w))
+    f32 = lambda t: t.to(torch.float32).contiguous()
+    return f32(tautx), torch.ones_like(f32(tautx)), f32(taurx), f32(apodrx)
+
+
+BATCH_NTX = (1, 5, 11, 31, 75)
+BATCH_NRX = (64, 128, 192)
+BATCH_NT = (1024, 2048, 4096)
+BATCH_NX = (128, 256, 512)
+BATCH_NZ = (128, 256, 512, 1024)
+
+
+def batch_frames(n=64, seed=64, n_speckle=300, n_points=5, pitch=0.2e-3, max_deg=16.0,
+                 window_s=64e-6, fnum=1.5, c=1540.0, device=None):
+    """Seeded uneven frames: kind (tabbed / synthetic), ntx from BATCH_NTX, nrx
+    from BATCH_NRX, nt from BATCH_NT, grid nx x nz from BATCH_NX x BATCH_NZ
+    (128 x 128 .. 512 x 1024).  The record window is window_s for every nt
+    (fs = nt / window_s, pulse centre fs / 5).  Returns dicts with the
+    beamformer arguments (tables as CUDA tensors for Tabbed frames) and rf."""
+    dev = _device(device)
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        kind = "tabbed" if rng.uniform() < 0.5 else "synthetic"
+        ntx = int(rng.choice(BATCH_NTX))
+        nrx = int(rng.choice(BATCH_NRX))
+        nt = int(rng.choice(BATCH_NT))
+        nx, nz = int(rng.choice(BATCH_NX)), int(rng.choice(BATCH_NZ))
+        fs = nt / window_s
+        fc = fs / 5.0
+        xele = helpers.element_positions(nrx, pitch)
+        half = 0.5 * nrx * pitch
+        steers = np.radians(np.linspace(-max_deg, max_deg, ntx)) if ntx > 1 else np.zeros(1)
+        xout = np.linspace(-half, half, nx)
+        zout = np.linspace(5e-3, 45e-3, nz)
+        pos, amp = scatterers(seed * 1000 + k, n_speckle, n_points, (-half, half), (5e-3, 45e-3))
+        entry = dict(kind=kind, ntx=ntx, nrx=nrx, nt=nt, nx=nx, nz=nz, t0=0.0, dt=1.0 / fs)
+        if kind == "tabbed":
+            tautx, apodtx, taurx, apodrx = pw_tabbed_tables_torch(steers, xele, xout, zout, c,
+                                                                  fnum, dev)
+            O = np.where(steers <= 0, xele[-1], xele[0])
+            tt = ((pos[None, :, 0] - O[:, None]) * np.sin(steers)[:, None]
+                  + pos[None, :, 1] * np.cos(steers)[:, None]) / c
+            entry.update(tautx=tautx, apodtx=apodtx, taurx=taurx, apodrx=apodrx)
+        else:
+            geo = helpers.pw_synthetic_points(steers, c, c, xele, fnum)
+            d = pos[None, :, :] - geo["ovectx"][:, None, :]
+            proj = np.sum(d * geo["nvectx"][:, None, :], axis=-1)
+            tt = np.sign(proj) * np.linalg.norm(d, axis=-1) / c + geo["t0tx"][:, None]
+            geo = dict(geo, c0=c, pnts=helpers.pixel_grid(xout, zout))
+            entry.update(geometry=geo)
+        tr = np.hypot(pos[None, :, 0] - xele[:, None], pos[None, :, 1]) / c
+        entry["rf"] = simulate_channels(torch.tensor(tt, device=dev), torch.tensor(tr, device=dev),
+                                        torch.tensor(amp, device=dev), 0.0, 1.0 / fs, nt, fc, 0.6,
+                                        -40.0, seed * 1000 + k)
+        out.append(entry)
+    return out

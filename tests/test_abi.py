@@ -158,3 +158,37 @@ def test_adjoint_entry_points_validate_first():
                                             None, p, None, 0, None) == _lib.EINVAL
     assert L.pycbf_gb_das_synthetic_slowness(ct.byref(_info(ndim=4)), p, ct.byref(geo), p, None,
                                              3, p, None) == _lib.EINVAL
+
+
+def test_batch_plan_validates_jobs():
+    L = _lib.load()
+    p = ct.c_void_p(16)
+    j = _lib.BatchJob()
+    j.geom = 0
+    j.rf = _info()
+    j.rfdata = j.coef = j.out = 16
+    j.tautx = j.apodtx = j.taurx = j.apodrx = 16
+    j.np = 300
+    j.thresh = 0.01
+    jobs = (_lib.BatchJob * 2)(j, j)
+    # 300 pixels = 3 tiles of 128: 3 items, or 2 of two tiles
+    hdr, desc = 16, None
+    n1 = L.pycbf_gb_batch_plan_bytes(jobs, 2, 1)
+    n2 = L.pycbf_gb_batch_plan_bytes(jobs, 2, 2)
+    assert n1 - n2 == 2 * 8 * (3 - 2)
+    assert L.pycbf_gb_batch_plan_bytes(jobs, 2, 9) == 0
+    info = _lib.BatchInfo()
+    plan = lambda js, n=2, tpi=1, order=1, nbytes=n1: L.pycbf_gb_batch_plan(
+        js, n, tpi, order, p, nbytes, ct.byref(info), None)
+    assert plan(jobs, nbytes=n1 - 1) == _lib.EWORKSPACE
+    assert plan(jobs, order=2) == _lib.EINVAL
+    bad = _lib.BatchJob.from_buffer_copy(j)
+    bad.rf.nframes = 2
+    assert plan((_lib.BatchJob * 2)(j, bad)) == _lib.EINVAL
+    bad = _lib.BatchJob.from_buffer_copy(j)
+    bad.coef = 8
+    assert plan((_lib.BatchJob * 2)(j, bad)) == _lib.EINVAL
+    bad = _lib.BatchJob.from_buffer_copy(j)
+    bad.geom = 1  # synthetic without geometry
+    assert plan((_lib.BatchJob * 2)(j, bad)) == _lib.EINVAL
+    assert L.pycbf_gb_batch_run(p, ct.byref(info), 6, 10, None) == _lib.EINVAL

@@ -143,3 +143,17 @@ def test_interp_known_answer():
         kat = json.load(fp)
     assert abs(float(np.sum(cubic.astype(np.float64))) - kat["checksum_cubic"]) < 1e-6 * abs(
         kat["checksum_cubic"])
+
+
+def test_fp64_columns_agree_with_the_scipy_spline():
+    """das_fp64_columns (banded float64 spline on the float32 time axis) and
+    das_tabbed_fp64 (SciPy CubicSpline on the float64 axis) agree to the
+    axis difference (~1e-6)."""
+    from pycbf_gb300 import phantom
+    w = phantom.linear_pw_tabbed(nele=16, nsteer=3, nt=512, nx=24, nz=40, xlim=(-2.4e-3, 2.4e-3),
+                                 zlim=(4e-3, 12e-3), n_speckle=200, n_points=3, device="cpu")
+    a = oracle.das_tabbed_fp64(w.rf, w.tautx, w.apodtx, w.taurx, w.apodrx, w.t0, w.dt, w.nt)
+    sub = np.arange(0, w.tautx.shape[1], 7)
+    c = oracle.das_fp64_columns(w.rf, w.tautx[:, sub], w.apodtx[:, sub], w.taurx[:, sub],
+                                w.apodrx[:, sub], w.t0, w.dt)
+    assert oracle.rel_l2(c, a[sub]) <= 1e-5
