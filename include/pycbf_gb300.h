@@ -44,7 +44,10 @@ enum {
     PYCBF_GB_INTERP_NEAREST = 0,      /* pycbf.c:264-267 (usf = 1)                          */
     PYCBF_GB_INTERP_LINEAR = 1,       /* two-point part of the cubic formula, cubic's range */
     PYCBF_GB_INTERP_CUBIC = 2,        /* natural cubic spline, pycbf.c:68-166               */
-    PYCBF_GB_INTERP_LINEAR_FLOOR = 3  /* __engines__.cu:36-53 as written (floor sample)     */
+    PYCBF_GB_INTERP_LINEAR_FLOOR = 3, /* __engines__.cu:36-53 as written (floor sample)     */
+    PYCBF_GB_INTERP_KORDER = 4,       /* k-point cubic, __engines__.cu:292-355: _poly calls  */
+    PYCBF_GB_INTERP_AKIMA = 5,        /* __engines__.cu:188-269: _poly calls                 */
+    PYCBF_GB_INTERP_MAKIMA = 6        /* __engines__.cu:58-183: _poly calls                  */
 };
 
 /* how taps are summed; 0..3 are the reference's flag values (__engines__.cu:500-504) */
@@ -165,6 +168,52 @@ int pycbf_gb_das_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef,
                                     const float *apodrx, long long np, const int *pixel_index,
                                     float thresh, int sumtype, const void *plan, float *out,
                                     void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Cubic upsampling for nearest-neighbour interpolation with usf > 1.      */
+/* Replaces the upsampling inside beamform_nearest (pycbf/cpu/pycbf.c:     */
+/* 223-253): out (nframes, ntx, nrx, usf*(nt-1)+1) float32, sample it the  */
+/* natural cubic spline of the channel at t0 + it*fl(dt/usf) (0 outside    */
+/* [t0, t0 + dt*(nt-1)]).  workspace: pycbf_gb_workspace_bytes(rf, CUBIC)  */
+/* bytes for the spline coefficients; out: pycbf_gb_upsampled_bytes.      */
+/* Beamform the result with interp = nearest and an rfinfo whose nt is     */
+/* usf*(nt-1)+1, dt is the float32 quotient dt/usf and dtype is F32; the   */
+/* taps are then those of beamform_nearest with that usf.                  */
+/* ---------------------------------------------------------------------- */
+size_t pycbf_gb_upsampled_bytes(const pycbf_gb_rfinfo *rf, int usf);
+int pycbf_gb_upsample(const pycbf_gb_rfinfo *rf, const void *rfdata, int usf, void *workspace,
+                      size_t workspace_bytes, float *out, size_t out_bytes, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* The interpolators the reference has only on the GPU: korder cubic (the  */
+/* default of pycbf.gpu, k-point derivative estimate with the k x k matrix */
+/* S of gpu/__core_bf_classes__.py:366-395), akima and makima              */
+/* (__engines__.cu:58-355).  A prefilter turns every interval of every     */
+/* channel into the float32 coefficients of its cubic (float32 records     */
+/* whatever the storage type); the delay-and-sum then gathers one record   */
+/* per tap like the cubic spline path.                                     */
+/*   pycbf_gb_poly_coefficients: interp KORDER (k even, 0..128, k <= nt;   */
+/*     S: host float32 k*k row-major; k = 0 gives zero derivatives, what   */
+/*     the reference's Synthetic korder kernel computes, its k arriving as */
+/*     0), AKIMA or MAKIMA (nt >= 5; k, S ignored).  coef: 16-byte aligned,*/
+/*     pycbf_gb_poly_workspace_bytes bytes.                                */
+/*   pycbf_gb_das_tabbed_poly / _synthetic_poly: as pycbf_gb_das_tabbed /  */
+/*     _synthetic without plan and workspace, on those coefficients.       */
+/* Range rules of the reference's kernels: korder fills outside            */
+/* [t0, t0 + dt*(nt-1)] (that bound one fused multiply-add, as NVRTC       */
+/* compiles it); akima/makima return y[nt-1] at the last knot.  A tap      */
+/* contributes when |apodtx*apodrx| >= thresh and it is in range.          */
+/* ---------------------------------------------------------------------- */
+size_t pycbf_gb_poly_workspace_bytes(const pycbf_gb_rfinfo *rf, int interp, int k);
+int pycbf_gb_poly_coefficients(const pycbf_gb_rfinfo *rf, const void *rfdata, int interp, int k,
+                               const float *S, void *coef, size_t coef_bytes, void *stream);
+int pycbf_gb_das_tabbed_poly(const pycbf_gb_rfinfo *rf, const void *coef, int interp,
+                             const float *tautx, const float *apodtx, const float *taurx,
+                             const float *apodrx, long long np, const int *pixel_index,
+                             float thresh, int sumtype, float *out, void *stream);
+int pycbf_gb_das_synthetic_poly(const pycbf_gb_rfinfo *rf, const void *coef, int interp,
+                                const pycbf_gb_synthetic *geo, const int *pixel_index,
+                                int sumtype, float *out, void *stream);
 
 /* ---------------------------------------------------------------------- */
 /* Synthetic-point delay-and-sum: delays and masks computed per pixel on   */

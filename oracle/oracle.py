@@ -84,6 +84,10 @@ def lib() -> ct.CDLL:
                                            _i, _p, _p, _p, _p, _p, _p, _p]
             L.orc_dmas.argtypes = [_p, _ll, _ll, _p, _i, _i, _i, _p]
             L.orc_slsc.argtypes = [_p, _p, _i, _i, _i, _i, _i, _p]
+            L.orc_poly_index.argtypes = [_i, _f, _f, _f, _i]
+            L.orc_poly_index.restype = _i
+            L.orc_das_poly.argtypes = [_i, _i, _p, _f, _f, _i, _p, _i, _i, _ll, _f, _p, _p, _p, _p,
+                                       _i, _p]
             _LIB = L
         return _LIB
 
@@ -210,7 +214,7 @@ def tap_census(tautx, apodtx, taurx, apodrx, t0, dt, nt, interp="cubic", usf=1, 
     ntx, nrx, np_ = tautx.shape[0], taurx.shape[0], tautx.shape[1]
     count = np.zeros(np_, dtype=np.int32)
     isum = np.zeros(np_, dtype=np.int64)
-    code = 1 if interp == "nearest" else 0
+    code = {"nearest": 1, "korder_cubic": 4, "akima": 5, "makima": 6}.get(interp, 0)
     lib().orc_tap_census(code, int(usf), float(t0), float(dt), int(nt), ntx, nrx, np_,
                          float(thresh), _ptr(tautx), _ptr(apodtx), _ptr(taurx), _ptr(apodrx),
                          _ptr(count), _ptr(isum))
@@ -391,3 +395,44 @@ def das_fp64_columns(rf, tautx, apodtx, taurx, apodrx, t0, dt, thresh=1e-2, z=No
          + (b ** 3 - b) * z[t_i, r_i, j1])
     apod = atx32.astype(np.float64)[:, None, :] * arx32.astype(np.float64)[None, :, :]
     return np.where(ok, apod * s, 0.0).sum(axis=(0, 1))
+
+
+POLY_CODES = {"korder_cubic": 4, "akima": 5, "makima": 6}
+
+
+def korder_S(k):
+    """The k x k derivative matrix of korder cubic interpolation, C^-1 P
+    (pycbf/gpu/__core_bf_classes__.py:366-395, from the published k-point
+    method of Praesius and Jensen), float64 then rounded to float32."""
+    c00 = np.ones(k)
+    c00[1:-1] = 4
+    cp1 = np.ones(k - 1)
+    cp1[0] = 2
+    C = np.diag(c00) + np.diag(cp1, 1) + np.diag(cp1[::-1], -1)
+    pp1 = 3 * np.ones(k - 1)
+    pp1[0] = 2
+    P = np.diag(pp1, 1) + np.diag(-pp1[::-1], -1)
+    P[0, 0] = -2.5
+    P[-1, -1] = 2.5
+    P[0, 2] = 0.5
+    P[-1, -3] = -0.5
+    return (np.linalg.inv(C) @ P).astype(np.float32)
+
+
+def das_poly(rf, tautx, apodtx, taurx, apodrx, t0, dt, nt, interp, k=8, S=None, thresh=1e-2,
+             sumtype="tx_and_rx"):
+    """Float32 Tabbed image with korder_cubic (k, S), akima or makima (restated
+    from pycbf/gpu/__engines__.cu:58-355)."""
+    rf = _c32(rf)
+    tautx, apodtx, taurx, apodrx = map(_c32, (tautx, apodtx, taurx, apodrx))
+    ntx, nrx, np_ = tautx.shape[0], taurx.shape[0], tautx.shape[1]
+    code = POLY_CODES[interp]
+    if code == 4:
+        S = korder_S(k) if S is None else _c32(S)
+    else:
+        S, k = np.zeros((1, 1), np.float32), 0
+    out = np.zeros(out_size(sumtype, ntx, nrx, np_), dtype=np.float32)
+    lib().orc_das_poly(code, int(k), _ptr(S), float(t0), float(dt), int(nt), _ptr(rf), ntx, nrx,
+                       np_, float(thresh), _ptr(tautx), _ptr(apodtx), _ptr(taurx), _ptr(apodrx),
+                       SUMTYPE_CODES[sumtype], _ptr(out))
+    return out

@@ -244,6 +244,169 @@ ORC_EXPORT void orc_das_tabbed(int interp, int usf, float t0, float dt, int nt,
 }
 
 /* ------------------------------------------------------------------------ */
+/* The interpolators the reference has only in its CUDA file: korder cubic  */
+/* (__engines__.cu:292-355, S from gpu/__core_bf_classes__.py:366-395),     */
+/* akima (:188-269) and makima (:58-183).  The reference compiles them with */
+/* NVRTC, whose default contracts x0 + dx*n and x - x0 - dx*n into one     */
+/* fused multiply-add each; they are written as fmaf here, every other      */
+/* operation as in the source, one rounding each.  Out-of-range values are  */
+/* the fill 0.  Two reads past the channel in the reference are given       */
+/* defined values: an akima/makima index at or past nx-1 (x a hair below    */
+/* the last knot with the quotient rounded up) returns y[nx-1].             */
+/* ------------------------------------------------------------------------ */
+ORC_EXPORT int orc_poly_index(int kind, float x, float x0, float dx, int nx)
+{
+    /* knot index of a tap, or -1 when the fill applies */
+    float xn = fmaf(dx, (float)(nx - 1), x0);
+    if (kind == 4) {
+        int ixin = (int)((x - x0) / dx);
+        if ((x < x0) || (ixin > nx - 1) || (x > xn)) return -1;
+        return ixin;
+    }
+    if (x == xn) return nx - 1;
+    if ((x < x0) || (x > xn)) return -1;
+    int ixo = (int)((x - x0) / dx);
+    return ixo > nx - 1 ? nx - 1 : ixo;
+}
+
+static float orc_korder_point(float x, const float *y, int nx, float x0, float dx,
+                              const float *S, int k)
+{
+    int ixin = orc_poly_index(4, x, x0, dx, nx);
+    if (ixin < 0) return 0.0f;
+    if (ixin == nx - 1) return y[nx - 1];
+    int ik0, iy0;
+    if (ixin < k / 2) {
+        ik0 = ixin;
+        iy0 = 0;
+    } else if (ixin > nx - k / 2 - 1) {
+        ik0 = k - nx + ixin;
+        iy0 = nx - k;
+    } else {
+        ik0 = (k - 1) / 2;
+        iy0 = ixin - (k - 1) / 2;
+    }
+    float y0 = y[ixin], y1 = y[ixin + 1], yp0 = 0.0f, yp1 = 0.0f;
+    for (int i = 0; i < k; ++i) {
+        yp0 = fmaf(S[ik0 * k + i], y[iy0 + i], yp0);
+        yp1 = fmaf(S[ik0 * k + k + i], y[iy0 + i], yp1);
+    }
+    float xnorm = fmaf(-dx, (float)ixin, x - x0) / dx;
+    float a0 = y0, a1 = yp0;
+    float a2 = 3.0f * (y1 - y0) - 2.0f * yp0 - yp1;
+    float a3 = 2.0f * (y0 - y1) + yp0 + yp1;
+    return a0 + a1 * xnorm + a2 * xnorm * xnorm + a3 * xnorm * xnorm * xnorm;
+}
+
+/* the one-sided slopes (sp0, sp1) and secant mp0 of interval ixo */
+ORC_EXPORT void orc_akima_slopes(const float *y, int nx, int ixo, int makima, float *sp0_,
+                                 float *sp1_, float *mp0_)
+{
+    float mm2 = 0, mm1 = 0, mp0 = 0, mp1 = 0, mp2 = 0, w0, w1, sp0, sp1;
+#define ORC_W(p, q) (fabsf((p) - (q)) + (makima ? fabsf((p) + (q)) / 2 : 0.0f))
+    if (ixo == 0) {
+        mp0 = y[ixo + 1] - y[ixo + 0];
+        mp1 = y[ixo + 2] - y[ixo + 1];
+        sp0 = mp0;
+        sp1 = (mp0 + mp1) / 2;
+    } else if (ixo == 1) {
+        mm1 = y[ixo + 0] - y[ixo - 1];
+        mp0 = y[ixo + 1] - y[ixo - 0];
+        mp1 = y[ixo + 2] - y[ixo + 1];
+        mp2 = y[ixo + 3] - y[ixo + 2];
+        sp0 = (mp0 + mm1) / 2;
+        if ((mm1 == mp0) && (mp0 == mp1) && (mp1 == mp2)) sp1 = 0;
+        else {
+            w0 = ORC_W(mp2, mp1);
+            w1 = ORC_W(mp0, mm1);
+            sp1 = (w0 * mp0 + w1 * mp1) / (w0 + w1);
+        }
+    } else if (ixo == nx - 3) {
+        mm2 = y[ixo - 1] - y[ixo - 2];
+        mm1 = y[ixo + 0] - y[ixo - 1];
+        mp0 = y[ixo + 1] - y[ixo - 0];
+        mp1 = y[ixo + 2] - y[ixo + 1];
+        if ((mm2 == mm1) && (mm1 == mp0) && (mp0 == mp1)) sp0 = 0;
+        else {
+            w0 = ORC_W(mp1, mp0);
+            w1 = ORC_W(mm1, mm2);
+            sp0 = (w0 * mm1 + w1 * mp0) / (w0 + w1);
+        }
+        sp1 = (mp0 + mp1) / 2;
+    } else if (ixo == nx - 2) {
+        mm1 = y[ixo + 0] - y[ixo - 1];
+        mp0 = y[ixo + 1] - y[ixo + 0];
+        sp0 = (mm1 + mp0) / 2;
+        sp1 = mp0;
+    } else {
+        mm2 = y[ixo - 1] - y[ixo - 2];
+        mm1 = y[ixo + 0] - y[ixo - 1];
+        mp0 = y[ixo + 1] - y[ixo + 0];
+        mp1 = y[ixo + 2] - y[ixo + 1];
+        mp2 = y[ixo + 3] - y[ixo + 2];
+        if ((mm2 == mm1) && (mm1 == mp0) && (mp0 == mp1)) sp0 = 0;
+        else {
+            w0 = ORC_W(mp1, mp0);
+            w1 = ORC_W(mm1, mm2);
+            sp0 = (w0 * mm1 + w1 * mp0) / (w0 + w1);
+        }
+        if ((mm1 == mp0) && (mp0 == mp1) && (mp1 == mp2)) sp1 = 0;
+        else {
+            w0 = ORC_W(mp2, mp1);
+            w1 = ORC_W(mp0, mm1);
+            sp1 = (w0 * mp0 + w1 * mp1) / (w0 + w1);
+        }
+    }
+#undef ORC_W
+    *sp0_ = sp0;
+    *sp1_ = sp1;
+    *mp0_ = mp0;
+}
+
+static float orc_akima_point(float x, const float *y, int nx, float x0, float dx, int makima)
+{
+    int ixo = orc_poly_index(5, x, x0, dx, nx);
+    if (ixo < 0) return 0.0f;
+    if (ixo == nx - 1) return y[nx - 1];
+    float sp0, sp1, mp0;
+    orc_akima_slopes(y, nx, ixo, makima, &sp0, &sp1, &mp0);
+    float a = y[ixo];
+    float b = sp0;
+    float c = (3 * mp0 - 2 * sp0 - sp1) / dx;
+    float d = (sp0 + sp1 - 2 * mp0) / (dx * dx);
+    float delta = x - fmaf(dx, (float)ixo, x0);
+    return a + b * delta + c * delta * delta + d * delta * delta * delta;
+}
+
+/* Tabbed image with kind 4 (korder, S k x k), 5 (akima), 6 (makima); a tap
+ * contributes when |apodtx*apodrx| >= thresh and it is in range; sumtype
+ * codes as orc_das_tabbed. */
+ORC_EXPORT void orc_das_poly(int kind, int k, const float *S, float t0, float dt, int nt,
+                             const float *rf, int ntx, int nrx, long long np, float thresh,
+                             const float *tautx, const float *apodtx, const float *taurx,
+                             const float *apodrx, int sumtype, float *out)
+{
+    for (int itx = 0; itx < ntx; ++itx)
+        for (int irx = 0; irx < nrx; ++irx) {
+            long long off;
+            if (sumtype == 0) off = np * ((long long)irx + (long long)itx * nrx);
+            else if (sumtype == 1) off = np * irx;
+            else if (sumtype == 2) off = np * itx;
+            else off = 0;
+            const float *sig = rf + ((long long)itx * nrx + irx) * nt;
+            for (long long i = 0; i < np; ++i) {
+                float apod = apodtx[itx * np + i] * apodrx[irx * np + i];
+                if (!(fabsf(apod) >= thresh)) continue;
+                float x = tautx[itx * np + i] + taurx[irx * np + i];
+                if (orc_poly_index(kind, x, t0, dt, nt) < 0) continue;
+                float v = kind == 4 ? orc_korder_point(x, sig, nt, t0, dt, S, k)
+                                    : orc_akima_point(x, sig, nt, t0, dt, kind == 6);
+                out[off + i] += apod * v;
+            }
+        }
+}
+
+/* ------------------------------------------------------------------------ */
 /* tap census: per pixel, the number of contributing (tx, rx) taps and the  */
 /* sum of their sample indices (knot j for cubic/linear, it for nearest).   */
 /* A tap contributes when |apodtx*apodrx| >= thresh and it is in range.     */
@@ -267,6 +430,9 @@ ORC_EXPORT void orc_tap_census(int interp, int usf, float t0, float dt, int nt,
                 if (interp == 1) {
                     idx = orc_nearest_index(x, t0, dtu);
                     if (idx < 0 || idx >= ntu) continue;
+                } else if (interp >= 4) {
+                    idx = orc_poly_index(interp, x, t0, dt, nt);
+                    if (idx < 0) continue;
                 } else {
                     if ((x < t0) || (x > xmax)) continue;
                     idx = orc_cubic_index(x, t0, dt);

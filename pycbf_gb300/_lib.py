@@ -17,7 +17,8 @@ OK, EINVAL, ERANGE, EWORKSPACE, EUNSUPPORTED, ECUDA = range(6)
 # storage types
 F32, F16, BF16 = 0, 1, 2
 # interpolation kinds
-INTERP = {"nearest": 0, "linear": 1, "cubic": 2, "linear_floor": 3}
+INTERP = {"nearest": 0, "linear": 1, "cubic": 2, "linear_floor": 3, "korder_cubic": 4, "akima": 5,
+          "makima": 6}
 # sum types (0..3 are the reference's flag values)
 SUMTYPE = {"none": 0, "tx_only": 1, "rx_only": 2, "tx_and_rx": 3, "dmas_ssr": 4, "dmas_power": 5}
 
@@ -30,7 +31,9 @@ EXPORTS = (
     "pycbf_gb_das_tabbed_cubic_noalloc", "pycbf_gb_das_synthetic_slowness",
     "pycbf_gb_adjoint_workspace_bytes", "pycbf_gb_das_tabbed_adjoint",
     "pycbf_gb_das_synthetic_adjoint", "pycbf_gb_batch_plan_bytes", "pycbf_gb_batch_plan",
-    "pycbf_gb_batch_run",
+    "pycbf_gb_batch_run", "pycbf_gb_upsampled_bytes", "pycbf_gb_upsample",
+    "pycbf_gb_poly_workspace_bytes", "pycbf_gb_poly_coefficients", "pycbf_gb_das_tabbed_poly",
+    "pycbf_gb_das_synthetic_poly",
 )
 NOALLOC_SCRATCH_BYTES = 64 << 20
 
@@ -120,11 +123,22 @@ def load() -> ct.CDLL:
         L.pycbf_gb_batch_plan_bytes.restype = sz
         L.pycbf_gb_batch_plan.argtypes = [P(BatchJob), i, i, i, vp, sz, P(BatchInfo), vp]
         L.pycbf_gb_batch_run.argtypes = [vp, P(BatchInfo), i, i, vp]
+        L.pycbf_gb_upsampled_bytes.argtypes = [P(RFInfo), i]
+        L.pycbf_gb_upsampled_bytes.restype = sz
+        L.pycbf_gb_upsample.argtypes = [P(RFInfo), vp, i, vp, sz, vp, sz, vp]
+        L.pycbf_gb_poly_workspace_bytes.argtypes = [P(RFInfo), i, i]
+        L.pycbf_gb_poly_workspace_bytes.restype = sz
+        L.pycbf_gb_poly_coefficients.argtypes = [P(RFInfo), vp, i, i, vp, vp, sz, vp]
+        L.pycbf_gb_das_tabbed_poly.argtypes = [P(RFInfo), vp, i, vp, vp, vp, vp, ll, vp, f, i, vp,
+                                               vp]
+        L.pycbf_gb_das_synthetic_poly.argtypes = [P(RFInfo), vp, i, P(SyntheticGeom), vp, i, vp,
+                                                  vp]
         for name in EXPORTS:
             if name not in ("pycbf_gb_abi_version", "pycbf_gb_status_string",
                             "pycbf_gb_last_cuda_error", "pycbf_gb_workspace_bytes",
                             "pycbf_gb_tabbed_plan_bytes", "pycbf_gb_adjoint_workspace_bytes",
-                            "pycbf_gb_batch_plan_bytes"):
+                            "pycbf_gb_batch_plan_bytes", "pycbf_gb_upsampled_bytes",
+                            "pycbf_gb_poly_workspace_bytes"):
                 getattr(L, name).restype = i
         _lib = L
         return L

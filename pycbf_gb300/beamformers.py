@@ -20,8 +20,11 @@ Differences, all deliberate:
   - interp kinds: 'cubic' (natural spline, the reference C path), 'nearest',
     'linear' (two-point interpolation; {'kind': 'linear', 'reference_floor':
     True} reproduces the reference CUDA linear_interp, which returns the floor
-    sample).  'korder_cubic', 'akima', 'makima' and nearest with usf > 1 raise
-    NotImplementedError;
+    sample).  nearest with usf > 1 upsamples each
+    channel by the cubic spline first (pycbf.c:223-253); 'korder_cubic'
+    (k-point derivative estimates; {'zero_slopes': True} reproduces the
+    reference's Synthetic korder kernel, whose k arrives as 0), 'akima' and
+    'makima' follow the reference's CUDA interpolators;
   - DMAS uses the values in ``lags`` (the reference kernel uses positions
     0..nlag-1; both agree when lags = arange(nlag)), takes nsep = ntx for
     lagaxis='tx', and handles 4-D input per frame;
@@ -36,12 +39,13 @@ from typing import ClassVar, Literal
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, helpers
 
 __all__ = ["BeamformerException", "Beamformer", "Tabbed", "Synthetic", "TabbedBeamformer",
            "SyntheticBeamformer", "TabbedDMASBeamformer", "SyntheticDMASBeamformer",
            "TabbedSLSCBeamformer", "SyntheticSLSCBeamformer", "DMASBeamformer"]
 
+_POLY = (_lib.INTERP["korder_cubic"], _lib.INTERP["akima"], _lib.INTERP["makima"])
 STORAGE = {"float32": (_lib.F32, torch.float32), "float16": (_lib.F16, torch.float16),
            "bfloat16": (_lib.BF16, torch.bfloat16)}
 
@@ -244,16 +248,23 @@ class _GPUBeamformer(Beamformer):
         if self.storage not in STORAGE:
             raise BeamformerException(f"storage must be one of {list(STORAGE)}")
         kind = self.interp["kind"]
-        if kind in ("korder_cubic", "akima", "makima"):
-            raise NotImplementedError(f"interp kind '{kind}' is not implemented by pycbf_gb300")
-        if kind == "nearest" and int(self.interp.get("usf", 1)) > 1:
-            raise NotImplementedError("nearest-neighbour upsampling (usf > 1) is not implemented")
+        self._usf = int(self.interp.get("usf", 1)) if kind == "nearest" else 1
         if kind == "linear" and self.interp.get("reference_floor", False):
             self._interp_code = _lib.INTERP["linear_floor"]
         else:
             self._interp_code = _lib.INTERP[kind]
         if not (int(self.nt) >= 1 and float(self.dt) > 0):
             raise BeamformerException("nt must be >= 1 and dt > 0")
+        self._k, self._S = 0, None
+        if kind == "korder_cubic":
+            k = int(self.interp["k"])
+            if k > 128 or k > int(self.nt):
+                raise BeamformerException("'k' for korder_cubic must be at most 128 and at most nt")
+            self._S = helpers.korder_matrix(k)
+            # zero_slopes: the reference Synthetic korder kernel, whose k arrives as 0
+            self._k = 0 if self.interp.get("zero_slopes", False) else k
+        if kind in ("akima", "makima") and int(self.nt) < 5:
+            raise BeamformerException(f"interp kind '{kind}' needs nt >= 5")
         self._dtype_code, self._torch_dtype = STORAGE[self.storage]
         self._workspace = None
 
@@ -313,6 +324,44 @@ class _GPUBeamformer(Beamformer):
         if self._workspace is None or self._workspace.numel() < need:
             self._workspace = torch.empty(need, dtype=torch.uint8, device="cuda")
         return self._workspace, need
+
+    def _usf_info(self, info):
+        """The rfinfo of the cubic-upsampled channel data (nearest, usf > 1):
+        usf*(nt-1)+1 samples at the float32 quotient dt/usf, float32."""
+        u = self._usf
+        return _lib.RFInfo(info.ntx, info.nrx, info.ndim, info.t0,
+                           float(np.float32(info.dt) / np.float32(u)), u * (info.nt - 1) + 1,
+                           info.nframes, _lib.F32)
+
+    def _prepare_channels(self, rf, info):
+        """(data, rfinfo, workspace, bytes) for the delay-and-sum call: for
+        nearest with usf > 1 the channels upsampled by the cubic spline
+        (pycbf.c:223-253), else the input and the interp's own workspace."""
+        if self._interp_code in _POLY:
+            need = self._lib.pycbf_gb_poly_workspace_bytes(ct.byref(info), self._interp_code,
+                                                           self._k)
+            if self._workspace is None or self._workspace.numel() < need:
+                self._workspace = torch.empty(need, dtype=torch.uint8, device="cuda")
+            S = self._S.ctypes.data_as(ct.c_void_p) if self._k > 0 else None
+            st = self._lib.pycbf_gb_poly_coefficients(ct.byref(info), _ptr(rf), self._interp_code,
+                                                      self._k, S, _ptr(self._workspace), need,
+                                                      _stream_ptr())
+            _lib.check(st, "pycbf_gb_poly_coefficients")
+            return self._workspace, info, None, 0
+        if self._usf <= 1:
+            ws, nws = self._workspace_for(info)
+            return rf, info, ws, nws
+        need = self._lib.pycbf_gb_workspace_bytes(ct.byref(info), _lib.INTERP["cubic"])
+        if self._workspace is None or self._workspace.numel() < need:
+            self._workspace = torch.empty(need, dtype=torch.uint8, device="cuda")
+        nbytes = self._lib.pycbf_gb_upsampled_bytes(ct.byref(info), self._usf)
+        up = getattr(self, "_upsampled", None)
+        if up is None or up.numel() * 4 < nbytes:
+            up = self._upsampled = torch.empty(nbytes // 4, dtype=torch.float32, device="cuda")
+        st = self._lib.pycbf_gb_upsample(ct.byref(info), _ptr(rf), self._usf, _ptr(self._workspace),
+                                         need, _ptr(up), nbytes, _stream_ptr())
+        _lib.check(st, "pycbf_gb_upsample")
+        return up, self._usf_info(info), None, 0
 
     def _output(self, shape, buffer):
         if buffer is None:
@@ -375,7 +424,8 @@ class TabbedBeamformer(Tabbed, _GPUBeamformer):
             self._pixel_index = perm.to(torch.int32).contiguous()
         self._tables = (tautx, apodtx, taurx, apodrx)
         self._plan = None
-        if self.stage_channels and self.ntx <= 12 and self._interp_code <= _lib.INTERP["cubic"]:
+        if (self.stage_channels and self.ntx <= 12 and self._interp_code <= _lib.INTERP["cubic"]
+                and self._usf == 1):
             nbytes = self._lib.pycbf_gb_tabbed_plan_bytes(self.nop, self.ntx, self.nrx)
             self._plan = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
             info = self._rfinfo(1)
@@ -387,7 +437,14 @@ class TabbedBeamformer(Tabbed, _GPUBeamformer):
 
     def _launch(self, rf, info, out, sumtype_code):
         tautx, apodtx, taurx, apodrx = self._tables
-        ws, nws = self._workspace_for(info)
+        rf, info, ws, nws = self._prepare_channels(rf, info)
+        if self._interp_code in _POLY:
+            st = self._lib.pycbf_gb_das_tabbed_poly(
+                ct.byref(info), _ptr(rf), self._interp_code, _ptr(tautx), _ptr(apodtx),
+                _ptr(taurx), _ptr(apodrx), self.nop, _ptr(self._pixel_index),
+                float(np.float32(self.thresh)), sumtype_code, _ptr(out), _stream_ptr())
+            _lib.check(st, "pycbf_gb_das_tabbed_poly")
+            return
         st = self._lib.pycbf_gb_das_tabbed(
             ct.byref(info), _ptr(rf), _ptr(tautx), _ptr(apodtx), _ptr(taurx), _ptr(apodrx),
             self.nop, _ptr(self._pixel_index), self._interp_code, float(np.float32(self.thresh)),
@@ -429,6 +486,8 @@ class TabbedBeamformer(Tabbed, _GPUBeamformer):
         """Per pixel (original order): contributing taps and the sum of their sample indices."""
         tautx, apodtx, taurx, apodrx = self._tables
         info = self._rfinfo(1)
+        if self._usf > 1:
+            info = self._usf_info(info)
         cnt = torch.empty(self.nop, dtype=torch.int32, device="cuda")
         isum = torch.empty(self.nop, dtype=torch.int64, device="cuda")
         st = self._lib.pycbf_gb_tap_census_tabbed(
@@ -494,7 +553,13 @@ class SyntheticBeamformer(Synthetic, _GPUBeamformer):
             np=self.nop, c0=float(np.float32(self.c0)))
 
     def _launch(self, rf, info, out, sumtype_code):
-        ws, nws = self._workspace_for(info)
+        rf, info, ws, nws = self._prepare_channels(rf, info)
+        if self._interp_code in _POLY:
+            st = self._lib.pycbf_gb_das_synthetic_poly(
+                ct.byref(info), _ptr(rf), self._interp_code, ct.byref(self._geom),
+                _ptr(self._pixel_index), sumtype_code, _ptr(out), _stream_ptr())
+            _lib.check(st, "pycbf_gb_das_synthetic_poly")
+            return
         st = self._lib.pycbf_gb_das_synthetic(
             ct.byref(info), _ptr(rf), ct.byref(self._geom), _ptr(self._pixel_index),
             self._interp_code, sumtype_code, _ptr(out), _ptr(ws), nws, _stream_ptr())
@@ -521,6 +586,8 @@ class SyntheticBeamformer(Synthetic, _GPUBeamformer):
 
     def tap_census(self):
         info = self._rfinfo(1, self.ndimp)
+        if self._usf > 1:
+            info = self._usf_info(info)
         cnt = torch.empty(self.nop, dtype=torch.int32, device="cuda")
         isum = torch.empty(self.nop, dtype=torch.int64, device="cuda")
         st = self._lib.pycbf_gb_tap_census_synthetic(ct.byref(info), ct.byref(self._geom),

@@ -67,6 +67,8 @@ void fill_time_axis(DasArgs &a, const pycbf_gb_rfinfo *rf) {
     volatile float span2 = rf->dt * (float)rf->nt;
     a.xend = rf->t0 + span2;
     a.eps = boundary_eps(rf->nt);
+    // the last knot as NVRTC compiles x0 + dx*(nx-1) in the reference's CUDA kernels
+    a.xfma = std::fmaf(rf->dt, (float)(rf->nt - 1), rf->t0);
 }
 
 bool das_shape_ok(int geom, int sumtype, long long ntx) {
@@ -122,6 +124,14 @@ int prepare_data(const pycbf_gb_rfinfo *rf, const void *rfdata, int interp, void
     if (st) return st;
     *data = workspace;
     return PYCBF_GB_OK;
+}
+
+// the kernels' interpolation kind of an interp code (akima and makima share
+// their gather: they differ only in the prefilter)
+int gather_kind(int interp) {
+    if (interp == PYCBF_GB_INTERP_KORDER) return KIND_POLY_NORM;
+    if (interp == PYCBF_GB_INTERP_AKIMA || interp == PYCBF_GB_INTERP_MAKIMA) return KIND_POLY_DELTA;
+    return interp;
 }
 
 bool geo_ok(const pycbf_gb_synthetic *g) {
@@ -207,6 +217,8 @@ int pycbf_gb_das_tabbed(const pycbf_gb_rfinfo *rf, const void *rfdata, const flo
     if (st) return st;
     if (!rfdata || !tautx || !apodtx || !taurx || !apodrx || !out) return PYCBF_GB_EINVAL;
     if (np <= 0 || np >= (1LL << 31)) return np == 0 ? PYCBF_GB_OK : PYCBF_GB_ERANGE;
+    if (interp >= PYCBF_GB_INTERP_KORDER && interp <= PYCBF_GB_INTERP_MAKIMA)
+        return PYCBF_GB_EUNSUPPORTED;  // pycbf_gb_das_tabbed_poly
     if (interp < 0 || interp > 3 || sumtype < 0 || sumtype > 5) return PYCBF_GB_EINVAL;
     if (std::isnan(thresh)) return PYCBF_GB_EINVAL;
     if (!das_shape_ok(GEOM_TABBED, sumtype, rf->ntx)) return PYCBF_GB_ERANGE;
@@ -262,6 +274,8 @@ int pycbf_gb_das_synthetic(const pycbf_gb_rfinfo *rf, const void *rfdata,
     int st = check_rf(rf, true);
     if (st) return st;
     if (!rfdata || !out || !geo_ok(geo)) return PYCBF_GB_EINVAL;
+    if (interp >= PYCBF_GB_INTERP_KORDER && interp <= PYCBF_GB_INTERP_MAKIMA)
+        return PYCBF_GB_EUNSUPPORTED;  // pycbf_gb_das_synthetic_poly
     if (interp < 0 || interp > 3 || sumtype < 0 || sumtype > 5) return PYCBF_GB_EINVAL;
     if (!das_shape_ok(GEOM_SYNTH, sumtype, rf->ntx)) return PYCBF_GB_ERANGE;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -288,8 +302,9 @@ int pycbf_gb_tap_census_tabbed(const pycbf_gb_rfinfo *rf, const float *tautx,
     if (st) return st;
     if (!tautx || !apodtx || !taurx || !apodrx || !count || !index_sum) return PYCBF_GB_EINVAL;
     if (np <= 0 || np >= (1LL << 31)) return np == 0 ? PYCBF_GB_OK : PYCBF_GB_ERANGE;
-    if (interp < 0 || interp > 3 || std::isnan(thresh)) return PYCBF_GB_EINVAL;
+    if (interp < 0 || interp > 6 || std::isnan(thresh)) return PYCBF_GB_EINVAL;
     if (!das_shape_ok(GEOM_TABBED, PYCBF_GB_SUM_TX_AND_RX, rf->ntx)) return PYCBF_GB_ERANGE;
+    interp = gather_kind(interp);
     DasArgs a = {};
     fill_time_axis(a, rf);
     a.nframes = 1;
@@ -310,7 +325,8 @@ int pycbf_gb_tap_census_synthetic(const pycbf_gb_rfinfo *rf, const pycbf_gb_synt
     int st = check_rf(rf, true);
     if (st) return st;
     if (!geo_ok(geo) || !count || !index_sum) return PYCBF_GB_EINVAL;
-    if (interp < 0 || interp > 3) return PYCBF_GB_EINVAL;
+    if (interp < 0 || interp > 6) return PYCBF_GB_EINVAL;
+    interp = gather_kind(interp);
     if (!das_shape_ok(GEOM_SYNTH, PYCBF_GB_SUM_TX_AND_RX, rf->ntx)) return PYCBF_GB_ERANGE;
     DasArgs a = {};
     fill_time_axis(a, rf);
@@ -621,6 +637,149 @@ int pycbf_gb_batch_run(const void *plan, const pycbf_gb_batch_info *info, int tx
     if (st) return st;
     return cuda_status(launch_batch_das(jobs, items, info->nitems, info->tiles_per_item, counter,
                                         tx_chunk, ctas, s));
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// cubic upsampling for nearest with usf > 1
+// ---------------------------------------------------------------------------
+extern "C" {
+
+size_t pycbf_gb_upsampled_bytes(const pycbf_gb_rfinfo *rf, int usf) {
+    if (!rf || usf < 1 || rf->ntx <= 0 || rf->nrx <= 0 || rf->nt <= 0 || rf->nframes <= 0) return 0;
+    const long long ntu = (long long)usf * (rf->nt - 1) + 1;
+    return sizeof(float) * (size_t)rf->nframes * (size_t)rf->ntx * (size_t)rf->nrx * (size_t)ntu;
+}
+
+int pycbf_gb_upsample(const pycbf_gb_rfinfo *rf, const void *rfdata, int usf, void *workspace,
+                      size_t workspace_bytes, float *out, size_t out_bytes, void *stream) {
+    int st = check_rf(rf, false);
+    if (st) return st;
+    if (!rfdata || !out || usf < 1) return PYCBF_GB_EINVAL;
+    const long long ntu = (long long)usf * (rf->nt - 1) + 1;
+    if (ntu >= kMaxNt) return PYCBF_GB_ERANGE;
+    if (out_bytes < pycbf_gb_upsampled_bytes(rf, usf)) return PYCBF_GB_EWORKSPACE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const void *data = nullptr;
+    st = prepare_data(rf, rfdata, PYCBF_GB_INTERP_CUBIC, workspace, workspace_bytes, s, &data);
+    if (st) return st;
+    DasArgs a = {};
+    fill_time_axis(a, rf);
+    a.data = data;
+    const float dtu = rf->dt / (float)usf;
+    return cuda_status(launch_upsample(a, rf->dtype, out, rf->nframes * rf->ntx * rf->nrx, (int)ntu,
+                                       dtu, s));
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// korder / akima / makima
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kMaxKorder = 128;
+
+bool poly_kind(int interp) {
+    return interp == PYCBF_GB_INTERP_KORDER || interp == PYCBF_GB_INTERP_AKIMA ||
+           interp == PYCBF_GB_INTERP_MAKIMA;
+}
+
+size_t poly_record_bytes(const pycbf_gb_rfinfo *rf) {
+    return (size_t)rf->nframes * (size_t)rf->ntx * (size_t)rf->nrx * (size_t)rf->nt * 16;
+}
+
+int poly_args(const pycbf_gb_rfinfo *rf, const void *coef, int interp, int sumtype, bool synth,
+              DasArgs &a) {
+    int st = check_rf(rf, synth);
+    if (st) return st;
+    if (!poly_kind(interp) || !coef || reinterpret_cast<uintptr_t>(coef) % 16) return PYCBF_GB_EINVAL;
+    if (sumtype < 0 || sumtype > 5) return PYCBF_GB_EINVAL;
+    if (!das_shape_ok(synth ? GEOM_SYNTH : GEOM_TABBED, sumtype, rf->ntx)) return PYCBF_GB_ERANGE;
+    a = DasArgs{};
+    fill_time_axis(a, rf);
+    a.data = coef;
+    return PYCBF_GB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t pycbf_gb_poly_workspace_bytes(const pycbf_gb_rfinfo *rf, int interp, int k) {
+    if (!rf || !poly_kind(interp) || rf->ntx <= 0 || rf->nrx <= 0 || rf->nt <= 0 ||
+        rf->nframes <= 0 || k < 0 || k > kMaxKorder)
+        return 0;
+    const size_t sbytes =
+        interp == PYCBF_GB_INTERP_KORDER ? ((sizeof(float) * (size_t)k * k + 15) & ~(size_t)15) : 0;
+    return poly_record_bytes(rf) + sbytes;
+}
+
+int pycbf_gb_poly_coefficients(const pycbf_gb_rfinfo *rf, const void *rfdata, int interp, int k,
+                               const float *S, void *coef, size_t coef_bytes, void *stream) {
+    int st = check_rf(rf, false);
+    if (st) return st;
+    if (!rfdata || !coef || !poly_kind(interp) || reinterpret_cast<uintptr_t>(coef) % 16)
+        return PYCBF_GB_EINVAL;
+    if (interp == PYCBF_GB_INTERP_KORDER) {
+        if (k < 0 || k > kMaxKorder || (k % 2) || k > rf->nt || (k > 0 && !S)) return PYCBF_GB_EINVAL;
+        if (rf->nt < 2) return PYCBF_GB_ERANGE;
+    } else {
+        k = 0;
+        if (rf->nt < 5) return PYCBF_GB_ERANGE;
+    }
+    if (coef_bytes < pycbf_gb_poly_workspace_bytes(rf, interp, k)) return PYCBF_GB_EWORKSPACE;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    float *dS = nullptr;
+    if (interp == PYCBF_GB_INTERP_KORDER && k > 0) {
+        dS = reinterpret_cast<float *>(static_cast<char *>(coef) + poly_record_bytes(rf));
+        st = cuda_status(cudaMemcpyAsync(dS, S, sizeof(float) * k * k, cudaMemcpyHostToDevice, s));
+        if (st) return st;
+    }
+    DasArgs a = {};
+    fill_time_axis(a, rf);
+    return cuda_status(launch_poly_records(a, rfdata, rf->dtype, interp, k, dS,
+                                           static_cast<float4 *>(coef),
+                                           rf->nframes * rf->ntx * rf->nrx, s));
+}
+
+int pycbf_gb_das_tabbed_poly(const pycbf_gb_rfinfo *rf, const void *coef, int interp,
+                             const float *tautx, const float *apodtx, const float *taurx,
+                             const float *apodrx, long long np, const int *pixel_index,
+                             float thresh, int sumtype, float *out, void *stream) {
+    DasArgs a;
+    int st = poly_args(rf, coef, interp, sumtype, false, a);
+    if (st) return st;
+    if (!tautx || !apodtx || !taurx || !apodrx || !out || std::isnan(thresh)) return PYCBF_GB_EINVAL;
+    if (np <= 0 || np >= (1LL << 31)) return np == 0 ? PYCBF_GB_OK : PYCBF_GB_ERANGE;
+    a.tautx = tautx;
+    a.apodtx = apodtx;
+    a.taurx = taurx;
+    a.apodrx = apodrx;
+    a.pixel_index = pixel_index;
+    a.out = out;
+    a.np = np;
+    a.thresh = thresh;
+    return cuda_status(launch_das(a, GEOM_TABBED, gather_kind(interp), sumtype, PYCBF_GB_F32, false,
+                                  static_cast<cudaStream_t>(stream)));
+}
+
+int pycbf_gb_das_synthetic_poly(const pycbf_gb_rfinfo *rf, const void *coef, int interp,
+                                const pycbf_gb_synthetic *geo, const int *pixel_index,
+                                int sumtype, float *out, void *stream) {
+    DasArgs a;
+    int st = poly_args(rf, coef, interp, sumtype, true, a);
+    if (st) return st;
+    if (!geo_ok(geo) || !out) return PYCBF_GB_EINVAL;
+    a.geo = *geo;
+    a.ndim = rf->ndim;
+    a.pixel_index = pixel_index;
+    a.out = out;
+    a.np = geo->np;
+    a.thresh = 0.01f;
+    return cuda_status(launch_das(a, GEOM_SYNTH, gather_kind(interp), sumtype, PYCBF_GB_F32, false,
+                                  static_cast<cudaStream_t>(stream)));
 }
 
 }  // extern "C"

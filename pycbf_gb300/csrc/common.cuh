@@ -120,7 +120,14 @@ struct DasArgs {
     int ntx, nrx, nt, ndim, nframes;
     float t0, dt, inv_dt, xmax, xend, thresh, eps;
     const float *slow;  // GEOM_SYNTH_SLOW: slowness per pixel (s/m), kernel pixel order
+    float xfma;         // fma(dt, nt-1, t0): the last knot as the reference's CUDA kernels round it
 };
+
+// gather kinds of the polynomial-record interpolators (records from poly.cu)
+constexpr int KIND_POLY_NORM = 4;   // korder: a0 + a1 u + a2 u^2 + a3 u^3, u in [0, 1)
+constexpr int KIND_POLY_DELTA = 5;  // akima / makima: a + b d + c d^2 + d d^3, d in seconds
+cudaError_t launch_poly_records(const DasArgs &a, const void *rf, int dtype, int interp, int k,
+                                const float *S, float4 *rec, long long nch, cudaStream_t s);
 cudaError_t launch_das(const DasArgs &a, int geom, int interp, int sumtype, int dtype, bool census,
                        cudaStream_t s);
 cudaError_t launch_synth_rx_mask(const DasArgs &a, unsigned char *mask, cudaStream_t s);
@@ -129,6 +136,11 @@ long long tabbed_plan_words(long long np, int ntx, int nrx);
 cudaError_t launch_tabbed_plan(const DasArgs &a, int interp, int dtype, int *plan, cudaStream_t s);
 cudaError_t launch_das_staged(const DasArgs &a, int interp, int sumtype, int dtype, const int *plan,
                               int *status, cudaStream_t s);
+
+// cubic upsampling for nearest with usf > 1: out (nch, ntu) float32 from the
+// spline records in a.data (time axis of the original channel data in a)
+cudaError_t launch_upsample(const DasArgs &a, int dtype, float *out, long long nch, int ntu,
+                            float dtu, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // uneven batches: one frame of one beamformer per job, all in one launch

@@ -21,6 +21,8 @@
 //   IEEE division is taken instead.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace pgb {
@@ -163,6 +165,52 @@ template <typename T> struct Kind<PYCBF_GB_INTERP_LINEAR_FLOOR, T> {
         return __fadd_rn(__fmul_rn(v, __fsub_rn(1.0f, frac)), __fmul_rn(v, frac));
     }
 };
+
+// ---------------------------------------------------------------------------
+// korder / akima / makima: one float32 record of cubic coefficients per
+// interval (poly.cu), whatever the storage type.  Knot ixo = (int)((x-t0)/dt)
+// with the correctly rounded quotient; korder fills outside [t0, xfma] or
+// past the last knot, akima/makima outside [t0, xfma] and take the last knot
+// at x == xfma (__engines__.cu:181-187, 266-269, 318-322).
+// ---------------------------------------------------------------------------
+template <int KIND, typename T> struct KindPoly {
+    using P = float4;
+    static __device__ __forceinline__ bool index(float x, const DasArgs &a, int &idx, bool &fix) {
+        const float q = __fmul_rn(__fsub_rn(x, a.t0), a.inv_dt);
+        const float fl = floorf(q);
+        const float f = q - fl;
+        fix = (f < a.eps) || (f > 1.f - a.eps);
+        return finish(x, fl, a, idx);
+    }
+    static __device__ __forceinline__ bool index_exact(float x, const DasArgs &a, int &idx) {
+        return finish(x, floorf(__fdiv_rn(__fsub_rn(x, a.t0), a.dt)), a, idx);
+    }
+    static __device__ __forceinline__ bool finish(float x, float fl, const DasArgs &a, int &idx) {
+        const float last = (float)(a.nt - 1);
+        bool inr = (x >= a.t0) && (x <= a.xfma);
+        if (KIND == KIND_POLY_NORM) inr = inr && (fl <= last);
+        float j = fminf(fl, last);
+        if (KIND == KIND_POLY_DELTA && x == a.xfma) j = last;
+        idx = inr ? (int)j : 0;
+        return inr;
+    }
+    static __device__ __forceinline__ P load(const void *data, long long ch, int idx,
+                                            const DasArgs &) {
+        return __ldg(static_cast<const float4 *>(data) + ch + idx);
+    }
+    static __device__ __forceinline__ float value(const P &c, float x, float fj, const DasArgs &a) {
+        float u;
+        if (KIND == KIND_POLY_NORM)
+            u = __fdiv_rn(fmaf(-a.dt, fj, __fsub_rn(x, a.t0)), a.dt);
+        else
+            u = __fsub_rn(x, fmaf(a.dt, fj, a.t0));
+        const float s1 = __fadd_rn(c.x, __fmul_rn(c.y, u));
+        const float s2 = __fadd_rn(s1, __fmul_rn(__fmul_rn(c.z, u), u));
+        return __fadd_rn(s2, __fmul_rn(__fmul_rn(__fmul_rn(c.w, u), u), u));
+    }
+};
+template <typename T> struct Kind<KIND_POLY_NORM, T> : KindPoly<KIND_POLY_NORM, T> {};
+template <typename T> struct Kind<KIND_POLY_DELTA, T> : KindPoly<KIND_POLY_DELTA, T> {};
 
 // ---------------------------------------------------------------------------
 // synthetic-point delays (__engines__.cu:382-470, acos tests as cos compares).
@@ -523,6 +571,12 @@ cudaError_t launch_das_sum(const DasArgs &a, int sum, cudaStream_t s) {
 template <int GEOM, typename T>
 cudaError_t launch_das_geom_type(const DasArgs &a, int interp, int sum, bool census, cudaStream_t s) {
     if (census) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (interp == KIND_POLY_NORM)
+                return launch_das_one<GEOM, KIND_POLY_NORM, PYCBF_GB_SUM_TX_AND_RX, T, true>(a, s);
+            if (interp == KIND_POLY_DELTA)
+                return launch_das_one<GEOM, KIND_POLY_DELTA, PYCBF_GB_SUM_TX_AND_RX, T, true>(a, s);
+        }
         switch (interp) {
             case PYCBF_GB_INTERP_CUBIC: return launch_das_one<GEOM, PYCBF_GB_INTERP_CUBIC, PYCBF_GB_SUM_TX_AND_RX, T, true>(a, s);
             case PYCBF_GB_INTERP_LINEAR: return launch_das_one<GEOM, PYCBF_GB_INTERP_LINEAR, PYCBF_GB_SUM_TX_AND_RX, T, true>(a, s);
@@ -530,6 +584,10 @@ cudaError_t launch_das_geom_type(const DasArgs &a, int interp, int sum, bool cen
             case PYCBF_GB_INTERP_LINEAR_FLOOR: return launch_das_one<GEOM, PYCBF_GB_INTERP_LINEAR_FLOOR, PYCBF_GB_SUM_TX_AND_RX, T, true>(a, s);
             default: return cudaErrorInvalidValue;
         }
+    }
+    if constexpr (std::is_same<T, float>::value) {  // polynomial records are float32 always
+        if (interp == KIND_POLY_NORM) return launch_das_sum<GEOM, KIND_POLY_NORM, T>(a, sum, s);
+        if (interp == KIND_POLY_DELTA) return launch_das_sum<GEOM, KIND_POLY_DELTA, T>(a, sum, s);
     }
     switch (interp) {
         case PYCBF_GB_INTERP_CUBIC: return launch_das_sum<GEOM, PYCBF_GB_INTERP_CUBIC, T>(a, sum, s);

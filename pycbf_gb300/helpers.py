@@ -96,3 +96,23 @@ def pw_synthetic_planewaves(steers, xele, fnum):
     alarx = np.arctan2(0.5, fnum) * np.ones(nrx)
     return dict(ovectx=orig, nvectx=nvectx, t0tx=z, doftx=z.copy(), alatx=z.copy(),
                 ovecrx=ovecrx, nvecrx=nvecrx, alarx=alarx)
+
+
+def korder_matrix(k: int) -> np.ndarray:
+    """S = C^-1 P of k-point cubic interpolation (the published method of
+    Praesius and Jensen, 2024), as pycbf/gpu/__core_bf_classes__.py:366-395
+    builds it: C tridiagonal with 4 inside and 1 at the ends (2 beside them),
+    P the matching difference operator.  float64 inverse, float32 result."""
+    c00 = np.ones(k)
+    c00[1:-1] = 4.0
+    cp1 = np.ones(k - 1)
+    cp1[0] = 2.0
+    C = np.diag(c00) + np.diag(cp1, 1) + np.diag(cp1[::-1], -1)
+    pp1 = 3.0 * np.ones(k - 1)
+    pp1[0] = 2.0
+    P = np.diag(pp1, 1) + np.diag(-pp1[::-1], -1)
+    P[0, 0] = -2.5
+    P[-1, -1] = 2.5
+    P[0, 2] = 0.5
+    P[-1, -3] = -0.5
+    return np.ascontiguousarray(np.linalg.inv(C) @ P, dtype=np.float32)

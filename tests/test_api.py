@@ -34,14 +34,18 @@ def test_bad_sumtype_and_interp():
         pg.TabbedBeamformer(**tabs(), **T, interp={"kind": "nearest", "usf": 0})
 
 
-def test_unimplemented_kinds_raise():
-    for kind in ("akima", "makima"):
-        with pytest.raises(NotImplementedError):
-            pg.TabbedBeamformer(**tabs(), **T, interp={"kind": kind})
-    with pytest.raises(NotImplementedError):
-        pg.TabbedBeamformer(**tabs(), **T, interp={"kind": "korder_cubic", "k": 8})
-    with pytest.raises(NotImplementedError):
-        pg.TabbedBeamformer(**tabs(), **T, interp={"kind": "nearest", "usf": 4})
+def test_korder_matrix_matches_the_oracle_restatement():
+    from oracle import oracle
+    from pycbf_gb300 import helpers
+    for k in (4, 8, 16, 126):
+        np.testing.assert_array_equal(helpers.korder_matrix(k), oracle.korder_S(k))
+
+
+def test_poly_kind_limits():
+    with pytest.raises(pg.BeamformerException):
+        pg.TabbedBeamformer(**tabs(), **T, interp={"kind": "korder_cubic", "k": 130})
+    with pytest.raises(pg.BeamformerException):
+        pg.TabbedBeamformer(**tabs(), t0=0.0, dt=1e-8, nt=4, interp={"kind": "akima"})
 
 
 def test_tabbed_shape_checks():

@@ -59,6 +59,34 @@ def test_synthetic_das_vs_oracle(c2_small, kind):
     np.testing.assert_array_equal(isum.cpu().numpy(), ok_isum)
 
 
+def test_synthetic_nearest_upsampled_vs_oracle(c2_small):
+    w = c2_small
+    tables = oracle_tables(w)
+    bf = synth_bf(w, interp={"kind": "nearest", "usf": 3})
+    out = bf(w.rf)
+    tt, at, tr, ar = tables
+    ref = oracle.das_tabbed(w.rf, tt, at, tr, ar, w.t0, w.dt, w.nt, interp="nearest", usf=3,
+                            thresh=0.01, threads=NCPU)
+    r, m = assert_image_close(out, ref, what="usf 3")
+    report("synthetic_c2small_nearest_usf3", rel_l2=r, max_abs_peak=m)
+    cnt, isum = bf.tap_census()
+    ok_cnt, ok_isum = oracle.tap_census(*tables, w.t0, w.dt, w.nt, interp="nearest", usf=3,
+                                        thresh=0.01)
+    np.testing.assert_array_equal(cnt.cpu().numpy(), ok_cnt)
+    np.testing.assert_array_equal(isum.cpu().numpy(), ok_isum)
+
+
+@pytest.mark.parametrize("interp", [dict(kind="korder_cubic", k=8), dict(kind="makima")])
+def test_synthetic_gpu_only_interpolators_vs_oracle(c2_small, interp):
+    w = c2_small
+    tt, at, tr, ar = oracle_tables(w)
+    out = synth_bf(w, interp=interp)(w.rf)
+    ref = oracle.das_poly(w.rf, tt, at, tr, ar, w.t0, w.dt, w.nt, interp["kind"],
+                          k=interp.get("k", 8), thresh=0.01)
+    r, m = assert_image_close(out, ref, what=str(interp))
+    report(f"synthetic_c2small_{interp['kind']}", rel_l2=r, max_abs_peak=m)
+
+
 @pytest.mark.parametrize("sumtype", ["tx_only", "rx_only", "none"])
 def test_synthetic_sumtypes(c2_small, sumtype):
     w = c2_small

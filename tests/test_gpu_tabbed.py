@@ -255,3 +255,66 @@ def test_staged_kernel_unstaged_receives():
     ref = oracle.das_tabbed(frames[2], case["tautx"], case["apodtx"], case["taurx"],
                             case["apodrx"], 0.0, float(dt), nt)
     assert_image_close(bf_for(case, "cubic")(frames)[2], ref, what="unstaged")
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_nearest_usf4_vs_reference_golden(golden, name):
+    """Nearest with the cubic 4x upsampling of beamform_nearest (pycbf.c:223-253):
+    the reference's own compiled output, and the tap set of the oracle."""
+    case = golden(f"tabbed_{name}.npz")
+    bf = bf_for(case, dict(kind="nearest", usf=4))
+    out = bf(case["rf"])
+    assert_image_close(out, case["ref_nearest_usf4_tx_and_rx"], what=name)
+    cnt, isum = bf.tap_census()
+    ok_cnt, ok_isum = oracle.tap_census(case["tautx"], case["apodtx"], case["taurx"], case["apodrx"],
+                                        float(case["t0"]), float(case["dt"]), int(case["nt"]),
+                                        interp="nearest", usf=4)
+    np.testing.assert_array_equal(cnt.cpu().numpy(), ok_cnt)
+    np.testing.assert_array_equal(isum.cpu().numpy(), ok_isum)
+
+
+@pytest.mark.parametrize("usf", [2, 5])
+def test_nearest_upsampled_vs_oracle(c1_small, usf):
+    out = bf_for(c1_small, dict(kind="nearest", usf=usf))(c1_small["rf"])
+    ref = oracle.das_tabbed(c1_small["rf"], c1_small["tautx"], c1_small["apodtx"], c1_small["taurx"],
+                            c1_small["apodrx"], c1_small["t0"], c1_small["dt"], c1_small["nt"],
+                            interp="nearest", usf=usf, threads=NCPU)
+    r, m = assert_image_close(out, ref, what=f"usf {usf}")
+    report(f"tabbed_nearest_usf{usf}", rel_l2=r, max_abs_peak=m)
+
+
+@pytest.mark.parametrize("interp", [dict(kind="korder_cubic", k=8), dict(kind="korder_cubic", k=16),
+                                    dict(kind="korder_cubic", k=8, zero_slopes=True),
+                                    dict(kind="akima"), dict(kind="makima")])
+def test_gpu_only_interpolators_vs_oracle(c1_small, interp):
+    """korder / akima / makima (the reference's CUDA interpolators, restated in
+    the oracle from __engines__.cu:58-355): tap set bit-exact, image within
+    the float32 bar."""
+    c = c1_small
+    bf = bf_for(c, interp)
+    out = bf(c["rf"])
+    kind = interp["kind"]
+    k = 0 if interp.get("zero_slopes") else interp.get("k", 8)
+    ref = oracle.das_poly(c["rf"], c["tautx"], c["apodtx"], c["taurx"], c["apodrx"], c["t0"],
+                          c["dt"], c["nt"], kind, k=k)
+    r, m = assert_image_close(out, ref, what=str(interp))
+    report(f"tabbed_{kind}_k{k}", rel_l2=r, max_abs_peak=m)
+    cnt, isum = bf.tap_census()
+    ok_cnt, ok_isum = oracle.tap_census(c["tautx"], c["apodtx"], c["taurx"], c["apodrx"], c["t0"],
+                                        c["dt"], c["nt"], interp=kind)
+    np.testing.assert_array_equal(cnt.cpu().numpy(), ok_cnt)
+    np.testing.assert_array_equal(isum.cpu().numpy(), ok_isum)
+
+
+def test_korder_large_k_and_edges(golden):
+    """k = 126 (the reference notebook's setting) on the short golden channels,
+    whose taps reach both ends of the record."""
+    for name in ("edge", "short3"):
+        case = golden(f"tabbed_{name}.npz")
+        nt = int(case["nt"])
+        k = min(126, nt - nt % 2)
+        out = bf_for(case, dict(kind="korder_cubic", k=k))(case["rf"])
+        ref = oracle.das_poly(case["rf"], case["tautx"], case["apodtx"], case["taurx"],
+                              case["apodrx"], float(case["t0"]), float(case["dt"]), nt,
+                              "korder_cubic", k=k)
+        assert_image_close(out, ref, what=f"{name} k={k}")
