@@ -427,9 +427,9 @@ def das_poly(rf, tautx, apodtx, taurx, apodrx, t0, dt, nt, interp, k=8, S=None, 
     tautx, apodtx, taurx, apodrx = map(_c32, (tautx, apodtx, taurx, apodrx))
     ntx, nrx, np_ = tautx.shape[0], taurx.shape[0], tautx.shape[1]
     code = POLY_CODES[interp]
-    if code == 4:
+    if code == 4 and k > 0:
         S = korder_S(k) if S is None else _c32(S)
-    else:
+    else:  # akima / makima, or korder with k = 0 (zero derivative estimates)
         S, k = np.zeros((1, 1), np.float32), 0
     out = np.zeros(out_size(sumtype, ntx, nrx, np_), dtype=np.float32)
     lib().orc_das_poly(code, int(k), _ptr(S), float(t0), float(dt), int(nt), _ptr(rf), ntx, nrx,

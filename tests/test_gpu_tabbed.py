@@ -307,9 +307,9 @@ def test_gpu_only_interpolators_vs_oracle(c1_small, interp):
 
 
 def test_korder_large_k_and_edges(golden):
-    """k = 126 (the reference notebook's setting) on the short golden channels,
+    """k = 126 (the reference notebook's setting) and k = nt on golden cases
     whose taps reach both ends of the record."""
-    for name in ("edge", "short3"):
+    for name in ("edge", "pw_small"):
         case = golden(f"tabbed_{name}.npz")
         nt = int(case["nt"])
         k = min(126, nt - nt % 2)
