@@ -380,6 +380,67 @@ def run_variants(a, w, dev, taps):
                      "storage": storage, "interp": kind}
     res.update(run_adjoint_variants(a, w, dev, taps))
     res.update(run_batch_variants(a, dev))
+    res.update(run_synthetic_variants(a, dev))
+    return res
+
+
+def _synthetic(cls, w, **kw):
+    g = w.geometry
+    keys = ("ovectx", "nvectx", "doftx", "alatx", "t0tx", "ovecrx", "nvecrx", "alarx", "c0", "pnts")
+    return cls(**{k: g[k] for k in keys}, t0=w.t0, dt=w.dt, nt=w.nt, **kw)
+
+
+def run_synthetic_variants(a, dev):
+    """Synthetic-point workloads with delays computed on the fly.
+
+    c2_*: 192 elements at 0.2 mm, 75 plane waves over -18..18 deg (far
+    virtual sources), fs 31.25 MHz, Nt 4096, 40 000 speckle + 30 points,
+    512 x 1024 pixels: DAS, DMAS (signed square root over all receive
+    pairs, fused) and SLSC (lags 1..16, axial kernel 7 pixels = 1 wavelength).
+    c5_3d_fp16: 32 x 32 matrix, 25 diverging waves, Nt 2048, float16 channel
+    data, 128 x 128 x 256 voxels, 8 frames per call (2 000 speckle + 50
+    points: the content does not change the work)."""
+    import numpy as np
+    import torch
+
+    import pycbf_gb300 as pg
+    from pycbf_gb300 import phantom
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    res = {}
+    w = phantom.linear_pw_synthetic(device=dev)
+    rf = torch.as_tensor(w.rf, device=dev)
+    nx, nz = w.grid
+    cub = {"kind": "cubic"}
+    nrx = w.geometry["ovecrx"].shape[0]
+    cases = {
+        "c2_das": _synthetic(pg.SyntheticBeamformer, w, interp=cub, sumtype="tx_and_rx"),
+        "c2_dmas": _synthetic(pg.SyntheticDMASBeamformer, w, interp=cub,
+                              lags=np.arange(1, nrx), lagaxis="rx", sumlags=True, dmastype="ssr"),
+        "c2_slsc": _synthetic(pg.SyntheticSLSCBeamformer, w, interp=cub, grid_shape=(nx, nz),
+                              nlag=16, nkern=3),
+    }
+    for name, bf in cases.items():
+        call = lambda: bf(rf, out_as_numpy=False)
+        call()
+        t = _event_time(call, 3, flush, stream)
+        taps = bf.ntx * bf.nrx * bf.nop
+        res[name] = {"value": taps / t, "unit": UNIT, "ms_per_call": 1e3 * t, "taps": taps,
+                     "workload": "synthetic 192el 75pw 4096s 512x1024", "interp": "cubic"}
+        del bf
+    del rf, w, cases
+    torch.cuda.empty_cache()
+    w = phantom.matrix_dw_synthetic(n_speckle=2000, device=dev)
+    bf = _synthetic(pg.SyntheticBeamformer, w, interp=cub, sumtype="tx_and_rx", storage="float16")
+    frames = torch.as_tensor(w.rf, device=dev).to(torch.float16)
+    frames = torch.stack([frames * (1.0 + 0.1 * k) for k in range(8)]).contiguous()
+    call = lambda: bf(frames, out_as_numpy=False)
+    call()
+    t = _event_time(call, 2, flush, stream)
+    taps = 8 * bf.ntx * bf.nrx * bf.nop
+    res["c5_3d_fp16"] = {"value": taps / t, "unit": UNIT, "ms_per_call": 1e3 * t,
+                         "frames_per_call": 8, "taps": taps, "storage": "float16",
+                         "workload": "synthetic 3-D 32x32 matrix 25dw 2048s 128x128x256"}
     return res
 
 

@@ -18,7 +18,7 @@ cudaError_t launch_staged_bf16(const DasArgs &, int, int, const int *, int *, cu
 
 long long tabbed_plan_words(long long np, int ntx, int nrx) {
     const long long tiles = (np + kBlock - 1) / kBlock;
-    return kPlanHeaderWords + tiles * plan_tile_words(ntx, nrx);
+    return kPlanHeaderWords + tiles * plan_tile_words(ntx, nrx) + tiles;
 }
 
 cudaError_t launch_tabbed_plan(const DasArgs &a, int interp, int dtype, int *plan, cudaStream_t s) {

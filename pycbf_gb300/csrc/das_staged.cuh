@@ -19,6 +19,8 @@
 // flight and returns.
 #pragma once
 
+#include <algorithm>
+
 #include "das_impl.cuh"
 
 namespace pgb {
@@ -27,10 +29,11 @@ constexpr int kStages = 4;
 constexpr int kStageBytes = 12 * 1024;
 constexpr unsigned kWaitLimit = 1u << 30;  // polls; the ~1 s clock bound ends a wait first
 
-// plan layout (int32 words): [0] status, [1] reserved, [2..3] pad, then per
-// tile a record of plan_tile_words(ntx, nrx) words:
+// plan layout (int32 words): [0] status, [1] work-queue head of the staged
+// kernel, [2..3] pad, then per tile a record of plan_tile_words(ntx, nrx) words:
 //   nlive | rx index per live receive (nrx) | rx lo,hi per live receive (2*nrx floats)
 //   | tx lo,hi per transmit (2*ntx floats)
+// and last the tile order (one int per tile, most live receives first).
 __host__ __device__ inline long long plan_tile_words(int ntx, int nrx) {
     return 1 + (long long)nrx + 2LL * nrx + 2LL * ntx;
 }
@@ -327,10 +330,16 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt,
     return accr;
 }
 
+// Persistent: a grid sized to the GPU takes (frame, tile) items from the
+// plan's queue head (plan[1], zeroed before the launch) in the plan's order,
+// the tiles with most live receives first, so the slowest tiles start first
+// and the last wave is short.  The ring's barriers live across tiles: item
+// number g (counted over all tiles this CTA has run) uses slot g % kStages and
+// phase parity (g / kStages) & 1.  Each tile is computed entirely by one CTA,
+// so the results do not depend on the scheduling.
 template <int KIND, int SUM, typename T>
 __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_constant__ DasArgs a,
-                                                              const int *__restrict__ plan,
-                                                              int *status) {
+                                                              int *__restrict__ plan) {
     using E = typename StagedElem<KIND, T>::E;
     constexpr int kWarps = kBlock / 32;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -340,204 +349,254 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     __shared__ int sstaged[kStages];
     __shared__ float s_txlh[2 * kTxReg];
     __shared__ int s_failed;
-    __shared__ int s_produced;  // receives whose copies have been issued
+    __shared__ long long s_produced;  // items (over all tiles) whose copies have been issued
+    __shared__ long long s_item;
     // the tile's plan: live receive indices and their delay bounds
     int *s_rx = reinterpret_cast<int *>(smem_raw + kStages * kStageBytes);
     float *s_rxlh = reinterpret_cast<float *>(s_rx + a.nrx);
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const long long tile = blockIdx.x;
-    const long long i = tile * kBlock + tid;
-    const bool valid = i < a.np;
-    const int f = blockIdx.y;
     const int ntx = a.ntx, nrx = a.nrx;
     const long long np = a.np;
-    const int *rec = plan + kPlanHeaderWords + tile * plan_tile_words(ntx, nrx);
-    const int nlive = __ldg(rec);
-    const long long frame_ch = (long long)f * ntx * nrx;
+    const long long tiles = (np + kBlock - 1) / kBlock;
+    const long long tile_words = plan_tile_words(ntx, nrx);
+    const long long nitems = tiles * a.nframes;
+    const int *order = plan + kPlanHeaderWords + tiles * tile_words;
+    unsigned *queue = reinterpret_cast<unsigned *>(plan + 1);
     const long long chs = (long long)nrx * a.nt;
-    const long long op = valid ? (a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i) : 0;
 
     if (tid < kStages) {
         mbar_init(&full[tid], 1);
         mbar_init(&empty[tid], kWarps);
-    }
-    {
-        const float *txlh = reinterpret_cast<const float *>(rec + 1 + 3 * nrx);
-        if (tid < 2 * ntx) s_txlh[tid] = __ldg(txlh + tid);
-        for (int k = tid; k < nlive; k += kBlock) s_rx[k] = __ldg(rec + 1 + k);
-        const float *rxlh = reinterpret_cast<const float *>(rec + 1 + nrx);
-        for (int k = tid; k < 2 * nlive; k += kBlock) s_rxlh[k] = __ldg(rxlh + k);
     }
     if (tid == 0) {
         s_failed = 0;
         s_produced = 0;
     }
     mbar_fence_init();
-    __syncthreads();
 
-    // producer: windows of live receive `it` into slot it % kStages
-    auto produce = [&](int it) {
-        const int slot = it % kStages;
-        const int code = s_rx[it];
-        bool staged = !(code & 0x40000000);
-        const int r = code & 0x3fffffff;
-        int e0 = 0, e1 = 0;
-        if (staged && lane < ntx) {
-            const float xlo = __fadd_rn(s_txlh[2 * lane], s_rxlh[2 * it]);
-            const float xhi = __fadd_rn(s_txlh[2 * lane + 1], s_rxlh[2 * it + 1]);
-            staged_window<KIND, T>(xlo, xhi, a, e0, e1);
+    long long g0 = 0;  // ring items this CTA has run before the current tile
+    for (;;) {
+        if (tid == 0) s_item = (long long)atomicAdd(queue, 1u);
+        __syncthreads();  // also: every warp is done with the previous tile's ring and plan data
+        const long long item = s_item;
+        if (item >= nitems || s_failed) break;
+        const int f = (int)(item / tiles);
+        const long long tile = __ldg(order + (item - (long long)f * tiles));
+        const long long i = tile * kBlock + tid;
+        const bool valid = i < np;
+        const int *rec = plan + kPlanHeaderWords + tile * tile_words;
+        const int nlive = __ldg(rec);
+        const long long frame_ch = (long long)f * ntx * nrx;
+        const long long op = valid ? (a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i) : 0;
+        {
+            const float *txlh = reinterpret_cast<const float *>(rec + 1 + 3 * nrx);
+            if (tid < 2 * ntx) s_txlh[tid] = __ldg(txlh + tid);
+            for (int k = tid; k < nlive; k += kBlock) s_rx[k] = __ldg(rec + 1 + k);
+            const float *rxlh = reinterpret_cast<const float *>(rec + 1 + nrx);
+            for (int k = tid; k < 2 * nlive; k += kBlock) s_rxlh[k] = __ldg(rxlh + k);
         }
-        const int cnt = e1 - e0;
-        int off = cnt;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, off, o);
-            if (lane >= o) off += v;
-        }
-        const int total = __shfl_sync(0xffffffffu, off, 31);
-        off -= cnt;
-        // the plan sized these windows to fit; a plan from other tables could
-        // not, and then this receive is gathered from global memory instead
-        if ((long long)total * (long long)sizeof(E) > kStageBytes) staged = false;
-        if (lane < kTxReg) sbase[slot][lane] = (staged && lane < ntx) ? off - e0 : 0;
-        if (lane == 0) sstaged[slot] = staged ? 1 : 0;
-        __syncwarp();
-        if (lane == 0) mbar_arrive_expect_tx(&full[slot], staged ? (unsigned)(total * sizeof(E)) : 0u);
-        __syncwarp();
-        if (staged && lane < ntx && cnt > 0) {
-            const E *src = static_cast<const E *>(a.data) + (frame_ch + (long long)lane * nrx + r) * a.nt + e0;
-            E *dst = reinterpret_cast<E *>(smem_raw + (size_t)slot * kStageBytes) + off;
-            tma_bulk_load(dst, src, (unsigned)(cnt * sizeof(E)), &full[slot]);
-        }
-    };
-    // warp 0 stages the first kStages receives; after that the producer role
-    // rotates over the warps (a bulk copy costs ~100 cycles to issue, and one
-    // warp issuing every receive's copies starved the others)
-    if (w == 0) {
-        for (int it = 0; it < kStages && it < nlive; ++it) produce(it);
-        if (lane == 0) atomicMax(&s_produced, min(kStages, nlive));
-    }
+        __syncthreads();
 
-    // transmit side of this pixel; slots past ntx carry zero weights
-    float rtau[kTxReg], rapod[kTxReg];
-    float amax = 0.f;
+        // producer: windows of live receive `it` of this tile into its ring slot
+        auto produce = [&](int it) {
+            const long long gi = g0 + it;
+            const int slot = (int)(gi % kStages);
+            const int code = s_rx[it];
+            bool staged = !(code & 0x40000000);
+            const int r = code & 0x3fffffff;
+            int e0 = 0, e1 = 0;
+            if (staged && lane < ntx) {
+                const float xlo = __fadd_rn(s_txlh[2 * lane], s_rxlh[2 * it]);
+                const float xhi = __fadd_rn(s_txlh[2 * lane + 1], s_rxlh[2 * it + 1]);
+                staged_window<KIND, T>(xlo, xhi, a, e0, e1);
+            }
+            const int cnt = e1 - e0;
+            int off = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, off, o);
+                if (lane >= o) off += v;
+            }
+            const int total = __shfl_sync(0xffffffffu, off, 31);
+            off -= cnt;
+            // the plan sized these windows to fit; a plan from other tables could
+            // not, and then this receive is gathered from global memory instead
+            if ((long long)total * (long long)sizeof(E) > kStageBytes) staged = false;
+            if (lane < kTxReg) sbase[slot][lane] = (staged && lane < ntx) ? off - e0 : 0;
+            if (lane == 0) sstaged[slot] = staged ? 1 : 0;
+            __syncwarp();
+            if (lane == 0) mbar_arrive_expect_tx(&full[slot], staged ? (unsigned)(total * sizeof(E)) : 0u);
+            __syncwarp();
+            if (staged && lane < ntx && cnt > 0) {
+                const E *src = static_cast<const E *>(a.data) + (frame_ch + (long long)lane * nrx + r) * a.nt + e0;
+                E *dst = reinterpret_cast<E *>(smem_raw + (size_t)slot * kStageBytes) + off;
+                tma_bulk_load(dst, src, (unsigned)(cnt * sizeof(E)), &full[slot]);
+            }
+        };
+        // warp 0 stages the tile's first kStages receives (their slots were freed
+        // by every warp before the barrier above); after that the producer role
+        // rotates over the warps (a bulk copy costs ~100 cycles to issue, and one
+        // warp issuing every receive's copies starved the others)
+        if (w == 0) {
+            for (int it = 0; it < kStages && it < nlive; ++it) produce(it);
+            if (lane == 0 && nlive > 0) atomicMax(&s_produced, g0 + min(kStages, nlive));
+        }
+
+        // transmit side of this pixel; slots past ntx carry zero weights
+        float rtau[kTxReg], rapod[kTxReg];
+        float amax = 0.f;
 #pragma unroll
-    for (int k = 0; k < kTxReg; ++k) {
-        rtau[k] = a.t0;
-        rapod[k] = 0.f;
-        if (k < ntx && valid) {
-            rtau[k] = __ldg(a.tautx + (long long)k * np + i);
-            rapod[k] = __ldg(a.apodtx + (long long)k * np + i);
-            amax = fmaxf(amax, fabsf(rapod[k]));
-        }
-    }
-
-    float acc = 0.f, s1 = 0.f;
-    bool failed = false;
-    // receive-side values, fetched two receives ahead
-    auto rx_load = [&](int it, float &trx, float &arx) {
-        const int r = s_rx[it] & 0x3fffffff;
-        trx = valid ? __ldg(a.taurx + (long long)r * np + i) : 0.f;
-        arx = valid ? __ldg(a.apodrx + (long long)r * np + i) : 0.f;
-    };
-    float trx1 = 0.f, arx1 = 0.f, trx2 = 0.f, arx2 = 0.f;
-    if (nlive > 0) rx_load(0, trx1, arx1);
-    if (nlive > 1) rx_load(1, trx2, arx2);
-
-    for (int it = 0; it < nlive; ++it) {
-        const int slot = it % kStages;
-        const int r = s_rx[it] & 0x3fffffff;
-        const float trx = trx1, arx = arx1;
-        trx1 = trx2;
-        arx1 = arx2;
-        if (it + 2 < nlive) rx_load(it + 2, trx2, arx2);
-        if (!mbar_wait_bounded(&full[slot], (unsigned)(it / kStages) & 1u)) failed = true;
-        if (failed || *(volatile int *)&s_failed) {
-            failed = true;
-            s_failed = 1;
-            break;
-        }
-
-        const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh);
-        float accr = 0.f;
-        if (live) {
-            const long long ch_first = (frame_ch + r) * a.nt;
-            if (sstaged[slot]) {
-                const E *stage = reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes);
-#pragma unroll
-                for (int g = 0; g < kTxReg; g += kTapGroup) {
-                    if (g < ntx) {
-                        const int4 b = *reinterpret_cast<const int4 *>(&sbase[slot][g]);
-                        const int bk[kTapGroup] = {b.x, b.y, b.z, b.w};
-                        accr = staged_group<KIND, T, true>(a, rtau + g, rapod + g, trx, arx, bk,
-                                                           stage, ch_first, chs, g, ntx, accr);
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int g = 0; g < kTxReg; g += kTapGroup) {
-                    if (g < ntx) {
-                        const int bk[kTapGroup] = {0, 0, 0, 0};
-                        accr = staged_group<KIND, T, false>(a, rtau + g, rapod + g, trx, arx, bk,
-                                                            nullptr, ch_first, chs, g, ntx, accr);
-                    }
-                }
+        for (int k = 0; k < kTxReg; ++k) {
+            rtau[k] = a.t0;
+            rapod[k] = 0.f;
+            if (k < ntx && valid) {
+                rtau[k] = __ldg(a.tautx + (long long)k * np + i);
+                rapod[k] = __ldg(a.apodtx + (long long)k * np + i);
+                amax = fmaxf(amax, fabsf(rapod[k]));
             }
         }
-        if (SUM == PYCBF_GB_SUM_TX_AND_RX) acc += accr;
-        if (SUM == PYCBF_GB_SUM_TX_ONLY && valid) a.out[((long long)f * nrx + r) * np + op] = accr;
-        if (SUM == PYCBF_GB_SUM_DMAS_SSR || SUM == PYCBF_GB_SUM_DMAS_POWER) {
-            const float s = (SUM == PYCBF_GB_SUM_DMAS_SSR) ? copysignf(sqrtf(fabsf(accr)), accr) : accr;
-            acc = fmaf(s, s1, acc);
-            s1 += s;
-        }
-        // this warp is done with the slot
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[slot]);
-        // warp it % kWarps refills the slot of the previous iteration once every
-        // warp left it
-        if (w == it % kWarps && it >= 1 && it - 1 + kStages < nlive) {
-            const int pit = it - 1;
-            if (!mbar_wait_bounded(&empty[pit % kStages], (unsigned)(pit / kStages) & 1u)) {
+
+        float acc = 0.f, s1 = 0.f;
+        bool failed = false;
+        // receive-side values, fetched two receives ahead
+        auto rx_load = [&](int it, float &trx, float &arx) {
+            const int r = s_rx[it] & 0x3fffffff;
+            trx = valid ? __ldg(a.taurx + (long long)r * np + i) : 0.f;
+            arx = valid ? __ldg(a.apodrx + (long long)r * np + i) : 0.f;
+        };
+        float trx1 = 0.f, arx1 = 0.f, trx2 = 0.f, arx2 = 0.f;
+        if (nlive > 0) rx_load(0, trx1, arx1);
+        if (nlive > 1) rx_load(1, trx2, arx2);
+
+        for (int it = 0; it < nlive; ++it) {
+            const long long gi = g0 + it;
+            const int slot = (int)(gi % kStages);
+            const int r = s_rx[it] & 0x3fffffff;
+            const float trx = trx1, arx = arx1;
+            trx1 = trx2;
+            arx1 = arx2;
+            if (it + 2 < nlive) rx_load(it + 2, trx2, arx2);
+            if (!mbar_wait_bounded(&full[slot], (unsigned)(gi / kStages) & 1u)) failed = true;
+            if (failed || *(volatile int *)&s_failed) {
                 failed = true;
                 s_failed = 1;
                 break;
             }
-            produce(pit + kStages);
-            if (lane == 0) atomicMax(&s_produced, pit + kStages + 1);
-        }
-    }
-    __syncthreads();
-    if (s_failed) {
-        // drain the copies still in flight before the CTA's shared memory goes
-        // away: the latest phase of each slot is one of the last kStages issued
-        if (tid == 0) {
-            if (status) atomicExch(status, 1);
-            const int produced = *(volatile int *)&s_produced;
-            for (int j = max(0, produced - kStages); j < produced; ++j)
-                (void)mbar_wait_bounded(&full[j % kStages], (unsigned)(j / kStages) & 1u);
+
+            const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh);
+            float accr = 0.f;
+            if (live) {
+                const long long ch_first = (frame_ch + r) * a.nt;
+                if (sstaged[slot]) {
+                    const E *stage = reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes);
+#pragma unroll
+                    for (int g = 0; g < kTxReg; g += kTapGroup) {
+                        if (g < ntx) {
+                            const int4 b = *reinterpret_cast<const int4 *>(&sbase[slot][g]);
+                            const int bk[kTapGroup] = {b.x, b.y, b.z, b.w};
+                            accr = staged_group<KIND, T, true>(a, rtau + g, rapod + g, trx, arx, bk,
+                                                               stage, ch_first, chs, g, ntx, accr);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int g = 0; g < kTxReg; g += kTapGroup) {
+                        if (g < ntx) {
+                            const int bk[kTapGroup] = {0, 0, 0, 0};
+                            accr = staged_group<KIND, T, false>(a, rtau + g, rapod + g, trx, arx, bk,
+                                                                nullptr, ch_first, chs, g, ntx, accr);
+                        }
+                    }
+                }
+            }
+            if (SUM == PYCBF_GB_SUM_TX_AND_RX) acc += accr;
+            if (SUM == PYCBF_GB_SUM_TX_ONLY && valid) a.out[((long long)f * nrx + r) * np + op] = accr;
+            if (SUM == PYCBF_GB_SUM_DMAS_SSR || SUM == PYCBF_GB_SUM_DMAS_POWER) {
+                const float sv = (SUM == PYCBF_GB_SUM_DMAS_SSR) ? copysignf(sqrtf(fabsf(accr)), accr) : accr;
+                acc = fmaf(sv, s1, acc);
+                s1 += sv;
+            }
+            // this warp is done with the slot
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[slot]);
+            // warp it % kWarps refills the slot of the previous receive once every
+            // warp left it
+            if (w == it % kWarps && it >= 1 && it - 1 + kStages < nlive) {
+                const long long pg = gi - 1;
+                if (!mbar_wait_bounded(&empty[pg % kStages], (unsigned)(pg / kStages) & 1u)) {
+                    failed = true;
+                    s_failed = 1;
+                    break;
+                }
+                produce(it - 1 + kStages);
+                if (lane == 0) atomicMax(&s_produced, pg + kStages + 1);
+            }
         }
         __syncthreads();
-        if (valid) {
-            const float nan = __int_as_float(0x7fc00000);
-            if (SUM == PYCBF_GB_SUM_TX_ONLY)
-                for (int r = 0; r < nrx; ++r) a.out[((long long)f * nrx + r) * np + op] = nan;
-            else
-                a.out[(long long)f * np + op] = nan;
+        if (s_failed) {
+            if (valid) {
+                const float nan = __int_as_float(0x7fc00000);
+                if (SUM == PYCBF_GB_SUM_TX_ONLY)
+                    for (int r = 0; r < nrx; ++r) a.out[((long long)f * nrx + r) * np + op] = nan;
+                else
+                    a.out[(long long)f * np + op] = nan;
+            }
+            break;
         }
-        return;
+        if (valid && SUM != PYCBF_GB_SUM_TX_ONLY) a.out[(long long)f * np + op] = acc;
+        g0 += nlive;
     }
-    if (valid && SUM != PYCBF_GB_SUM_TX_ONLY) a.out[(long long)f * np + op] = acc;
+    __syncthreads();
+    if (s_failed && tid == 0) {
+        // drain the copies still in flight before the CTA's shared memory goes
+        // away: the latest phase of each slot is one of the last kStages issued
+        atomicExch(plan, 1);
+        const long long produced = *(volatile long long *)&s_produced;
+        for (long long j = max(0LL, produced - kStages); j < produced; ++j)
+            (void)mbar_wait_bounded(&full[j % kStages], (unsigned)(j / kStages) & 1u);
+    }
 }
 
 inline size_t staged_smem_bytes(int nrx) {
     return (size_t)kStages * kStageBytes + sizeof(int) * 3 * (size_t)nrx;
 }
 
+// The order the persistent kernel takes the tiles in: most live receives
+// first (a counting sort over nlive, one CTA).  Ties may come in any order;
+// the images do not depend on it.
+static __global__ void __launch_bounds__(1024) plan_order_kernel(int *plan, long long tiles, int ntx,
+                                                          int nrx) {
+    extern __shared__ int bins[];  // nrx + 1 bins, nlive = nrx first
+    const long long tw = plan_tile_words(ntx, nrx);
+    int *order = plan + kPlanHeaderWords + tiles * tw;
+    for (int b = threadIdx.x; b <= nrx; b += blockDim.x) bins[b] = 0;
+    __syncthreads();
+    for (long long t = threadIdx.x; t < tiles; t += blockDim.x)
+        atomicAdd(&bins[nrx - min(max(plan[kPlanHeaderWords + t * tw], 0), nrx)], 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int b = 0; b <= nrx; ++b) {
+            const int c = bins[b];
+            bins[b] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    for (long long t = threadIdx.x; t < tiles; t += blockDim.x) {
+        const int b = nrx - min(max(plan[kPlanHeaderWords + t * tw], 0), nrx);
+        order[atomicAdd(&bins[b], 1)] = (int)t;
+    }
+}
+
 template <int KIND, typename T>
 cudaError_t launch_plan_one(const DasArgs &a, int *plan, cudaStream_t s) {
     const long long tiles = (a.np + kBlock - 1) / kBlock;
     tabbed_plan_kernel<KIND, T><<<(unsigned)tiles, kBlock, 0, s>>>(a, plan);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    const size_t smem = sizeof(int) * ((size_t)a.nrx + 1);
+    plan_order_kernel<<<1, 1024, smem, s>>>(plan, tiles, a.ntx, a.nrx);
     return cudaGetLastError();
 }
 
@@ -547,8 +606,19 @@ cudaError_t launch_staged_one(const DasArgs &a, const int *plan, int *status, cu
     const int smem = (int)staged_smem_bytes(a.nrx);
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (err != cudaSuccess) return err;
-    const long long tiles = (a.np + kBlock - 1) / kBlock;
-    kern<<<dim3((unsigned)tiles, (unsigned)a.nframes), kBlock, smem, s>>>(a, plan, status);
+    int dev = 0, nsm = 0, per_sm = 0;
+    if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
+    if ((err = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+        return err;
+    if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, smem)) !=
+        cudaSuccess)
+        return err;
+    const long long items = (a.np + kBlock - 1) / kBlock * (long long)a.nframes;
+    const long long grid = std::min<long long>(items, (long long)std::max(1, per_sm) * nsm);
+    // the queue head, plan[1], starts at zero
+    err = cudaMemsetAsync(status + 1, 0, sizeof(int), s);
+    if (err != cudaSuccess) return err;
+    kern<<<(unsigned)grid, kBlock, smem, s>>>(a, const_cast<int *>(plan));
     return cudaGetLastError();
 }
 

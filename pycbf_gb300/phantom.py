@@ -298,3 +298,53 @@ def batch_frames(n=64, seed=64, n_speckle=300, n_points=5, pitch=0.2e-3, max_deg
                                         -40.0, seed * 1000 + k)
         out.append(entry)
     return out
+
+
+def matrix_dw_synthetic(nside=32, pitch=0.3e-3, nvs=5, vs_behind=10e-3, fs=20e6, fc=3.5e6,
+                        bw=0.6, nt=2048, c=1540.0, nvox=(128, 128, 256),
+                        lims=((-10e-3, 10e-3), (-10e-3, 10e-3), (5e-3, 65e-3)), n_speckle=200_000,
+                        n_points=50, fnum=1.5, noise_db=-40.0, seed=5353, device=None,
+                        name="matrix_3d") -> SyntheticWorkload:
+    """3-D diverging waves from a matrix array (defaults: 32 x 32 elements at
+    0.3 mm, 25 virtual sources on a 5 x 5 grid 10 mm behind the array, fs 20
+    MHz, 3.5 MHz pulse, Nt 2048, 128 x 128 x 256 voxels over 20 x 20 x 60 mm).
+
+    Transmits are virtual sources (synthetic-point form with dof = 0): delay
+    |p - v| / c - |v| ... written as sign(proj) |p - v| / c + t0tx with t0tx
+    = -(distance from the source to the array plane) / c, acceptance angle
+    covering the aperture; receives take the F-number mask."""
+    dev = _device(device)
+    e1 = helpers.element_positions(nside, pitch)
+    ex, ey = np.meshgrid(e1, e1, indexing="ij")
+    nele = nside * nside
+    ovecrx = np.stack([ex.ravel(), ey.ravel(), np.zeros(nele)], axis=1)
+    nvecrx = np.tile(np.array([0.0, 0.0, 1.0]), (nele, 1))
+    alarx = np.arctan2(0.5, fnum) * np.ones(nele)
+    half = 0.5 * nside * pitch
+    v1 = np.linspace(-half, half, nvs)
+    vx, vy = np.meshgrid(v1, v1, indexing="ij")
+    ntx = nvs * nvs
+    ovectx = np.stack([vx.ravel(), vy.ravel(), -vs_behind * np.ones(ntx)], axis=1)
+    nvectx = np.tile(np.array([0.0, 0.0, 1.0]), (ntx, 1))
+    t0tx = -vs_behind / c * np.ones(ntx)
+    # the cone from each source through the whole aperture and beyond
+    alatx = np.arctan2(2.0 * half, vs_behind) * np.ones(ntx)
+    doftx = np.zeros(ntx)
+    axes = [np.linspace(lo, hi, n) for (lo, hi), n in zip(lims, nvox)]
+    X, Y, Z = np.meshgrid(*axes, indexing="ij")
+    pnts = np.ascontiguousarray(np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1))
+    rng = np.random.default_rng(seed)
+    ns = n_speckle + n_points
+    pos = np.stack([rng.uniform(lo, hi, ns) for lo, hi in lims], axis=1)
+    amp = np.concatenate([rng.normal(0.0, 1.0, n_speckle), np.full(n_points, 10.0)])
+    d = pos[None, :, :] - ovectx[:, None, :]
+    proj = np.sum(d * nvectx[:, None, :], axis=-1)
+    tt = np.sign(proj) * np.linalg.norm(d, axis=-1) / c + t0tx[:, None]
+    tr = np.linalg.norm(pos[None, :, :] - ovecrx[:, None, :], axis=-1) / c
+    t0, dt = 0.0, 1.0 / fs
+    rf = simulate_channels(torch.tensor(tt, device=dev), torch.tensor(tr, device=dev),
+                           torch.tensor(amp, device=dev), t0, dt, nt, fc, bw, noise_db, seed)
+    geo = dict(ovectx=ovectx, nvectx=nvectx, t0tx=t0tx, doftx=doftx, alatx=alatx, ovecrx=ovecrx,
+               nvecrx=nvecrx, alarx=alarx, c0=c, pnts=pnts)
+    return SyntheticWorkload(name, rf.cpu().numpy(), geo, t0, dt, nt, tuple(nvox),
+                             dict(nside=nside, pitch=pitch, fs=fs, fc=fc, c=c, seed=seed))

@@ -96,7 +96,7 @@ def test_plan_validation():
     L = _lib.load()
     info = _info()
     p = ct.c_void_p(16)
-    assert L.pycbf_gb_tabbed_plan_bytes(1000, 11, 128) == 4 * (4 + 8 * (1 + 128 * 3 + 22))
+    assert L.pycbf_gb_tabbed_plan_bytes(1000, 11, 128) == 4 * (4 + 8 * (1 + 128 * 3 + 22) + 8)
     assert L.pycbf_gb_tabbed_plan_bytes(0, 11, 128) == 0
     call = lambda **kw: L.pycbf_gb_tabbed_plan(
         ct.byref(kw.get("info", info)), p, p, p, p, kw.get("np", 10), kw.get("interp", 2), 0.01,
