@@ -402,8 +402,11 @@ int run_adjoint(const pycbf_gb_rfinfo *rf, AdjArgs &g, void *workspace, size_t w
         if (!workspace || workspace_bytes < need || reinterpret_cast<uintptr_t>(workspace) % 16)
             return PYCBF_GB_EWORKSPACE;
         g.gk_buf = static_cast<float *>(workspace);
-        g.partial = reinterpret_cast<float *>(static_cast<char *>(workspace) +
-                                              adjoint_grad_bytes(rf->nframes, rf->nrx, g.d.np));
+        char *ws = static_cast<char *>(workspace);
+        const size_t gb = adjoint_grad_bytes(rf->nframes, rf->nrx, g.d.np);
+        g.partial = reinterpret_cast<float *>(ws + gb);
+        g.live = reinterpret_cast<unsigned char *>(
+            ws + gb + adjoint_partial_bytes(rf->nframes, rf->ntx, rf->nrx, g.d.np, rf->nt));
     }
     return cuda_status(launch_adjoint(g, rf->dtype, s));
 }

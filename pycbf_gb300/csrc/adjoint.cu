@@ -181,6 +181,43 @@ __global__ void __launch_bounds__(kBlock) adj_delay_kernel(const __grid_constant
 }
 
 // ---------------------------------------------------------------------------
+// which receives can contribute to which tiles of kBlock pixels: Tabbed, some
+// pixel has fl(max_t |apodtx| * |apodrx|) >= thresh (by monotonic rounding
+// every tap of a dead pair fails the threshold); Synthetic, the receive's mask
+// accepts some pixel.  One CTA per tile.
+// ---------------------------------------------------------------------------
+template <int GEOM>
+__global__ void __launch_bounds__(kBlock) adj_live_kernel(const __grid_constant__ AdjArgs g) {
+    const DasArgs &a = g.d;
+    const long long tile = blockIdx.x;
+    const long long tiles = gridDim.x;
+    const long long i = tile * kBlock + threadIdx.x;
+    const bool valid = i < a.np;
+    float amax = 0.f;
+    float pnt[3] = {0.f, 0.f, 0.f};
+    if (valid) {
+        if (GEOM == GEOM_TABBED)
+            for (int t = 0; t < a.ntx; ++t)
+                amax = fmaxf(amax, fabsf(__ldg(a.apodtx + (long long)t * a.np + i)));
+        else
+            for (int k = 0; k < a.ndim; ++k) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
+    }
+    for (int r = 0; r < a.nrx; ++r) {
+        bool v = false;
+        if (valid) {
+            if (GEOM == GEOM_TABBED) {
+                v = __fmul_rn(amax, fabsf(__ldg(a.apodrx + (long long)r * a.np + i))) >= a.thresh;
+            } else {
+                float D;
+                v = synth_rx_path(a, r, pnt, D);
+            }
+        }
+        v = __syncthreads_or(v);
+        if (threadIdx.x == 0) g.live[(long long)r * tiles + tile] = v ? 1 : 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // channel data: transpose of the interpolation, per (channel, part)
 // ---------------------------------------------------------------------------
 template <int GEOM, int SUM>
@@ -224,11 +261,20 @@ __global__ void __launch_bounds__(128) adj_scatter_kernel(const __grid_constant_
         }
         in.gp = __ldg(grow + i);
     };
+    // steps of blockDim pixels whose tile receive r can contribute to; the
+    // others are skipped (the same for every thread of the CTA)
+    const unsigned char *rx_live = g.live + (long long)r * ((np + kBlock - 1) / kBlock);
+    auto next_live = [&](long long b) {
+        while (b < i1 && !rx_live[b / kBlock]) b += blockDim.x;
+        return b;
+    };
     In cur = {{0.f, 0.f, 0.f, 0.f}, 0.f}, nxt = cur;
-    fetch(i0 + threadIdx.x, cur);
-    for (long long base = i0; base < i1; base += blockDim.x) {
+    long long nbase = next_live(i0);
+    if (nbase < i1) fetch(nbase + threadIdx.x, cur);
+    for (long long base = nbase; base < i1; base = nbase) {  // `continue` advances too
         const long long i = base + threadIdx.x;
-        fetch(i + blockDim.x, nxt);
+        nbase = next_live(base + blockDim.x);
+        if (nbase < i1) fetch(nbase + threadIdx.x, nxt);
         bool hit = false;
         int j = 0;
         float am = 0.f, b = 0.f, v = 0.f;
@@ -388,6 +434,10 @@ cudaError_t launch_scatter_one(const AdjArgs &g, cudaStream_t s) {
     const int Lp = (a.nt + 1 + 3) & ~3;
     const long long per = (a.np + nparts - 1) / nparts;
     const long long part_len = (per + 127) / 128 * 128;
+    const long long tiles = (a.np + kBlock - 1) / kBlock;
+    adj_live_kernel<GEOM><<<(unsigned)tiles, kBlock, 0, s>>>(g);
+    cudaError_t lerr = cudaGetLastError();
+    if (lerr != cudaSuccess) return lerr;
     const size_t smem = (size_t)nw * 2 * Lp * sizeof(float);
     auto kern = adj_scatter_kernel<GEOM, SUM>;
     cudaError_t err =
@@ -465,12 +515,18 @@ size_t adjoint_grad_bytes(long long nframes, long long nrx, long long np) {
     return ((size_t)nframes * (size_t)nrx * (size_t)np * sizeof(float) + 255) & ~(size_t)255;
 }
 
-size_t adjoint_workspace_bytes(long long nframes, long long ntx, long long nrx, long long np,
-                               int nt) {
+size_t adjoint_partial_bytes(long long nframes, long long ntx, long long nrx, long long np,
+                             int nt) {
     const long long nch = nframes * ntx * nrx;
     const size_t Lp = (size_t)((nt + 1 + 3) & ~3);
-    return adjoint_grad_bytes(nframes, nrx, np) +
-           (size_t)adjoint_parts(nch, np) * (size_t)nch * 2 * Lp * sizeof(float);
+    return (size_t)adjoint_parts(nch, np) * (size_t)nch * 2 * Lp * sizeof(float);
+}
+
+size_t adjoint_workspace_bytes(long long nframes, long long ntx, long long nrx, long long np,
+                               int nt) {
+    const size_t tiles = (size_t)((np + kBlock - 1) / kBlock);
+    return adjoint_grad_bytes(nframes, nrx, np) + adjoint_partial_bytes(nframes, ntx, nrx, np, nt) +
+           (((size_t)nrx * tiles + 255) & ~(size_t)255);
 }
 
 cudaError_t launch_adjoint(const AdjArgs &g, int dtype, cudaStream_t s) {

@@ -174,13 +174,16 @@ struct AdjArgs {
     float *grad_slow;     // Synthetic (np), or NULL
     float *gk_buf;        // workspace: grad_out gathered into kernel pixel order
     float *partial;       // workspace: per-part sums of the spline-record adjoints
+    unsigned char *live;  // workspace: live[r * tiles + tile] = receive r can contribute to the tile
     const float *gk;      // set by launch_adjoint: gk_buf, or grad_out without pixel_index
 };
 // parts of the pixel range whose channel adjoints are summed separately, and
 // the workspace: [gathered gradient (nframes * nrx * np floats, 256-byte
-// rounded)][partial sums (parts * nch * 2 * Lp floats)]
+// rounded)][partial sums (parts * nch * 2 * Lp floats)][receive-tile liveness
+// (nrx * tiles bytes, 256-byte rounded)]
 int adjoint_parts(long long nch, long long np);
 size_t adjoint_grad_bytes(long long nframes, long long nrx, long long np);
+size_t adjoint_partial_bytes(long long nframes, long long ntx, long long nrx, long long np, int nt);
 size_t adjoint_workspace_bytes(long long nframes, long long ntx, long long nrx, long long np,
                                int nt);
 int adjoint_rows_warps(int nt);  // warps (private accumulation rows) per scatter CTA, 0 = nt too large

@@ -257,12 +257,12 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
 // ---------------------------------------------------------------------------
 constexpr int kTapGroup = 4;
 
-// One group of kTapGroup taps of receive (trx, arx): index, gather, weight,
+// One group of N <= kTapGroup taps of receive (trx, arx): index, gather, weight,
 // accumulate.  STAGED gathers from the shared-memory stage at clamped
 // indices, otherwise from global memory.  A tap whose quotient lies within
 // a few ulp of a rounding boundary has its index redone with the IEEE
 // division; the group branches only when some tap needs it.
-template <int KIND, typename T, bool STAGED>
+template <int KIND, typename T, bool STAGED, int N>
 __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt, const float *at,
                                               float trx, float arx, const int *bk,
                                               const typename StagedElem<KIND, T>::E *stage,
@@ -270,14 +270,37 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt,
                                               float accr) {
     using K = Kind<KIND, T>;
     constexpr unsigned cap = kStageBytes / sizeof(typename StagedElem<KIND, T>::E);
-    float xs[kTapGroup], ap[kTapGroup], fl[kTapGroup];
-    bool ok[kTapGroup];
+    float xs[N], ap[N], fl[N];
+    bool ok[N];
     bool nearb = false;
 #pragma unroll
-    for (int k = 0; k < kTapGroup; ++k) {
-        const float x = __fadd_rn(tt[k], trx);
-        const float apod = __fmul_rn(at[k], arx);
-        const float q = __fmul_rn(__fsub_rn(x, a.t0), a.inv_dt);
+    // delay sums, weights and quotients two taps at a time in packed float32
+    // pairs (each lane rounded as the scalar operation: the same bits)
+    float px[N], pa[N], pq[N];
+#pragma unroll
+    for (int k = 0; k < N; k += 2) {
+        if (k + 1 < N) {
+            const float2 x2 = __fadd2_rn(make_float2(tt[k], tt[k + 1]), make_float2(trx, trx));
+            const float2 a2 = __fmul2_rn(make_float2(at[k], at[k + 1]), make_float2(arx, arx));
+            const float2 q2 = __fmul2_rn(__fadd2_rn(x2, make_float2(-a.t0, -a.t0)),
+                                         make_float2(a.inv_dt, a.inv_dt));
+            px[k] = x2.x;
+            px[k + 1] = x2.y;
+            pa[k] = a2.x;
+            pa[k + 1] = a2.y;
+            pq[k] = q2.x;
+            pq[k + 1] = q2.y;
+        } else {
+            px[k] = __fadd_rn(tt[k], trx);
+            pa[k] = __fmul_rn(at[k], arx);
+            pq[k] = __fmul_rn(__fsub_rn(px[k], a.t0), a.inv_dt);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const float x = px[k];
+        const float apod = pa[k];
+        const float q = pq[k];
         // |q_fast - q_exact| <= 1.5 ulp(q) <= 1.5 |q| 2^-23; flag within |q| 2^-21
         const float tol = fmaf(fabsf(q), 4.76837158e-7f, 1e-30f);
         float flk;
@@ -298,7 +321,7 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt,
     }
     if (nearb) {
 #pragma unroll
-        for (int k = 0; k < kTapGroup; ++k) {
+        for (int k = 0; k < N; ++k) {
             const float qe = __fdiv_rn(__fsub_rn(xs[k], a.t0), a.dt);
             if (KIND == PYCBF_GB_INTERP_NEAREST) {
                 fl[k] = truncf(qe + 0.5f);
@@ -309,9 +332,9 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt,
             }
         }
     }
-    typename K::P pv[kTapGroup];
+    typename K::P pv[N];
 #pragma unroll
-    for (int k = 0; k < kTapGroup; ++k) {
+    for (int k = 0; k < N; ++k) {
         const int j = min(max((int)fl[k], 0), a.nt - 1);
         if (STAGED) {
             pv[k] = staged_load<KIND, T>(stage, bk[k], j, cap, a);
@@ -323,7 +346,7 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt,
         }
     }
 #pragma unroll
-    for (int k = 0; k < kTapGroup; ++k) {
+    for (int k = 0; k < N; ++k) {
         const float c = fmaf(ap[k], K::value(pv[k], xs[k], fl[k], a), accr);
         accr = ok[k] ? c : accr;
     }
@@ -494,8 +517,16 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
                         if (g < ntx) {
                             const int4 b = *reinterpret_cast<const int4 *>(&sbase[slot][g]);
                             const int bk[kTapGroup] = {b.x, b.y, b.z, b.w};
-                            accr = staged_group<KIND, T, true>(a, rtau + g, rapod + g, trx, arx, bk,
-                                                               stage, ch_first, chs, g, ntx, accr);
+                            // the last group holds only the transmits left (no padded tap)
+                            const int rem = ntx - g;
+#define PGB_GROUP(n)                                                                            \
+    staged_group<KIND, T, true, n>(a, rtau + g, rapod + g, trx, arx, bk, stage, ch_first, chs, g, \
+                                   ntx, accr)
+                            if (rem >= 4) accr = PGB_GROUP(4);
+                            else if (rem == 3) accr = PGB_GROUP(3);
+                            else if (rem == 2) accr = PGB_GROUP(2);
+                            else accr = PGB_GROUP(1);
+#undef PGB_GROUP
                         }
                     }
                 } else {
@@ -503,7 +534,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
                     for (int g = 0; g < kTxReg; g += kTapGroup) {
                         if (g < ntx) {
                             const int bk[kTapGroup] = {0, 0, 0, 0};
-                            accr = staged_group<KIND, T, false>(a, rtau + g, rapod + g, trx, arx, bk,
+                            accr = staged_group<KIND, T, false, kTapGroup>(a, rtau + g, rapod + g, trx, arx, bk,
                                                                 nullptr, ch_first, chs, g, ntx, accr);
                         }
                     }
