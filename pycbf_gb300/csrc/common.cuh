@@ -72,6 +72,40 @@ template <> struct CoefRec<__nv_bfloat16> {
 };
 
 // ---------------------------------------------------------------------------
+// packed float32 pairs (sm_100+ f32x2 arithmetic, one instruction for two
+// lanes, each rounded to nearest as the scalar operation).  A packed multiply
+// whose result feeds a packed add was observed to come out with one rounding,
+// as a fused multiply-add -- with the float2 intrinsics and with this PTX
+// alike -- so code here never feeds a packed product into a packed add; a
+// product that must be rounded on its own is formed with __fmul_rn.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long pack2(float2 v) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(v.x), "f"(v.y));
+    return r;
+}
+__device__ __forceinline__ float2 unpack2(unsigned long long r) {
+    float2 v;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+    return v;
+}
+__device__ __forceinline__ float2 add2_rn(float2 a, float2 b) {
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+    return unpack2(r);
+}
+__device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+    return unpack2(r);
+}
+__device__ __forceinline__ float2 fma2_rn(float2 a, float2 b, float2 c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)), "l"(pack2(c)));
+    return unpack2(r);
+}
+
+// ---------------------------------------------------------------------------
 // spline prefilter
 // ---------------------------------------------------------------------------
 // The forward sweep of the natural-spline tridiagonal solve (pycbf.c:126-133)

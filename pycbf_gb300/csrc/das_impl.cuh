@@ -79,12 +79,15 @@ template <typename T> struct Kind<PYCBF_GB_INTERP_CUBIC, T> {
         return CoefRec<T>::load(static_cast<const rec *>(data) + ch + idx);
     }
     // fj: the knot index as a float (exact: j < 2^23)
+    // knot positions (xhi, xlo), fractions (a, b) and cubic weights in packed
+    // float32 pairs, each lane rounded as knot_fractions rounds it; b comes
+    // from (xlo - x) * -1/dt, the same bits as (x - xlo) * 1/dt
     static __device__ __forceinline__ float value(const P &c, float x, float fj, const DasArgs &a) {
-        float am, b;
-        knot_fractions(x, fj, a, am, b);
-        const float wa = fmaf(am * am, am, -am);
-        const float wb = fmaf(b * b, b, -b);
-        return fmaf(am, c.x, fmaf(b, c.y, fmaf(wa, c.z, wb * c.w)));
+        const float2 K = add2_rn(make_float2(a.t0, a.t0),
+                                 make_float2(__fmul_rn(a.dt, __fadd_rn(fj, 1.0f)), __fmul_rn(a.dt, fj)));
+        const float2 AB = mul2_rn(add2_rn(K, make_float2(-x, -x)), make_float2(a.inv_dt, -a.inv_dt));
+        const float2 W = fma2_rn(mul2_rn(AB, AB), AB, make_float2(-AB.x, -AB.y));
+        return fmaf(AB.x, c.x, fmaf(AB.y, c.y, fmaf(W.x, c.z, W.y * c.w)));
     }
 };
 

@@ -273,16 +273,15 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt,
     float xs[N], ap[N], fl[N];
     bool ok[N];
     bool nearb = false;
-#pragma unroll
     // delay sums, weights and quotients two taps at a time in packed float32
     // pairs (each lane rounded as the scalar operation: the same bits)
     float px[N], pa[N], pq[N];
 #pragma unroll
     for (int k = 0; k < N; k += 2) {
         if (k + 1 < N) {
-            const float2 x2 = __fadd2_rn(make_float2(tt[k], tt[k + 1]), make_float2(trx, trx));
-            const float2 a2 = __fmul2_rn(make_float2(at[k], at[k + 1]), make_float2(arx, arx));
-            const float2 q2 = __fmul2_rn(__fadd2_rn(x2, make_float2(-a.t0, -a.t0)),
+            const float2 x2 = add2_rn(make_float2(tt[k], tt[k + 1]), make_float2(trx, trx));
+            const float2 a2 = mul2_rn(make_float2(at[k], at[k + 1]), make_float2(arx, arx));
+            const float2 q2 = mul2_rn(add2_rn(x2, make_float2(-a.t0, -a.t0)),
                                          make_float2(a.inv_dt, a.inv_dt));
             px[k] = x2.x;
             px[k + 1] = x2.y;
