@@ -465,16 +465,33 @@ class TabbedBeamformer(Tabbed, _GPUBeamformer):
         if self._interp_code != _lib.INTERP["cubic"]:
             raise BeamformerException("the differentiable path interpolates with the cubic spline")
         rf = self._autograd_input(txrxt)
-        ktx, kap_tx, krx, kap_rx = self._tables
-        perm = None if self._pixel_index is None else self._pixel_index.long()
-        order = (lambda t: t) if perm is None else (lambda t: t[:, perm])
-        if tautx is not None:
-            ktx = order(tautx.to(device="cuda", dtype=torch.float32))
-        if taurx is not None:
-            krx = order(taurx.to(device="cuda", dtype=torch.float32))
-        return adjoint.das_tabbed(rf, ktx, krx, kap_tx, kap_rx, t0=self.t0, dt=self.dt,
-                                  thresh=self.thresh, sumtype=sumtype or self.sumtype,
-                                  pixel_index=self._pixel_index)
+        if tautx is None and taurx is None:
+            ktx, kap_tx, krx, kap_rx = self._tables
+            return adjoint.das_tabbed(rf, ktx, krx, kap_tx, kap_rx, t0=self.t0, dt=self.dt,
+                                      thresh=self.thresh, sumtype=sumtype or self.sumtype,
+                                      pixel_index=self._pixel_index)
+        # caller-owned delay tables: run in the caller's pixel order, so that
+        # no permutation (and no scatter of its gradient) is needed
+        ntx_, nap_tx, nrx_, nap_rx = self._natural_tables()
+        ktx = ntx_ if tautx is None else tautx.to(device="cuda", dtype=torch.float32)
+        krx = nrx_ if taurx is None else taurx.to(device="cuda", dtype=torch.float32)
+        return adjoint.das_tabbed(rf, ktx, krx, nap_tx, nap_rx, t0=self.t0, dt=self.dt,
+                                  thresh=self.thresh, sumtype=sumtype or self.sumtype)
+
+    def _natural_tables(self):
+        """The tables in the caller's pixel order (kept after the first use)."""
+        if getattr(self, "_nat_tables", None) is None:
+            if self._pixel_index is None:
+                self._nat_tables = self._tables
+            else:
+                perm = self._pixel_index.long()
+                nat = []
+                for t in self._tables:
+                    u = torch.empty_like(t)
+                    u[:, perm] = t
+                    nat.append(u)
+                self._nat_tables = tuple(nat)
+        return self._nat_tables
 
     def kernel_status(self) -> int:
         """0, or 1 if a staged launch gave up a bounded wait (its outputs are NaN)."""

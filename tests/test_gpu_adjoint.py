@@ -225,3 +225,26 @@ def test_speed_of_sound_loss_backpropagates(syn):
     an = float(model.c.grad)
     print("dL/dc analytic", an, "central differences", fd)
     assert abs(fd[1e-4] - an) <= 0.05 * abs(an) and abs(fd[3e-5] - an) <= 0.05 * abs(an)
+
+
+def test_caller_delay_tables_in_any_pixel_order(tab):
+    """Learnable delay tables go through the beamformer in the caller's pixel
+    order whatever order the beamformer keeps its own tables in."""
+    tautx, taurx, apodtx, apodrx = _tables(tab)
+    rf = torch.as_tensor(tab.rf, device="cuda")
+    res = []
+    for order in ("auto", "natural"):
+        bf = TabbedBeamformer(tautx=tab.tautx, apodtx=tab.apodtx, taurx=tab.taurx, apodrx=tab.apodrx,
+                              t0=tab.t0, dt=tab.dt, nt=tab.nt, interp={"kind": "cubic"},
+                              pixel_order=order)
+        r = rf.clone().requires_grad_(True)
+        ttx, trx = tautx.clone().requires_grad_(True), taurx.clone().requires_grad_(True)
+        out = bf.differentiable(r, tautx=ttx, taurx=trx)
+        out.sum().backward()
+        res.append((out.detach(), r.grad, ttx.grad, trx.grad))
+    assert torch.equal(res[0][0], res[1][0])
+    assert torch.equal(res[0][2], res[1][2]) and torch.equal(res[0][3], res[1][3])
+    assert rel(res[0][1], res[1][1]) <= 1e-6
+    ref = TabbedBeamformer(tautx=tab.tautx, apodtx=tab.apodtx, taurx=tab.taurx, apodrx=tab.apodrx,
+                           t0=tab.t0, dt=tab.dt, nt=tab.nt, interp={"kind": "cubic"})(rf, out_as_numpy=False)
+    assert torch.equal(res[0][0], ref)
