@@ -218,6 +218,31 @@ int pycbf_gb_das_synthetic_poly(const pycbf_gb_rfinfo *rf, const void *coef, int
                                 int sumtype, float *out, void *stream);
 
 /* ---------------------------------------------------------------------- */
+/* Delay tables and apodizations of a linear array on a pixel grid, built  */
+/* on the GPU.  Replaces make_tabs_and_apods_2D                            */
+/* (pycbf/helpers/__full_aperture_2D__.py:170-203) and the table functions */
+/* it calls (:3-168), whose float64 NumPy result the reference classes     */
+/* cast to float32.  Pixels: meshgrid(xout, zout, indexing='ij')           */
+/* flattened (z fastest), np = nx*nz.  txkind 0 plane wave, 1 diverging,   */
+/* 2 focused; tx_params (host, ntx <= 256 rows of 6 doubles), computed as  */
+/* those functions compute them:                                           */
+/*   plane wave  (ox, oz, sin s', cos s', -, -): origin, steering after    */
+/*               the speed-of-sound correction s' = asin(cm sin s / ctx)   */
+/*   diverging   (ox, oz, -, -, tau0, -): source and its reference delay   */
+/*   focused     (ox, oz, nx, nz, t0tx, alatx): the synthetic-point fields */
+/* xele (nele), xout (nx), zout (nz): device float64.  Outputs (device     */
+/* float32): tautx, apodtx (ntx, np); taurx, apodrx (nele, np).  Every     */
+/* value is computed in float64 in NumPy's order of operations, without    */
+/* fused multiply-adds, then rounded to float32.  hann = 1 weights the     */
+/* receive F-number mask by cos^2(pi/2 dx/a), a = z/(2 fnum) (an           */
+/* extension; 0 gives the reference's 0/1 mask).                           */
+/* ---------------------------------------------------------------------- */
+int pycbf_gb_tables_2d(int txkind, int ntx, const double *tx_params, int nele,
+                       const double *xele, int nx, const double *xout, int nz,
+                       const double *zout, double cm, double fnum, int hann, float *tautx,
+                       float *apodtx, float *taurx, float *apodrx, void *stream);
+
+/* ---------------------------------------------------------------------- */
 /* Synthetic-point delay-and-sum: delays and masks computed per pixel on   */
 /* the fly.  Replaces das_bmode_synthetic_korder_cubic /                   */
 /* das_bmode_synthetic_multi_interp (pycbf/gpu/__engines__.cu:506-694,     */

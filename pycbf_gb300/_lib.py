@@ -33,7 +33,7 @@ EXPORTS = (
     "pycbf_gb_das_synthetic_adjoint", "pycbf_gb_batch_plan_bytes", "pycbf_gb_batch_plan",
     "pycbf_gb_batch_run", "pycbf_gb_upsampled_bytes", "pycbf_gb_upsample",
     "pycbf_gb_poly_workspace_bytes", "pycbf_gb_poly_coefficients", "pycbf_gb_das_tabbed_poly",
-    "pycbf_gb_das_synthetic_poly",
+    "pycbf_gb_das_synthetic_poly", "pycbf_gb_tables_2d",
 )
 NOALLOC_SCRATCH_BYTES = 64 << 20
 
@@ -133,6 +133,8 @@ def load() -> ct.CDLL:
                                                vp]
         L.pycbf_gb_das_synthetic_poly.argtypes = [P(RFInfo), vp, i, P(SyntheticGeom), vp, i, vp,
                                                   vp]
+        d = ct.c_double
+        L.pycbf_gb_tables_2d.argtypes = [i, i, vp, i, vp, i, vp, i, vp, d, d, i, vp, vp, vp, vp, vp]
         for name in EXPORTS:
             if name not in ("pycbf_gb_abi_version", "pycbf_gb_status_string",
                             "pycbf_gb_last_cuda_error", "pycbf_gb_workspace_bytes",

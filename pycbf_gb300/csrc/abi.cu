@@ -786,3 +786,33 @@ int pycbf_gb_das_synthetic_poly(const pycbf_gb_rfinfo *rf, const void *coef, int
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// delay tables of a linear array on a grid
+// ---------------------------------------------------------------------------
+extern "C" int pycbf_gb_tables_2d(int txkind, int ntx, const double *tx_params, int nele,
+                                  const double *xele, int nx, const double *xout, int nz,
+                                  const double *zout, double cm, double fnum, int hann,
+                                  float *tautx, float *apodtx, float *taurx, float *apodrx,
+                                  void *stream) {
+    if (txkind < 0 || txkind > 2 || !tx_params || !xele || !xout || !zout || !tautx || !apodtx ||
+        !taurx || !apodrx)
+        return PYCBF_GB_EINVAL;
+    if (ntx <= 0 || nele <= 0 || nx <= 0 || nz <= 0 || !std::isfinite(cm) || cm <= 0.0 ||
+        !std::isfinite(fnum) || fnum <= 0.0)
+        return PYCBF_GB_EINVAL;
+    if (ntx > kTables2DMaxTx || (long long)nx * nz >= (1LL << 31)) return PYCBF_GB_ERANGE;
+    Tables2D p = {};
+    p.txkind = txkind;
+    p.ntx = ntx;
+    p.nele = nele;
+    p.nx = nx;
+    p.nz = nz;
+    p.hann = hann ? 1 : 0;
+    p.cm = cm;
+    p.fnum2 = 2.0 * fnum;
+    for (int t = 0; t < ntx; ++t)
+        for (int k = 0; k < 6; ++k) p.tx[t][k] = tx_params[6 * t + k];
+    return cuda_status(launch_tables_2d(p, xele, xout, zout, tautx, apodtx, taurx, apodrx,
+                                        static_cast<cudaStream_t>(stream)));
+}

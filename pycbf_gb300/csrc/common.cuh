@@ -177,6 +177,20 @@ cudaError_t launch_upsample(const DasArgs &a, int dtype, float *out, long long n
                             float dtu, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
+// delay tables of a linear array on a grid (tables.cu)
+// ---------------------------------------------------------------------------
+constexpr int kTables2DMaxTx = 256;
+struct Tables2D {
+    int txkind;                      // 0 plane wave, 1 diverging, 2 focused
+    int ntx, nele, nx, nz, hann;
+    double cm, fnum2;                // speed of sound, 2 * f-number
+    double tx[kTables2DMaxTx][6];    // per transmit: ox, oz, nx, nz, t0 (tau0 / t0tx), ala
+};
+cudaError_t launch_tables_2d(const Tables2D &p, const double *xele, const double *xout,
+                             const double *zout, float *tautx, float *apodtx, float *taurx,
+                             float *apodrx, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
 // uneven batches: one frame of one beamformer per job, all in one launch
 // ---------------------------------------------------------------------------
 struct BatchJob {
