@@ -381,7 +381,44 @@ def run_variants(a, w, dev, taps):
     res.update(run_adjoint_variants(a, w, dev, taps))
     res.update(run_batch_variants(a, dev))
     res.update(run_synthetic_variants(a, dev))
+    res.update(run_table_variant(a, dev))
     return res
+
+
+def run_table_variant(a, dev):
+    """The workload's tables (11 plane waves, 128 elements, 256 x 512 pixels,
+    Hann-weighted F#1.5 receive mask) built on the GPU, against the same
+    float64 NumPy build on the host plus its copy to the device."""
+    import numpy as np
+    import torch
+
+    from pycbf_gb300 import helpers
+    from pycbf_gb300.tables import make_tabs_and_apods_2d
+    xele = helpers.element_positions(128, 0.3e-3)
+    steers = np.radians(np.linspace(-10, 10, 11))
+    xout, zout = np.linspace(-19e-3, 19e-3, 256), np.linspace(5e-3, 45e-3, 512)
+    build = lambda: make_tabs_and_apods_2d(steers, 0.0, 1540.0, 1540.0, xele, xout, zout, 1.5,
+                                           hann=True, device=dev)
+    build()
+    stream = torch.cuda.current_stream()
+    times = []
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        build()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    t = time.perf_counter()
+    tx, _ = helpers.pw_tx_tables(steers, 1540.0, 1540.0, xele, xout, zout)
+    rx, ap = helpers.rx_tables(1540.0, xele, xout, zout, 1.5, hann=True)
+    host = [torch.as_tensor(v.astype(np.float32)).to(dev) for v in (tx, rx, ap)]
+    torch.cuda.synchronize()
+    host_s = time.perf_counter() - t
+    nbytes = 4 * (2 * 11 + 2 * 128) * 256 * 512
+    return {"tables_c1": {"gpu_ms": statistics.median(times), "host_numpy_and_copy_ms": 1e3 * host_s,
+                          "table_bytes": nbytes,
+                          "gpu_write_gbs": nbytes / (statistics.median(times) * 1e-3) / 1e9}}
 
 
 def _synthetic(cls, w, **kw):

@@ -31,7 +31,7 @@ size_t dtype_bytes(int dtype) {
 
 // Largest sample count the nearest-neighbour rounding handles exactly in float.
 constexpr int kMaxNt = 1 << 22;
-constexpr int kMaxNtSpline = 18000;  // three shared-memory copies of a channel per warp (216 KB)
+constexpr int kMaxNtSpline = 18000;  // two shared-memory copies of a channel per warp (144 KB)
 
 int check_rf(const pycbf_gb_rfinfo *rf, bool synthetic) {
     if (!rf) return PYCBF_GB_EINVAL;

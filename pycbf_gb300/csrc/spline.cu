@@ -34,7 +34,9 @@ void make_spline_table(SplineTable *t) {
 }
 
 // One channel by one warp: src (nt samples) -> dst (nt records); smem holds
-// three arrays of (nt + 4) & ~3 floats.
+// two arrays of (nt + 4) & ~3 floats: the channel, and u overwritten in place
+// by z (each lane first runs its back-substitution warm-up over the next
+// lanes' u, then all lanes overwrite their own chunks).
 template <typename T>
 __device__ __forceinline__ void spline_channel(const T *__restrict__ src,
                                                typename CoefRec<T>::raw *__restrict__ dst, int nt,
@@ -42,8 +44,7 @@ __device__ __forceinline__ void spline_channel(const T *__restrict__ src,
     const int lane = threadIdx.x & 31;
     const int stride = (nt + 4) & ~3;  // >= nt+1, keeps every array 16-byte aligned
     float *y = smem;
-    float *u = y + stride;
-    float *z = u + stride;
+    float *uz = y + stride;  // u, then z
 
     // stage the channel: 16-byte vector loads, several in flight per lane
     constexpr int V = 16 / sizeof(T);
@@ -61,9 +62,9 @@ __device__ __forceinline__ void spline_channel(const T *__restrict__ src,
     }
     if (lane == 0) {
         y[nt] = 0.f;
-        u[0] = 0.f;
-        z[nt] = 0.f;
-        z[nt - 1] = 0.f;
+        uz[0] = 0.f;
+        uz[nt] = 0.f;
+        uz[nt - 1] = 0.f;
     }
     __syncwarp();
 
@@ -84,27 +85,29 @@ __device__ __forceinline__ void spline_channel(const T *__restrict__ src,
                 const float d1 = (y[i + 1] - y[i]) * inv_dt;
                 const float d0 = (y[i] - y[i - 1]) * inv_dt;
                 const float ui = fmaf(d1 - d0, cscale, -0.5f * up) * tab.invp[min(i, kSplineTab - 1)];
-                if (i >= ib) u[i] = ui;
+                if (i >= ib) uz[i] = ui;
                 up = ui;
             }
         }
     }
     __syncwarp();
-    // back-substitution: y2_k for k in [s, min(e, nt-1)), y2_{nt-1} = 0
-    {
-        const int kb = s, ke = min(e, nt - 1);
-        if (kb < ke) {
-            float yn = 0.f;
-            for (int k = min(nt - 2, ke - 1 + kWarm); k >= kb; --k) {
-                const float uk = (k == 0) ? 0.f : u[k];
-                const float y2k = fmaf(tab.c[min(k, kSplineTab - 1)], yn, uk);
-                if (k < ke) z[k] = y2k * zscale;
-                yn = y2k;
-            }
-        }
-    }
+    // back-substitution: y2_k for k in [s, min(e, nt-1)), y2_{nt-1} = 0; the
+    // warm-up over the next lanes' u first, then this lane's chunk in place
+    const int kb = s, ke = min(e, nt - 1);
+    float yn = 0.f;
+    if (kb < ke)
+        for (int k = min(nt - 2, ke - 1 + kWarm); k >= ke; --k)
+            yn = fmaf(tab.c[min(k, kSplineTab - 1)], yn, uz[k]);
     __syncwarp();
-    for (int k = lane; k < nt; k += 32) dst[k] = CoefRec<T>::pack(y[k], y[k + 1], z[k], z[k + 1]);
+    if (kb < ke)
+        for (int k = ke - 1; k >= kb; --k) {
+            const float uk = (k == 0) ? 0.f : uz[k];
+            const float y2k = fmaf(tab.c[min(k, kSplineTab - 1)], yn, uk);
+            uz[k] = y2k * zscale;
+            yn = y2k;
+        }
+    __syncwarp();
+    for (int k = lane; k < nt; k += 32) dst[k] = CoefRec<T>::pack(y[k], y[k + 1], uz[k], uz[k + 1]);
 }
 
 template <typename T>
@@ -118,7 +121,7 @@ spline_coef_kernel(const T *__restrict__ rf, typename CoefRec<T>::raw *__restric
     if (ch >= nch) return;
     const int stride = (nt + 4) & ~3;
     spline_channel<T>(rf + ch * (long long)nt, coef + ch * (long long)nt, nt, dt, tab,
-                      smem + (size_t)w * 3 * stride);
+                      smem + (size_t)w * 2 * stride);
 }
 
 // Batched: one warp per channel of any job (jobs' channels numbered
@@ -150,7 +153,7 @@ batch_spline_kernel(const BatchJob *__restrict__ jobs, int njobs, long long nch_
     }
     const BatchJob &j = jobs[lo];
     const long long ch = gc - j.ch0;
-    float *sm = smem + (size_t)w * 3 * max_stride;
+    float *sm = smem + (size_t)w * 2 * max_stride;
     switch (j.dtype) {
         case PYCBF_GB_F32: batch_spline_one<float>(j, ch, sm, tab); break;
         case PYCBF_GB_F16: batch_spline_one<__half>(j, ch, sm, tab); break;
@@ -160,8 +163,8 @@ batch_spline_kernel(const BatchJob *__restrict__ jobs, int njobs, long long nch_
 
 template <typename T>
 static cudaError_t launch_spline_t(const SplineArgs &a, cudaStream_t s) {
-    const size_t per_warp = sizeof(float) * 3 * (size_t)((a.nt + 4) & ~3);
-    int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (96 * 1024) / per_warp));
+    const size_t per_warp = sizeof(float) * 2 * (size_t)((a.nt + 4) & ~3);
+    int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (72 * 1024) / per_warp));
     const size_t smem = per_warp * wpb;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     static SplineTable tab = [] {
@@ -183,8 +186,8 @@ static cudaError_t launch_spline_t(const SplineArgs &a, cudaStream_t s) {
 cudaError_t launch_batch_spline(const BatchJob *jobs, int njobs, long long nch_total, int max_nt,
                                 cudaStream_t s, bool set_attr) {
     const int stride = (max_nt + 4) & ~3;
-    const size_t per_warp = sizeof(float) * 3 * (size_t)stride;
-    const int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (96 * 1024) / per_warp));
+    const size_t per_warp = sizeof(float) * 2 * (size_t)stride;
+    const int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (72 * 1024) / per_warp));
     const size_t smem = per_warp * wpb;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     static SplineTable tab = [] {
