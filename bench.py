@@ -321,6 +321,9 @@ def main_ours(a):
     variants = {}
     if not a.no_variants:
         variants = run_variants(a, w, dev, taps)
+        for k in ("demod_c1", "demod_512x1024"):
+            if k in variants:
+                variants[k]["iq_fp32_frac"] = variants[k]["iq_tflops"] / fp32_peak
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
@@ -382,6 +385,45 @@ def run_variants(a, w, dev, taps):
     res.update(run_batch_variants(a, dev))
     res.update(run_synthetic_variants(a, dev))
     res.update(run_table_variant(a, dev))
+    res.update(run_demod_variant(a, dev))
+    return res
+
+
+def run_demod_variant(a, dev):
+    """IQ demodulation of beamformed images (the examples' fft_tukey_demod,
+    1-9 MHz band, Tukey 0.25) and the B-mode display chain (envelope,
+    99th percentile, log compression), on the 256 x 512 image of the
+    workload's grid (z 5..45 mm) and on a 512 x 1024 image of the same extent.
+    FLOPs: 4 per (line, input sample, output sample) of the complex matrix."""
+    import numpy as np
+    import torch
+
+    from pycbf_gb300.demod import Demodulator
+    res = {}
+    stream = torch.cuda.current_stream()
+    for name, nx, nz in (("demod_c1", 256, 512), ("demod_512x1024", 512, 1024)):
+        dz = 40e-3 / (nz - 1)
+        d = Demodulator(nz, 2 * 1e6 / 1540.0, 2 * 9e6 / 1540.0, 1 / dz)
+        img = torch.as_tensor(np.random.default_rng(nz).standard_normal((nx, nz)).astype(np.float32),
+                              device=dev)
+        t = {}
+        for what, fn in (("iq", lambda: d.iq(img)), ("bmode", lambda: d.bmode(img))):
+            for _ in range(3):
+                fn()
+            ms = []
+            for _ in range(10):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            t[what] = statistics.median(ms)
+        flops = 4 * nx * nz * d.M
+        res[name] = {"iq_us": 1e3 * t["iq"], "bmode_us": 1e3 * t["bmode"], "lines": nx,
+                     "samples_in": nz, "samples_out": d.M, "flops": flops,
+                     "iq_tflops": flops / (t["iq"] * 1e-3) / 1e12,
+                     "launches_bmode": 7}
     return res
 
 

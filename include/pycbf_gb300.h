@@ -431,6 +431,39 @@ int pycbf_gb_batch_run(const void *plan, const pycbf_gb_batch_info *info, int tx
 /* ---------------------------------------------------------------------- */
 int pycbf_gb_fp32_probe(float *out, int blocks, int iters, void *stream);
 
+/* ---------------------------------------------------------------------- */
+/* IQ demodulation, envelope and log compression of beamformed images (the */
+/* step after the path).  Replaces the examples' fft_tukey_demod           */
+/* (examples/SyntheticPointBeamforming.ipynb cell 1; the same function in  */
+/* SyntheticVsTabbed.ipynb cell 1, develop_dmas_class.ipynb cell 7), a     */
+/* CuPy rfft -> band slice -> Tukey window -> ifftshift -> ifft chain, and */
+/* their display line 20*log10(env/np.percentile(env, 99) + 1e-10)         */
+/* (SyntheticPointBeamforming.ipynb cell 11).                              */
+/*                                                                         */
+/* pycbf_gb_demod: iq[c][m] = sum_k x[c][k] * W[k][m] for ncols lines of n */
+/* samples (x row-major, device float32); W (n, M) complex, interleaved    */
+/* float32 pairs, the whole FFT chain as one matrix (pycbf_gb300.demod     */
+/* builds it).  iq (ncols, M) complex interleaved and/or env (ncols, M)    */
+/* = |iq|; either may be NULL, not both.                                   */
+/*                                                                         */
+/* pycbf_gb_percentile: out[s] = NumPy's percentile (method 'linear') of   */
+/* segment s of v (nseg segments of n contiguous floats), q in [0, 100];   */
+/* NaN in a segment gives NaN.  The two order statistics are selected      */
+/* exactly.  Workspace: pycbf_gb_percentile_workspace_bytes(nseg) device   */
+/* bytes.  out is device memory.                                            */
+/*                                                                         */
+/* pycbf_gb_log_compress: out[s*n + i] = 20 log10(env[s*n + i] / ref[s] +  */
+/* floor_add), ref in device memory (the percentile's output).  out may    */
+/* alias env.                                                              */
+/* ---------------------------------------------------------------------- */
+int pycbf_gb_demod(const float *x, long long ncols, int n, const float *W, int M, float *iq,
+                   float *env, void *stream);
+size_t pycbf_gb_percentile_workspace_bytes(long long nseg);
+int pycbf_gb_percentile(const float *v, long long nseg, long long n, double q, float *out,
+                        void *workspace, size_t workspace_bytes, void *stream);
+int pycbf_gb_log_compress(const float *env, long long nseg, long long n, const float *ref,
+                          float floor_add, float *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

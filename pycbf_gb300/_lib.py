@@ -33,7 +33,8 @@ EXPORTS = (
     "pycbf_gb_das_synthetic_adjoint", "pycbf_gb_batch_plan_bytes", "pycbf_gb_batch_plan",
     "pycbf_gb_batch_run", "pycbf_gb_upsampled_bytes", "pycbf_gb_upsample",
     "pycbf_gb_poly_workspace_bytes", "pycbf_gb_poly_coefficients", "pycbf_gb_das_tabbed_poly",
-    "pycbf_gb_das_synthetic_poly", "pycbf_gb_tables_2d",
+    "pycbf_gb_das_synthetic_poly", "pycbf_gb_tables_2d", "pycbf_gb_demod",
+    "pycbf_gb_percentile_workspace_bytes", "pycbf_gb_percentile", "pycbf_gb_log_compress",
 )
 NOALLOC_SCRATCH_BYTES = 64 << 20
 
@@ -135,12 +136,18 @@ def load() -> ct.CDLL:
                                                   vp]
         d = ct.c_double
         L.pycbf_gb_tables_2d.argtypes = [i, i, vp, i, vp, i, vp, i, vp, d, d, i, vp, vp, vp, vp, vp]
+        L.pycbf_gb_demod.argtypes = [vp, ll, i, vp, i, vp, vp, vp]
+        L.pycbf_gb_percentile_workspace_bytes.argtypes = [ll]
+        L.pycbf_gb_percentile_workspace_bytes.restype = sz
+        L.pycbf_gb_percentile.argtypes = [vp, ll, ll, d, vp, vp, sz, vp]
+        L.pycbf_gb_log_compress.argtypes = [vp, ll, ll, vp, f, vp, vp]
         for name in EXPORTS:
             if name not in ("pycbf_gb_abi_version", "pycbf_gb_status_string",
                             "pycbf_gb_last_cuda_error", "pycbf_gb_workspace_bytes",
                             "pycbf_gb_tabbed_plan_bytes", "pycbf_gb_adjoint_workspace_bytes",
                             "pycbf_gb_batch_plan_bytes", "pycbf_gb_upsampled_bytes",
-                            "pycbf_gb_poly_workspace_bytes"):
+                            "pycbf_gb_poly_workspace_bytes",
+                            "pycbf_gb_percentile_workspace_bytes"):
                 getattr(L, name).restype = i
         _lib = L
         return L

@@ -816,3 +816,38 @@ extern "C" int pycbf_gb_tables_2d(int txkind, int ntx, const double *tx_params, 
     return cuda_status(launch_tables_2d(p, xele, xout, zout, tautx, apodtx, taurx, apodrx,
                                         static_cast<cudaStream_t>(stream)));
 }
+
+// ---------------------------------------------------------------------------
+// demodulation, envelope, percentile and log compression
+// ---------------------------------------------------------------------------
+extern "C" int pycbf_gb_demod(const float *x, long long ncols, int n, const float *W, int M,
+                              float *iq, float *env, void *stream) {
+    if (!x || !W || (!iq && !env) || ncols < 0 || n <= 0 || M <= 0) return PYCBF_GB_EINVAL;
+    if ((ncols + 31) / 32 > 0x7fffffffLL || ((long long)M + 31) / 32 > 65535) return PYCBF_GB_ERANGE;
+    return cuda_status(launch_demod(x, ncols, n, reinterpret_cast<const float2 *>(W), M,
+                                    reinterpret_cast<float2 *>(iq), env,
+                                    static_cast<cudaStream_t>(stream)));
+}
+
+extern "C" size_t pycbf_gb_percentile_workspace_bytes(long long nseg) {
+    return nseg > 0 ? percentile_workspace_bytes(nseg) : 0;
+}
+
+extern "C" int pycbf_gb_percentile(const float *v, long long nseg, long long n, double q,
+                                   float *out, void *workspace, size_t workspace_bytes,
+                                   void *stream) {
+    if (!v || !out || nseg < 0 || n <= 0 || !(q >= 0.0 && q <= 100.0)) return PYCBF_GB_EINVAL;
+    if (n > 0x7fffffffLL || nseg > 65535) return PYCBF_GB_ERANGE;
+    if (nseg == 0) return PYCBF_GB_OK;
+    if (!workspace || workspace_bytes < percentile_workspace_bytes(nseg)) return PYCBF_GB_EWORKSPACE;
+    return cuda_status(launch_percentile(v, nseg, n, q, out, workspace,
+                                         static_cast<cudaStream_t>(stream)));
+}
+
+extern "C" int pycbf_gb_log_compress(const float *env, long long nseg, long long n,
+                                     const float *ref, float floor_add, float *out, void *stream) {
+    if (!env || !ref || !out || nseg < 0 || n <= 0 || !std::isfinite(floor_add)) return PYCBF_GB_EINVAL;
+    if (nseg > 0 && n > std::numeric_limits<long long>::max() / nseg) return PYCBF_GB_ERANGE;
+    return cuda_status(launch_log_compress(env, nseg, n, ref, floor_add, out,
+                                           static_cast<cudaStream_t>(stream)));
+}

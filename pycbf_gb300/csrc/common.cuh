@@ -247,4 +247,16 @@ cudaError_t launch_dmas(const float *im, long long nframes, long long nsep, long
 cudaError_t launch_slsc(const float *im, const unsigned char *mask, long long nframes, int nrx,
                         int nx, int nz, int nlag, int nkern, float *out, cudaStream_t s);
 
+// ---------------------------------------------------------------------------
+// demodulation, percentile, log compression (demod.cu)
+// ---------------------------------------------------------------------------
+// iq / env: (ncols, M) complex / float, either may be null
+cudaError_t launch_demod(const float *x, long long ncols, int n, const float2 *W, int M,
+                         float2 *iq, float *env, cudaStream_t s);
+size_t percentile_workspace_bytes(long long nseg);
+cudaError_t launch_percentile(const float *v, long long nseg, long long n, double q, float *out,
+                              void *ws, cudaStream_t s);
+cudaError_t launch_log_compress(const float *env, long long nseg, long long n, const float *ref,
+                                float floor_add, float *out, cudaStream_t s);
+
 }  // namespace pgb

@@ -64,11 +64,11 @@ __global__ void __launch_bounds__(256) tables_2d_kernel(const __grid_constant__ 
         tautx[(long long)t * np + i] = __double2float_rn(tau);
         apodtx[(long long)t * np + i] = __double2float_rn(apod);
     }
+    // |dx| - dz / (2 fnum) < 0 (the caller passes 2 fnum); dz = pz for every element
+    const double half = __ddiv_rn(pz, p.fnum2);
     for (int r = 0; r < p.nele; ++r) {
         const double dx = __dsub_rn(px, __ldg(xele + r)), dz = pz;  // elements at z = 0
         taurx[(long long)r * np + i] = __double2float_rn(__ddiv_rn(hyp(dx, dz), p.cm));
-        // |dx| - dz / (2 fnum) < 0 (the caller passes 2 fnum)
-        const double half = __ddiv_rn(dz, p.fnum2);
         const bool inside = __dsub_rn(fabs(dx), half) < 0.0;
         double w = inside ? 1.0 : 0.0;
         if (p.hann && inside) {  // Hann weight across the active aperture (an extension)
