@@ -12,8 +12,8 @@
  *   - keeps no mutable global state, so it is safe to call from several
  *     host threads on distinct outputs.
  *
- * All arithmetic is float32.  Channel data may be stored as float32, float16
- * or bfloat16; delays, weights and sums stay float32.
+ * All arithmetic is float32.  Channel data may be stored as float32, float16,
+ * bfloat16 or int16; delays, weights and sums stay float32.
  */
 #ifndef PYCBF_GB300_H
 #define PYCBF_GB300_H
@@ -36,8 +36,16 @@ enum {
     PYCBF_GB_ECUDA = 5         /* a CUDA call failed: see pycbf_gb_last_cuda_error() */
 };
 
-/* storage type of channel data */
-enum { PYCBF_GB_F32 = 0, PYCBF_GB_F16 = 1, PYCBF_GB_BF16 = 2 };
+/* Channel-data storage types.  PYCBF_GB_I16: int16 samples (raw converter */
+/* counts, as acquisition systems deliver them), converted exactly to      */
+/* float32 by the first kernel that reads them -- inside the spline        */
+/* prefilter for cubic, one conversion pass into the workspace for         */
+/* nearest/linear -- so the host-to-device copy moves 2 bytes a sample.    */
+/* Accepted by pycbf_gb_das_tabbed, pycbf_gb_das_synthetic,                */
+/* pycbf_gb_spline_coefficients (float32 records) and the plan and census  */
+/* calls; other entry points return PYCBF_GB_EUNSUPPORTED (convert first   */
+/* with pycbf_gb_convert_i16).                                             */
+enum { PYCBF_GB_F32 = 0, PYCBF_GB_F16 = 1, PYCBF_GB_BF16 = 2, PYCBF_GB_I16 = 3 };
 
 /* interpolation kinds */
 enum {
@@ -72,7 +80,7 @@ typedef struct pycbf_gb_rfinfo {
     float dt;            /* sample period (tInfo.dx)                               */
     int nt;              /* samples per channel (tInfo.nx)                         */
     long long nframes;
-    int dtype;           /* PYCBF_GB_F32 / _F16 / _BF16                            */
+    int dtype;           /* PYCBF_GB_F32 / _F16 / _BF16 / _I16                     */
 } pycbf_gb_rfinfo;
 
 /* Synthetic-point geometry, all device pointers (float32).  The fields follow
@@ -107,8 +115,8 @@ const char *pycbf_gb_status_string(int status);
 int pycbf_gb_last_cuda_error(void);
 
 /* Bytes of workspace a Tabbed or Synthetic call with this channel data and
- * interpolation kind needs (0 for nearest/linear; the spline coefficients for
- * cubic). */
+ * interpolation kind needs: the spline coefficients for cubic; for
+ * nearest/linear 0, or nframes*ntx*nrx*nt float32 samples for int16 data. */
 size_t pycbf_gb_workspace_bytes(const pycbf_gb_rfinfo *rf, int interp);
 
 /* ---------------------------------------------------------------------- */
@@ -116,8 +124,8 @@ size_t pycbf_gb_workspace_bytes(const pycbf_gb_rfinfo *rf, int interp);
 /* Replaces tie_knots1D_fixed (pycbf/cpu/pycbf.c:114-166), which the      */
 /* reference runs per channel inside beamform_cubic (pycbf.c:194).        */
 /* coef receives, per channel and sample j, (y_j, y_j+1, z_j, z_j+1) with  */
-/* z = y'' dt^2 / 6 and y_nt = z_nt = 0; float32 x4 for F32 channel data,  */
-/* the storage type x4 otherwise.  coef must hold                          */
+/* z = y'' dt^2 / 6 and y_nt = z_nt = 0; float32 x4 for F32 and I16       */
+/* channel data, the storage type x4 otherwise.  coef must hold            */
 /* pycbf_gb_workspace_bytes(rf, PYCBF_GB_INTERP_CUBIC) bytes.              */
 /* ---------------------------------------------------------------------- */
 int pycbf_gb_spline_coefficients(const pycbf_gb_rfinfo *rf, const void *rfdata, void *coef,
@@ -430,6 +438,10 @@ int pycbf_gb_batch_run(const void *plan, const pycbf_gb_batch_info *info, int tx
 /* FP32 peak that the benchmark's FP32 roofline fraction divides by.      */
 /* ---------------------------------------------------------------------- */
 int pycbf_gb_fp32_probe(float *out, int blocks, int iters, void *stream);
+
+/* int16 -> float32 on the device (n samples, exact): the conversion the  */
+/* PYCBF_GB_I16 paths fuse, for the entry points that take float data.    */
+int pycbf_gb_convert_i16(const short *src, long long n, float *dst, void *stream);
 
 /* ---------------------------------------------------------------------- */
 /* IQ demodulation, envelope and log compression of beamformed images (the */

@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(HERE, "libpycbf_gb300.so")
 # status codes
 OK, EINVAL, ERANGE, EWORKSPACE, EUNSUPPORTED, ECUDA = range(6)
 # storage types
-F32, F16, BF16 = 0, 1, 2
+F32, F16, BF16, I16 = 0, 1, 2, 3
 # interpolation kinds
 INTERP = {"nearest": 0, "linear": 1, "cubic": 2, "linear_floor": 3, "korder_cubic": 4, "akima": 5,
           "makima": 6}
@@ -35,6 +35,7 @@ EXPORTS = (
     "pycbf_gb_poly_workspace_bytes", "pycbf_gb_poly_coefficients", "pycbf_gb_das_tabbed_poly",
     "pycbf_gb_das_synthetic_poly", "pycbf_gb_tables_2d", "pycbf_gb_demod",
     "pycbf_gb_percentile_workspace_bytes", "pycbf_gb_percentile", "pycbf_gb_log_compress",
+    "pycbf_gb_convert_i16",
 )
 NOALLOC_SCRATCH_BYTES = 64 << 20
 
@@ -141,6 +142,7 @@ def load() -> ct.CDLL:
         L.pycbf_gb_percentile_workspace_bytes.restype = sz
         L.pycbf_gb_percentile.argtypes = [vp, ll, ll, d, vp, vp, sz, vp]
         L.pycbf_gb_log_compress.argtypes = [vp, ll, ll, vp, f, vp, vp]
+        L.pycbf_gb_convert_i16.argtypes = [vp, ll, vp, vp]
         for name in EXPORTS:
             if name not in ("pycbf_gb_abi_version", "pycbf_gb_status_string",
                             "pycbf_gb_last_cuda_error", "pycbf_gb_workspace_bytes",

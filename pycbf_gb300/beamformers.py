@@ -308,10 +308,26 @@ class _GPUBeamformer(Beamformer):
             nframes = int(t.shape[0])
         else:
             raise BeamformerException("txrxt must be 3-D (ntx, nrx, nt) or 4-D (nframes, ntx, nrx, nt)")
+        if t.dtype == torch.int16:
+            # raw converter counts: copied as int16, converted on the device
+            return t.to(device="cuda", non_blocking=True).contiguous(), nframes
         if not (t.is_floating_point()):
-            raise BeamformerException("txrxt must hold floating-point samples")
+            raise BeamformerException("txrxt must hold floating-point or int16 samples")
         t = t.to(device="cuda", dtype=self._torch_dtype, non_blocking=True).contiguous()
         return t, nframes
+
+    def _ingest_i16(self, rf, info):
+        """int16 channel data: passed as PYCBF_GB_I16 where the call converts
+        it itself (nearest/linear/cubic, usf 1, float32 storage), else
+        converted to float32 by pycbf_gb_convert_i16 and cast to the storage."""
+        if self._interp_code <= _lib.INTERP["linear_floor"] and self._usf <= 1 \
+                and self._dtype_code == _lib.F32:
+            info.dtype = _lib.I16
+            return rf
+        f = torch.empty(rf.shape, dtype=torch.float32, device=rf.device)
+        st = self._lib.pycbf_gb_convert_i16(_ptr(rf), rf.numel(), _ptr(f), _stream_ptr())
+        _lib.check(st, "pycbf_gb_convert_i16")
+        return f.to(self._torch_dtype)
 
     def _rfinfo(self, nframes, ndim=0):
         return _lib.RFInfo(self.ntx, self.nrx, ndim, float(np.float32(self.t0)),
@@ -385,6 +401,8 @@ class _GPUBeamformer(Beamformer):
     def _beamform(self, txrxt, buffer=None, sumtype=None):
         rf, nframes = self._prepare_input(txrxt)
         info = self._rfinfo(nframes, getattr(self, "ndimp", 0) if isinstance(self, Synthetic) else 0)
+        if rf.dtype == torch.int16:
+            rf = self._ingest_i16(rf, info)
         out = self._output(self._out_shape(nframes, sumtype), buffer)
         self._launch(rf, info, out, _lib.SUMTYPE[sumtype or self.sumtype])
         return out

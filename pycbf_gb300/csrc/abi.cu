@@ -24,7 +24,8 @@ size_t dtype_bytes(int dtype) {
     switch (dtype) {
         case PYCBF_GB_F32: return 4;
         case PYCBF_GB_F16:
-        case PYCBF_GB_BF16: return 2;
+        case PYCBF_GB_BF16:
+        case PYCBF_GB_I16: return 2;
         default: return 0;
     }
 }
@@ -33,10 +34,12 @@ size_t dtype_bytes(int dtype) {
 constexpr int kMaxNt = 1 << 22;
 constexpr int kMaxNtSpline = 18000;  // two shared-memory copies of a channel per warp (144 KB)
 
-int check_rf(const pycbf_gb_rfinfo *rf, bool synthetic) {
+// i16_ok: the entry point converts int16 channel data itself (or reads none)
+int check_rf(const pycbf_gb_rfinfo *rf, bool synthetic, bool i16_ok = false) {
     if (!rf) return PYCBF_GB_EINVAL;
     if (rf->ntx <= 0 || rf->nrx <= 0 || rf->nt <= 0 || rf->nframes <= 0) return PYCBF_GB_EINVAL;
     if (!dtype_bytes(rf->dtype)) return PYCBF_GB_EINVAL;
+    if (rf->dtype == PYCBF_GB_I16 && !i16_ok) return PYCBF_GB_EUNSUPPORTED;
     if (!std::isfinite(rf->t0) || !std::isfinite(rf->dt) || !(rf->dt > 0.f)) return PYCBF_GB_EINVAL;
     if (synthetic && rf->ndim != 2 && rf->ndim != 3) return PYCBF_GB_EINVAL;
     if (rf->ntx > (1 << 20) || rf->nrx > (1 << 20) || rf->nt >= kMaxNt || rf->nframes > 65535)
@@ -104,10 +107,28 @@ int launch_tabbed(const pycbf_gb_rfinfo *rf, DasArgs &a, int interp, int sumtype
     return cuda_status(launch_das(a, GEOM_TABBED, interp, sumtype, rf->dtype, false, s));
 }
 
+// The data the delay-and-sum gathers from, and its rfinfo (eff): the spline
+// records for cubic, the channels themselves for nearest/linear.  int16
+// channels come out as float32: converted inside the prefilter for cubic,
+// by one conversion pass into the workspace otherwise.
 int prepare_data(const pycbf_gb_rfinfo *rf, const void *rfdata, int interp, void *workspace,
-                 size_t workspace_bytes, cudaStream_t s, const void **data) {
+                 size_t workspace_bytes, cudaStream_t s, const void **data,
+                 pycbf_gb_rfinfo *eff) {
+    *eff = *rf;
+    if (rf->dtype == PYCBF_GB_I16) eff->dtype = PYCBF_GB_F32;
     if (interp != PYCBF_GB_INTERP_CUBIC) {
-        *data = rfdata;
+        if (rf->dtype != PYCBF_GB_I16) {
+            *data = rfdata;
+            return PYCBF_GB_OK;
+        }
+        const size_t need = pycbf_gb_workspace_bytes(rf, interp);
+        if (!workspace || workspace_bytes < need) return PYCBF_GB_EWORKSPACE;
+        if (reinterpret_cast<uintptr_t>(workspace) % 16) return PYCBF_GB_EINVAL;
+        const long long n = rf->nframes * rf->ntx * rf->nrx * (long long)rf->nt;
+        int st = cuda_status(launch_convert_i16(static_cast<const short *>(rfdata), n,
+                                                static_cast<float *>(workspace), s));
+        if (st) return st;
+        *data = workspace;
         return PYCBF_GB_OK;
     }
     const size_t need = pycbf_gb_workspace_bytes(rf, interp);
@@ -161,20 +182,26 @@ const char *pycbf_gb_status_string(int status) {
 int pycbf_gb_last_cuda_error(void) { return g_last_cuda_error; }
 
 size_t pycbf_gb_workspace_bytes(const pycbf_gb_rfinfo *rf, int interp) {
-    if (!rf || interp != PYCBF_GB_INTERP_CUBIC) return 0;
-    if (rf->ntx <= 0 || rf->nrx <= 0 || rf->nt <= 0 || rf->nframes <= 0) return 0;
-    const size_t rec = rf->dtype == PYCBF_GB_F32 ? 16 : 8;
-    return (size_t)rf->nframes * (size_t)rf->ntx * (size_t)rf->nrx * (size_t)rf->nt * rec;
+    if (!rf || rf->ntx <= 0 || rf->nrx <= 0 || rf->nt <= 0 || rf->nframes <= 0) return 0;
+    const size_t nsamp = (size_t)rf->nframes * (size_t)rf->ntx * (size_t)rf->nrx * (size_t)rf->nt;
+    const bool f32rec = rf->dtype == PYCBF_GB_F32 || rf->dtype == PYCBF_GB_I16;
+    if (interp == PYCBF_GB_INTERP_CUBIC) return nsamp * (f32rec ? 16 : 8);
+    if (rf->dtype == PYCBF_GB_I16 &&
+        (interp == PYCBF_GB_INTERP_NEAREST || interp == PYCBF_GB_INTERP_LINEAR ||
+         interp == PYCBF_GB_INTERP_LINEAR_FLOOR))
+        return nsamp * sizeof(float);
+    return 0;
 }
 
 int pycbf_gb_spline_coefficients(const pycbf_gb_rfinfo *rf, const void *rfdata, void *coef,
                                  size_t coef_bytes, void *stream) {
-    int st = check_rf(rf, false);
+    int st = check_rf(rf, false, true);
     if (st) return st;
     if (!rfdata) return PYCBF_GB_EINVAL;
     const void *data = nullptr;
+    pycbf_gb_rfinfo eff;
     return prepare_data(rf, rfdata, PYCBF_GB_INTERP_CUBIC, coef, coef_bytes,
-                        static_cast<cudaStream_t>(stream), &data);
+                        static_cast<cudaStream_t>(stream), &data, &eff);
 }
 
 size_t pycbf_gb_tabbed_plan_bytes(long long np, int ntx, int nrx) {
@@ -185,7 +212,7 @@ size_t pycbf_gb_tabbed_plan_bytes(long long np, int ntx, int nrx) {
 int pycbf_gb_tabbed_plan(const pycbf_gb_rfinfo *rf, const float *tautx, const float *apodtx,
                          const float *taurx, const float *apodrx, long long np, int interp,
                          float thresh, void *plan, size_t plan_bytes, void *stream) {
-    int st = check_rf(rf, false);
+    int st = check_rf(rf, false, true);
     if (st) return st;
     if (!tautx || !apodtx || !taurx || !apodrx || !plan) return PYCBF_GB_EINVAL;
     if (np <= 0 || np >= (1LL << 31)) return PYCBF_GB_ERANGE;
@@ -205,7 +232,8 @@ int pycbf_gb_tabbed_plan(const pycbf_gb_rfinfo *rf, const float *tautx, const fl
     a.thresh = thresh;
     st = cuda_status(cudaMemsetAsync(plan, 0, sizeof(int) * 4, s));
     if (st) return st;
-    return cuda_status(launch_tabbed_plan(a, interp, rf->dtype, static_cast<int *>(plan), s));
+    const int gdt = rf->dtype == PYCBF_GB_I16 ? PYCBF_GB_F32 : rf->dtype;  // as gathered
+    return cuda_status(launch_tabbed_plan(a, interp, gdt, static_cast<int *>(plan), s));
 }
 
 int pycbf_gb_das_tabbed(const pycbf_gb_rfinfo *rf, const void *rfdata, const float *tautx,
@@ -213,7 +241,7 @@ int pycbf_gb_das_tabbed(const pycbf_gb_rfinfo *rf, const void *rfdata, const flo
                         long long np, const int *pixel_index, int interp, float thresh,
                         int sumtype, const void *plan, float *out, void *workspace,
                         size_t workspace_bytes, void *stream) {
-    int st = check_rf(rf, false);
+    int st = check_rf(rf, false, true);
     if (st) return st;
     if (!rfdata || !tautx || !apodtx || !taurx || !apodrx || !out) return PYCBF_GB_EINVAL;
     if (np <= 0 || np >= (1LL << 31)) return np == 0 ? PYCBF_GB_OK : PYCBF_GB_ERANGE;
@@ -224,7 +252,8 @@ int pycbf_gb_das_tabbed(const pycbf_gb_rfinfo *rf, const void *rfdata, const flo
     if (!das_shape_ok(GEOM_TABBED, sumtype, rf->ntx)) return PYCBF_GB_ERANGE;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const void *data = nullptr;
-    st = prepare_data(rf, rfdata, interp, workspace, workspace_bytes, s, &data);
+    pycbf_gb_rfinfo eff;
+    st = prepare_data(rf, rfdata, interp, workspace, workspace_bytes, s, &data, &eff);
     if (st) return st;
     DasArgs a = {};
     fill_time_axis(a, rf);
@@ -237,7 +266,7 @@ int pycbf_gb_das_tabbed(const pycbf_gb_rfinfo *rf, const void *rfdata, const flo
     a.out = out;
     a.np = np;
     a.thresh = thresh;
-    return launch_tabbed(rf, a, interp, sumtype, plan, s);
+    return launch_tabbed(&eff, a, interp, sumtype, plan, s);
 }
 
 int pycbf_gb_das_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef,
@@ -245,7 +274,7 @@ int pycbf_gb_das_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef,
                                     const float *apodrx, long long np, const int *pixel_index,
                                     float thresh, int sumtype, const void *plan, float *out,
                                     void *stream) {
-    int st = check_rf(rf, false);
+    int st = check_rf(rf, false, true);
     if (st) return st;
     if (!coef || !tautx || !apodtx || !taurx || !apodrx || !out) return PYCBF_GB_EINVAL;
     if (reinterpret_cast<uintptr_t>(coef) % 16) return PYCBF_GB_EINVAL;
@@ -263,7 +292,9 @@ int pycbf_gb_das_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef,
     a.out = out;
     a.np = np;
     a.thresh = thresh;
-    return launch_tabbed(rf, a, PYCBF_GB_INTERP_CUBIC, sumtype, plan,
+    pycbf_gb_rfinfo eff = *rf;  // int16 channels were prefiltered into float32 records
+    if (rf->dtype == PYCBF_GB_I16) eff.dtype = PYCBF_GB_F32;
+    return launch_tabbed(&eff, a, PYCBF_GB_INTERP_CUBIC, sumtype, plan,
                          static_cast<cudaStream_t>(stream));
 }
 
@@ -271,7 +302,7 @@ int pycbf_gb_das_synthetic(const pycbf_gb_rfinfo *rf, const void *rfdata,
                            const pycbf_gb_synthetic *geo, const int *pixel_index, int interp,
                            int sumtype, float *out, void *workspace, size_t workspace_bytes,
                            void *stream) {
-    int st = check_rf(rf, true);
+    int st = check_rf(rf, true, true);
     if (st) return st;
     if (!rfdata || !out || !geo_ok(geo)) return PYCBF_GB_EINVAL;
     if (interp >= PYCBF_GB_INTERP_KORDER && interp <= PYCBF_GB_INTERP_MAKIMA)
@@ -280,7 +311,8 @@ int pycbf_gb_das_synthetic(const pycbf_gb_rfinfo *rf, const void *rfdata,
     if (!das_shape_ok(GEOM_SYNTH, sumtype, rf->ntx)) return PYCBF_GB_ERANGE;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const void *data = nullptr;
-    st = prepare_data(rf, rfdata, interp, workspace, workspace_bytes, s, &data);
+    pycbf_gb_rfinfo eff;
+    st = prepare_data(rf, rfdata, interp, workspace, workspace_bytes, s, &data, &eff);
     if (st) return st;
     DasArgs a = {};
     fill_time_axis(a, rf);
@@ -291,14 +323,14 @@ int pycbf_gb_das_synthetic(const pycbf_gb_rfinfo *rf, const void *rfdata,
     a.out = out;
     a.np = geo->np;
     a.thresh = 0.01f;
-    return cuda_status(launch_das(a, GEOM_SYNTH, interp, sumtype, rf->dtype, false, s));
+    return cuda_status(launch_das(a, GEOM_SYNTH, interp, sumtype, eff.dtype, false, s));
 }
 
 int pycbf_gb_tap_census_tabbed(const pycbf_gb_rfinfo *rf, const float *tautx,
                                const float *apodtx, const float *taurx, const float *apodrx,
                                long long np, int interp, float thresh, int *count,
                                long long *index_sum, void *stream) {
-    int st = check_rf(rf, false);
+    int st = check_rf(rf, false, true);
     if (st) return st;
     if (!tautx || !apodtx || !taurx || !apodrx || !count || !index_sum) return PYCBF_GB_EINVAL;
     if (np <= 0 || np >= (1LL << 31)) return np == 0 ? PYCBF_GB_OK : PYCBF_GB_ERANGE;
@@ -322,7 +354,7 @@ int pycbf_gb_tap_census_tabbed(const pycbf_gb_rfinfo *rf, const float *tautx,
 
 int pycbf_gb_tap_census_synthetic(const pycbf_gb_rfinfo *rf, const pycbf_gb_synthetic *geo,
                                   int interp, int *count, long long *index_sum, void *stream) {
-    int st = check_rf(rf, true);
+    int st = check_rf(rf, true, true);
     if (st) return st;
     if (!geo_ok(geo) || !count || !index_sum) return PYCBF_GB_EINVAL;
     if (interp < 0 || interp > 6) return PYCBF_GB_EINVAL;
@@ -343,7 +375,7 @@ int pycbf_gb_tap_census_synthetic(const pycbf_gb_rfinfo *rf, const pycbf_gb_synt
 
 int pycbf_gb_synthetic_rx_mask(const pycbf_gb_rfinfo *rf, const pycbf_gb_synthetic *geo,
                                unsigned char *mask, void *stream) {
-    int st = check_rf(rf, true);
+    int st = check_rf(rf, true, true);
     if (st) return st;
     if (!geo_ok(geo) || !mask) return PYCBF_GB_EINVAL;
     DasArgs a = {};
@@ -665,7 +697,8 @@ int pycbf_gb_upsample(const pycbf_gb_rfinfo *rf, const void *rfdata, int usf, vo
     if (out_bytes < pycbf_gb_upsampled_bytes(rf, usf)) return PYCBF_GB_EWORKSPACE;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const void *data = nullptr;
-    st = prepare_data(rf, rfdata, PYCBF_GB_INTERP_CUBIC, workspace, workspace_bytes, s, &data);
+    pycbf_gb_rfinfo eff;
+    st = prepare_data(rf, rfdata, PYCBF_GB_INTERP_CUBIC, workspace, workspace_bytes, s, &data, &eff);
     if (st) return st;
     DasArgs a = {};
     fill_time_axis(a, rf);
@@ -850,4 +883,9 @@ extern "C" int pycbf_gb_log_compress(const float *env, long long nseg, long long
     if (nseg > 0 && n > std::numeric_limits<long long>::max() / nseg) return PYCBF_GB_ERANGE;
     return cuda_status(launch_log_compress(env, nseg, n, ref, floor_add, out,
                                            static_cast<cudaStream_t>(stream)));
+}
+
+extern "C" int pycbf_gb_convert_i16(const short *src, long long n, float *dst, void *stream) {
+    if (!src || !dst || n < 0) return PYCBF_GB_EINVAL;
+    return cuda_status(launch_convert_i16(src, n, dst, static_cast<cudaStream_t>(stream)));
 }

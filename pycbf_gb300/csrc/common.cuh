@@ -24,6 +24,9 @@ __device__ __forceinline__ float load_sample(const __nv_bfloat16 *p) {
 __device__ __forceinline__ float load_sample_reg(float v) { return v; }
 __device__ __forceinline__ float load_sample_reg(__half v) { return __half2float(v); }
 __device__ __forceinline__ float load_sample_reg(__nv_bfloat16 v) { return __bfloat162float(v); }
+// int16 channel data (raw converter counts): exact in float32
+__device__ __forceinline__ float load_sample(const short *p) { return (float)__ldg(p); }
+__device__ __forceinline__ float load_sample_reg(short v) { return (float)v; }
 
 // A spline coefficient record (y_j, y_j+1, z_j, z_j+1): float4 for float32
 // channel data, four 16-bit values packed in a uint2 otherwise.
@@ -36,6 +39,8 @@ template <> struct CoefRec<float> {
         return make_float4(a, b, c, d);
     }
 };
+// int16 channels are prefiltered into float32 records
+template <> struct CoefRec<short> : CoefRec<float> {};
 template <> struct CoefRec<__half> {
     using raw = uint2;
     static __device__ __forceinline__ float4 load(const raw *p) { return unpack(__ldg(p)); }
@@ -246,6 +251,9 @@ cudaError_t launch_dmas(const float *im, long long nframes, long long nsep, long
                         cudaStream_t s);
 cudaError_t launch_slsc(const float *im, const unsigned char *mask, long long nframes, int nrx,
                         int nx, int nz, int nlag, int nkern, float *out, cudaStream_t s);
+
+// int16 channel data -> float32 (spline.cu)
+cudaError_t launch_convert_i16(const short *src, long long n, float *dst, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // demodulation, percentile, log compression (demod.cu)

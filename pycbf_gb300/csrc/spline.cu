@@ -212,8 +212,46 @@ cudaError_t launch_spline(const SplineArgs &a, int dtype, cudaStream_t s) {
         case PYCBF_GB_F32: return launch_spline_t<float>(a, s);
         case PYCBF_GB_F16: return launch_spline_t<__half>(a, s);
         case PYCBF_GB_BF16: return launch_spline_t<__nv_bfloat16>(a, s);
+        case PYCBF_GB_I16: return launch_spline_t<short>(a, s);  // conversion fused into the staging
         default: return cudaErrorInvalidValue;
     }
+}
+
+// int16 -> float32 for the interpolations that gather samples directly:
+// eight samples per thread (one 16-byte load, two 16-byte stores) where the
+// buffers are 16-byte aligned, else one.
+__global__ void __launch_bounds__(256) convert_i16_kernel(const short *__restrict__ src,
+                                                          long long n, float *__restrict__ dst,
+                                                          int vec) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (vec) {
+        const long long n8 = n / 8;
+        for (long long k = i; k < n8; k += stride) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(src) + k);
+            const short *e = reinterpret_cast<const short *>(&v);
+            float4 *d = reinterpret_cast<float4 *>(dst) + 2 * k;
+            d[0] = make_float4(e[0], e[1], e[2], e[3]);
+            d[1] = make_float4(e[4], e[5], e[6], e[7]);
+        }
+        for (long long k = n8 * 8 + i; k < n; k += stride) dst[k] = (float)__ldg(src + k);
+    } else {
+        for (long long k = i; k < n; k += stride) dst[k] = (float)__ldg(src + k);
+    }
+}
+
+cudaError_t launch_convert_i16(const short *src, long long n, float *dst, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int vec = (reinterpret_cast<uintptr_t>(src) % 16 == 0 &&
+                     reinterpret_cast<uintptr_t>(dst) % 16 == 0) ? 1 : 0;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        sms = 148;
+    long long blocks = ((vec ? n / 8 : n) + 255) / 256;
+    blocks = std::max(1LL, std::min(blocks, 8LL * sms));
+    convert_i16_kernel<<<(unsigned)blocks, 256, 0, s>>>(src, n, dst, vec);
+    return cudaGetLastError();
 }
 
 }  // namespace pgb
