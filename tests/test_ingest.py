@@ -133,7 +133,7 @@ def test_synthetic_int16_equals_float_counts(kind):
 def test_convert_kernel_vector_and_scalar_paths():
     import torch
     L = _lib.load()
-    src = torch.randint(-32768, 32767, (1 << 16) + 5, dtype=torch.int16, device="cuda")
+    src = torch.randint(-32768, 32767, ((1 << 16) + 5,), dtype=torch.int16, device="cuda")
     stream = ct.c_void_p(torch.cuda.current_stream().cuda_stream)
     for off in (0, 1, 3):      # 16-byte aligned, and two misaligned starts
         s = src[off:]
