@@ -467,6 +467,11 @@ int pycbf_gb_convert_i16(const short *src, long long n, float *dst, void *stream
 /* pycbf_gb_log_compress: out[s*n + i] = 20 log10(env[s*n + i] / ref[s] +  */
 /* floor_add), ref in device memory (the percentile's output).  out may    */
 /* alias env.                                                              */
+/*                                                                         */
+/* pycbf_gb_log_compress_percentile: both -- ref[s] = the q-th percentile  */
+/* of segment s, out its log compression -- in one launch per call for     */
+/* segments of up to 2^18 values (one CTA per segment).  Workspace as for  */
+/* pycbf_gb_percentile; out may alias env.                                 */
 /* ---------------------------------------------------------------------- */
 int pycbf_gb_demod(const float *x, long long ncols, int n, const float *W, int M, float *iq,
                    float *env, void *stream);
@@ -475,6 +480,9 @@ int pycbf_gb_percentile(const float *v, long long nseg, long long n, double q, f
                         void *workspace, size_t workspace_bytes, void *stream);
 int pycbf_gb_log_compress(const float *env, long long nseg, long long n, const float *ref,
                           float floor_add, float *out, void *stream);
+int pycbf_gb_log_compress_percentile(const float *env, long long nseg, long long n, double q,
+                                     float floor_add, float *out, float *ref, void *workspace,
+                                     size_t workspace_bytes, void *stream);
 
 #ifdef __cplusplus
 }

@@ -856,7 +856,7 @@ extern "C" int pycbf_gb_tables_2d(int txkind, int ntx, const double *tx_params, 
 extern "C" int pycbf_gb_demod(const float *x, long long ncols, int n, const float *W, int M,
                               float *iq, float *env, void *stream) {
     if (!x || !W || (!iq && !env) || ncols < 0 || n <= 0 || M <= 0) return PYCBF_GB_EINVAL;
-    if ((ncols + 31) / 32 > 0x7fffffffLL || ((long long)M + 31) / 32 > 65535) return PYCBF_GB_ERANGE;
+    if ((ncols + 15) / 16 > 0x7fffffffLL || ((long long)M + 31) / 32 > 65535) return PYCBF_GB_ERANGE;
     return cuda_status(launch_demod(x, ncols, n, reinterpret_cast<const float2 *>(W), M,
                                     reinterpret_cast<float2 *>(iq), env,
                                     static_cast<cudaStream_t>(stream)));
@@ -875,6 +875,20 @@ extern "C" int pycbf_gb_percentile(const float *v, long long nseg, long long n, 
     if (!workspace || workspace_bytes < percentile_workspace_bytes(nseg)) return PYCBF_GB_EWORKSPACE;
     return cuda_status(launch_percentile(v, nseg, n, q, out, workspace,
                                          static_cast<cudaStream_t>(stream)));
+}
+
+extern "C" int pycbf_gb_log_compress_percentile(const float *env, long long nseg, long long n,
+                                                double q, float floor_add, float *out, float *ref,
+                                                void *workspace, size_t workspace_bytes,
+                                                void *stream) {
+    if (!env || !out || !ref || nseg < 0 || n <= 0 || !(q >= 0.0 && q <= 100.0) ||
+        !std::isfinite(floor_add))
+        return PYCBF_GB_EINVAL;
+    if (n > 0x7fffffffLL || nseg > 65535) return PYCBF_GB_ERANGE;
+    if (nseg == 0) return PYCBF_GB_OK;
+    if (!workspace || workspace_bytes < percentile_workspace_bytes(nseg)) return PYCBF_GB_EWORKSPACE;
+    return cuda_status(launch_percentile(env, nseg, n, q, ref, workspace,
+                                         static_cast<cudaStream_t>(stream), floor_add, out));
 }
 
 extern "C" int pycbf_gb_log_compress(const float *env, long long nseg, long long n,

@@ -262,8 +262,10 @@ cudaError_t launch_convert_i16(const short *src, long long n, float *dst, cudaSt
 cudaError_t launch_demod(const float *x, long long ncols, int n, const float2 *W, int M,
                          float2 *iq, float *env, cudaStream_t s);
 size_t percentile_workspace_bytes(long long nseg);
+// out (nseg, device): the percentiles; logout (optional): the log compression of v with them
 cudaError_t launch_percentile(const float *v, long long nseg, long long n, double q, float *out,
-                              void *ws, cudaStream_t s);
+                              void *ws, cudaStream_t s, float floor_add = 0.f,
+                              float *logout = nullptr);
 cudaError_t launch_log_compress(const float *env, long long nseg, long long n, const float *ref,
                                 float floor_add, float *out, cudaStream_t s);
 

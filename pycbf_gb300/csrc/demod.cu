@@ -27,60 +27,105 @@ namespace pgb {
 
 namespace {
 
-constexpr int kDmC = 32;        // image lines per CTA
+constexpr int kDmC = 16;        // image lines per CTA
 constexpr int kDmM = 32;        // complex outputs per CTA
-constexpr int kDmK = 32;        // input samples per shared-memory stage
-constexpr int kDmThreads = 128; // 8 x 16 threads, each 4 lines x 2 outputs
+constexpr int kDmK = 32;        // input samples per stage
+constexpr int kDmGroup = 128;   // threads of one K group: 8 x 16, each 2 lines x 2 outputs
+constexpr int kDmGroups = 2;    // K groups per CTA (stages g, g+2, ...), summed at the end
 
-__global__ void __launch_bounds__(kDmThreads) demod_kernel(const float *__restrict__ x,
-                                                           long long ncols, int n,
-                                                           const float2 *__restrict__ W, int M,
-                                                           float2 *__restrict__ iq,
-                                                           float *__restrict__ env) {
-    __shared__ float xs[kDmK][kDmC + 1];  // [k][line]: odd row length, no bank conflicts
-    __shared__ float2 ws[kDmK][kDmM];
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+// Each K group stages its x and W tiles through registers: the next stage's
+// loads are issued before the current stage's products, so their latency
+// hides behind the arithmetic.  The groups' partial sums are added in a fixed
+// order, so the result does not depend on scheduling.
+__global__ void __launch_bounds__(kDmGroup * kDmGroups) demod_kernel(
+    const float *__restrict__ x, long long ncols, int n, const float2 *__restrict__ W, int M,
+    float2 *__restrict__ iq, float *__restrict__ env) {
+    __shared__ float xs[kDmGroups][kDmK][kDmC + 1];  // [k][line]: odd rows, no bank conflicts
+    __shared__ __align__(16) float2 ws[kDmGroups][kDmK][kDmM];
+    const int tid = threadIdx.x, grp = tid / kDmGroup, t = tid % kDmGroup;
+    const int tx = t & 15, ty = t >> 4;
     const long long c0 = (long long)blockIdx.x * kDmC;
     const int m0 = blockIdx.y * kDmM;
-    float2 acc[4][2];
+    const int nst = (n + kDmK - 1) / kDmK;
+    constexpr int XQ = kDmC * kDmK / kDmGroup;  // 4 x values per thread and stage
+    constexpr int WQ = kDmK * kDmM / kDmGroup;  // 8 W values
+    float xr[XQ];
+    float2 wr[WQ];
+    auto fetch = [&](int st) {
+        const int k0 = st * kDmK;
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+        for (int q = 0; q < XQ; ++q) {
+            const int e = t + kDmGroup * q, r = e / kDmK, kk = e % kDmK;
+            const long long c = c0 + r;
+            const int k = k0 + kk;
+            xr[q] = (c < ncols && k < n) ? __ldg(x + c * n + k) : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < WQ; ++q) {
+            const int e = t + kDmGroup * q, kk = e / kDmM, mm = e % kDmM;
+            const int k = k0 + kk, m = m0 + mm;
+            wr[q] = (k < n && m < M) ? __ldg(W + (long long)k * M + m) : make_float2(0.f, 0.f);
+        }
+    };
+    auto group_sync = [&]() {  // named barrier of this group's 128 threads
+        asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "r"(kDmGroup) : "memory");
+    };
+    float2 acc[2][2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
 #pragma unroll
         for (int j = 0; j < 2; ++j) acc[i][j] = make_float2(0.f, 0.f);
 
-    for (int k0 = 0; k0 < n; k0 += kDmK) {
-        for (int e = tid; e < kDmC * kDmK; e += kDmThreads) {
-            const int r = e / kDmK, kk = e % kDmK;
-            const long long c = c0 + r;
-            const int k = k0 + kk;
-            xs[kk][r] = (c < ncols && k < n) ? __ldg(x + c * n + k) : 0.f;
+    int st = grp;
+    if (st < nst) fetch(st);
+    for (; st < nst; st += kDmGroups) {
+#pragma unroll
+        for (int q = 0; q < XQ; ++q) {
+            const int e = t + kDmGroup * q;
+            xs[grp][e % kDmK][e / kDmK] = xr[q];
         }
-        for (int e = tid; e < kDmK * kDmM; e += kDmThreads) {
-            const int kk = e / kDmM, mm = e % kDmM;
-            const int k = k0 + kk, m = m0 + mm;
-            ws[kk][mm] = (k < n && m < M) ? __ldg(W + (long long)k * M + m) : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < WQ; ++q) {
+            const int e = t + kDmGroup * q;
+            ws[grp][e / kDmM][e % kDmM] = wr[q];
         }
-        __syncthreads();
+        group_sync();
+        if (st + kDmGroups < nst) fetch(st + kDmGroups);
 #pragma unroll 8
         for (int kk = 0; kk < kDmK; ++kk) {
-            float a[4];
-            float2 b[2];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = xs[kk][ty + 8 * i];
-#pragma unroll
-            for (int j = 0; j < 2; ++j) b[j] = ws[kk][tx + 16 * j];
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 2; ++j) {
-                    acc[i][j].x = fmaf(a[i], b[j].x, acc[i][j].x);
-                    acc[i][j].y = fmaf(a[i], b[j].y, acc[i][j].y);
-                }
+            const float a0 = xs[grp][kk][ty], a1 = xs[grp][kk][ty + 8];
+            const float2 b0 = ws[grp][kk][tx], b1 = ws[grp][kk][tx + 16];
+            acc[0][0].x = fmaf(a0, b0.x, acc[0][0].x);
+            acc[0][0].y = fmaf(a0, b0.y, acc[0][0].y);
+            acc[0][1].x = fmaf(a0, b1.x, acc[0][1].x);
+            acc[0][1].y = fmaf(a0, b1.y, acc[0][1].y);
+            acc[1][0].x = fmaf(a1, b0.x, acc[1][0].x);
+            acc[1][0].y = fmaf(a1, b0.y, acc[1][0].y);
+            acc[1][1].x = fmaf(a1, b1.x, acc[1][1].x);
+            acc[1][1].y = fmaf(a1, b1.y, acc[1][1].y);
         }
-        __syncthreads();
+        group_sync();
     }
+    __syncthreads();
+    // group 1 hands its partial sums to group 0 through its W tile
+    float4 *red = reinterpret_cast<float4 *>(&ws[1][0][0]);
+    if (grp == 1) {
+        red[2 * t] = make_float4(acc[0][0].x, acc[0][0].y, acc[0][1].x, acc[0][1].y);
+        red[2 * t + 1] = make_float4(acc[1][0].x, acc[1][0].y, acc[1][1].x, acc[1][1].y);
+    }
+    __syncthreads();
+    if (grp != 0) return;
+    const float4 r0 = red[2 * t], r1 = red[2 * t + 1];
+    acc[0][0].x += r0.x;
+    acc[0][0].y += r0.y;
+    acc[0][1].x += r0.z;
+    acc[0][1].y += r0.w;
+    acc[1][0].x += r1.x;
+    acc[1][0].y += r1.y;
+    acc[1][1].x += r1.z;
+    acc[1][1].y += r1.w;
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 2; ++i)
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
             const long long c = c0 + ty + 8 * i;
@@ -232,6 +277,83 @@ __global__ void __launch_bounds__(32) pct_final_kernel(unsigned k0, unsigned k1,
     }
 }
 
+// Segments of up to kPctCtaMax values: one CTA per segment runs the four radix
+// passes with its histograms in shared memory (no workspace, no replays),
+// writes the interpolated percentile to ref[seg] and, when out is given, the
+// segment's log compression with it.  v and out may be the same array.
+constexpr int kPctCta = 1024;
+constexpr long long kPctCtaMax = 1LL << 18;
+
+__global__ void __launch_bounds__(kPctCta) pct_cta_kernel(const float *v, long long n, unsigned k0,
+                                                          unsigned k1, double gamma,
+                                                          float *__restrict__ ref, float floor_add,
+                                                          float *out) {
+    __shared__ unsigned h[2][256];
+    __shared__ unsigned s_pre[2], s_kr[2];
+    __shared__ int s_nan;
+    __shared__ float s_ref;
+    const int tid = threadIdx.x;
+    const long long base = (long long)blockIdx.x * n;
+    const float *vs = v + base;
+    if (tid == 0) {
+        s_pre[0] = s_pre[1] = 0;
+        s_kr[0] = k0;
+        s_kr[1] = k1;
+        s_nan = 0;
+    }
+    for (int pass = 0; pass < 4; ++pass) {
+        if (tid < 512) h[tid >> 8][tid & 255] = 0;
+        __syncthreads();
+        const int shift = 24 - 8 * pass;
+        const unsigned p0 = s_pre[0], p1 = s_pre[1];
+        const bool split = p0 != p1;
+        bool nan_seen = false;
+        for (long long i = tid; i < n; i += kPctCta) {
+            const float val = vs[i];
+            nan_seen |= val != val;
+            const unsigned key = pct_key(val);
+            const unsigned d = (key >> shift) & 255u;
+            if (pass == 0) {
+                atomicAdd(&h[0][d], 1u);
+            } else {
+                const int hi = shift + 8;
+                if ((key >> hi) == (p0 >> hi)) atomicAdd(&h[0][d], 1u);
+                if (split && (key >> hi) == (p1 >> hi)) atomicAdd(&h[1][d], 1u);
+            }
+        }
+        if (__syncthreads_or(nan_seen ? 1 : 0) && tid == 0) s_nan = 1;
+        if (tid < 32) {
+            unsigned kr0 = s_kr[0], kr1 = s_kr[1];
+            const int b0 = warp_pick(h[0], kr0);
+            const int b1 = warp_pick(split ? h[1] : h[0], kr1);
+            if (tid == 0) {
+                s_pre[0] = p0 | ((unsigned)b0 << shift);
+                s_pre[1] = p1 | ((unsigned)b1 << shift);
+                s_kr[0] = kr0;
+                s_kr[1] = kr1;
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        float r;
+        if (s_nan) {
+            r = __int_as_float(0x7fc00000);
+        } else {
+            const double a = pct_value(s_pre[0]), b = pct_value(s_pre[1]);
+            const double d = b - a;
+            r = __double2float_rn((gamma >= 0.5) ? b - d * (1.0 - gamma) : a + d * gamma);
+        }
+        s_ref = r;
+        ref[blockIdx.x] = r;
+    }
+    if (!out) return;
+    __syncthreads();
+    const float r = s_ref;
+    for (long long i = tid; i < n; i += kPctCta)
+        out[base + i] = 20.0f * log10f(__fadd_rn(__fdiv_rn(vs[i], r), floor_add));
+}
+
 // env and out may be the same array (each element is read, then written, by one thread)
 __global__ void __launch_bounds__(256) log_compress_kernel(const float *env, long long nseg,
                                                            long long n,
@@ -261,7 +383,8 @@ cudaError_t launch_demod(const float *x, long long ncols, int n, const float2 *W
     const long long gx = (ncols + kDmC - 1) / kDmC;
     const long long gy = ((long long)M + kDmM - 1) / kDmM;
     if (gx > 0x7fffffffLL || gy > 65535) return cudaErrorInvalidValue;
-    demod_kernel<<<dim3((unsigned)gx, (unsigned)gy), kDmThreads, 0, s>>>(x, ncols, n, W, M, iq, env);
+    demod_kernel<<<dim3((unsigned)gx, (unsigned)gy), kDmGroup * kDmGroups, 0, s>>>(x, ncols, n, W, M,
+                                                                                iq, env);
     return cudaGetLastError();
 }
 
@@ -270,15 +393,20 @@ size_t percentile_workspace_bytes(long long nseg) {
 }
 
 cudaError_t launch_percentile(const float *v, long long nseg, long long n, double q, float *out,
-                              void *ws, cudaStream_t s) {
+                              void *ws, cudaStream_t s, float floor_add, float *logout) {
     if (nseg == 0) return cudaSuccess;
     const double idx = (double)(n - 1) * (q / 100.0);
     const long long lo = (long long)floor(idx);
     const long long k0 = lo < 0 ? 0 : (lo > n - 1 ? n - 1 : lo);
     const long long k1 = k0 + 1 < n ? k0 + 1 : n - 1;
     const double gamma = idx - (double)lo;
-    cudaError_t e = cudaMemsetAsync(ws, 0, percentile_workspace_bytes(nseg), s);
-    if (e != cudaSuccess) return e;
+    cudaError_t e;
+    if (n <= kPctCtaMax) {
+        pct_cta_kernel<<<(unsigned)nseg, kPctCta, 0, s>>>(v, n, (unsigned)k0, (unsigned)k1, gamma, out,
+                                                         floor_add, logout);
+        return cudaGetLastError();
+    }
+    if ((e = cudaMemsetAsync(ws, 0, percentile_workspace_bytes(nseg), s)) != cudaSuccess) return e;
     long long gx = (n + 4095) / 4096;
     const long long want = (4LL * sm_count() + nseg - 1) / nseg;
     if (gx > want) gx = want;
@@ -290,7 +418,8 @@ cudaError_t launch_percentile(const float *v, long long nseg, long long n, doubl
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     pct_final_kernel<<<(unsigned)nseg, 32, 0, s>>>((unsigned)k0, (unsigned)k1, gamma, w, out);
-    return cudaGetLastError();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return logout ? launch_log_compress(v, nseg, n, out, floor_add, logout, s) : cudaSuccess;
 }
 
 cudaError_t launch_log_compress(const float *env, long long nseg, long long n, const float *ref,

@@ -26,7 +26,7 @@ import torch
 from . import _lib
 
 __all__ = ["Demodulator", "fft_tukey_demod", "zout_fft_tukey_demod", "percentile",
-           "log_compress", "tukey", "demod_matrix"]
+           "log_compress", "bmode_compress", "tukey", "demod_matrix"]
 
 
 def _stream():
@@ -123,6 +123,26 @@ def log_compress(env: torch.Tensor, ref: torch.Tensor, floor: float = 1e-10,
     return out
 
 
+def bmode_compress(env: torch.Tensor, q: float = 99.0, floor: float = 1e-10, segments: int = 1,
+                   out: torch.Tensor | None = None):
+    """(20 log10(env / percentile(env, q) + floor), percentiles) per segment,
+    the percentile and the compression in one launch for images of up to
+    2^18 values."""
+    env = _as_cuda_f32(env).contiguous()
+    if segments <= 0 or env.numel() % segments:
+        raise ValueError("env must split into `segments` equal parts")
+    L = _lib.load()
+    ws = torch.empty(max(1, L.pycbf_gb_percentile_workspace_bytes(segments)), dtype=torch.uint8,
+                     device=env.device)
+    ref = torch.empty(segments, dtype=torch.float32, device=env.device)
+    out = torch.empty_like(env) if out is None else out
+    st = L.pycbf_gb_log_compress_percentile(_p(env), segments, env.numel() // segments, float(q),
+                                            float(np.float32(floor)), _p(out), _p(ref), _p(ws),
+                                            ws.numel(), _stream())
+    _lib.check(st, "pycbf_gb_log_compress_percentile")
+    return out, ref
+
+
 class Demodulator:
     """fft_tukey_demod for lines of n samples, its matrix kept on the device.
 
@@ -177,8 +197,7 @@ class Demodulator:
               image_ndim: int | None = None) -> torch.Tensor:
         env = self.envelope(x, axis).contiguous()
         nseg = 1 if image_ndim is None else int(np.prod(env.shape[: env.ndim - image_ndim]))
-        ref = percentile(env, q, nseg)
-        return log_compress(env, ref, floor, out=env)
+        return bmode_compress(env, q, floor, nseg, out=env)[0]
 
 
 _CACHE: "OrderedDict[tuple, Demodulator]" = OrderedDict()

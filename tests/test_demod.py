@@ -115,7 +115,8 @@ def test_gpu_demod_matches_golden(g, case):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n,nseg", [(1, 1), (2, 3), (1000, 1), (4097, 2), (100003, 3)])
+@pytest.mark.parametrize("n,nseg", [(1, 1), (2, 3), (1000, 1), (4097, 2), (100003, 3),
+                                    (300007, 2)])
 def test_gpu_percentile_is_numpys(n, nseg):
     import torch
     rng = np.random.default_rng(n + nseg)
@@ -157,3 +158,19 @@ def test_gpu_bmode_matches_display_line(g):
         want = demod_ref.log_compress(np.abs(g["frames_iq"][f]))
         m = want > -60.0
         assert np.abs(db2[f] - want)[m].max() <= 2e-3
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,nseg", [(5000, 3), (300007, 2)])
+def test_gpu_fused_percentile_and_compression(n, nseg):
+    """The one-launch path (segments up to 2^18 values) and the multi-CTA
+    path give the percentile of pycbf_gb_percentile and the compression of
+    pycbf_gb_log_compress, bit for bit."""
+    import torch
+    rng = np.random.default_rng(n)
+    env = torch.as_tensor(np.abs(rng.standard_normal(n * nseg)).astype(np.float32), device="cuda")
+    out, ref = dm.bmode_compress(env, 99.0, 1e-10, nseg)
+    assert torch.equal(ref, dm.percentile(env, 99.0, nseg))
+    assert torch.equal(out, dm.log_compress(env, ref, 1e-10))
+    want = np.percentile(env.cpu().numpy().reshape(nseg, n).astype(np.float64), 99.0, axis=1)
+    assert np.array_equal(ref.cpu().numpy(), want.astype(np.float32))
