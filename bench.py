@@ -481,7 +481,8 @@ def run_demod_variant(a, dev):
                      "iq_api_us": 1e3 * api["iq"], "bmode_api_us": 1e3 * api["bmode"],
                      "lines": nx, "samples_in": nz, "samples_out": d.M, "flops": flops,
                      "iq_tflops": flops / (t["iq"] * 1e-3) / 1e12,
-                     "launches_bmode": 7, "timing": "CUDA graph replay; *_api_us: eager Python calls"}
+                     "launches_bmode": 2 if nx * d.M <= (1 << 18) else 8,
+                     "timing": "CUDA graph replay; *_api_us: eager Python calls"}
     return res
 
 
