@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--variants", default="all",
+                    help="comma list of secondary groups to run: batch8, adjoint, batch64, "
+                         "synthetic, tables, demod, ingest (default all)")
     ap.add_argument("--pixel-order", default="auto", choices=["auto", "natural"])
     return ap.parse_args()
 
@@ -353,15 +356,15 @@ def run_variants(a, w, dev, taps):
 
     import pycbf_gb300 as pg
     res = {}
+    want = (lambda g: True) if a.variants == "all" else (lambda g: g in a.variants.split(","))
     nfr = 8
     rng = np.random.default_rng(0)
     frames = np.stack([w.rf] + [w.rf * np.float32(rng.uniform(0.5, 1.5)) for _ in range(nfr - 1)])
     stream = torch.cuda.current_stream()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
-    for name, storage, kind, nf in (("fp32_batch8", "float32", "cubic", nfr),
-                                    ("fp16_batch8", "float16", "cubic", nfr),
-                                    ("bf16_batch8", "bfloat16", "cubic", nfr),
-                                    ("nearest_fp32", "float32", "nearest", 1)):
+    batch8 = (("fp32_batch8", "float32", "cubic", nfr), ("fp16_batch8", "float16", "cubic", nfr),
+              ("bf16_batch8", "bfloat16", "cubic", nfr), ("nearest_fp32", "float32", "nearest", 1))
+    for name, storage, kind, nf in batch8 if want("batch8") else ():
         bf = pg.TabbedBeamformer(tautx=w.tautx, taurx=w.taurx, apodtx=w.apodtx, apodrx=w.apodrx,
                                  t0=w.t0, dt=w.dt, nt=w.nt, interp={"kind": kind}, storage=storage)
         x = torch.as_tensor(frames[:nf] if nf > 1 else w.rf, device=dev).to(
@@ -381,12 +384,14 @@ def run_variants(a, w, dev, taps):
         res[name] = {"value": taps * nf / statistics.mean(times), "unit": UNIT,
                      "ms_per_call": 1e3 * statistics.mean(times), "frames_per_call": nf,
                      "storage": storage, "interp": kind}
-    res.update(run_adjoint_variants(a, w, dev, taps))
-    res.update(run_batch_variants(a, dev))
-    res.update(run_synthetic_variants(a, dev))
-    res.update(run_table_variant(a, dev))
-    res.update(run_demod_variant(a, dev))
-    res.update(run_ingest_variant(a, w, dev, taps))
+    for group, fn in (("adjoint", lambda: run_adjoint_variants(a, w, dev, taps)),
+                      ("batch64", lambda: run_batch_variants(a, dev)),
+                      ("synthetic", lambda: run_synthetic_variants(a, dev)),
+                      ("tables", lambda: run_table_variant(a, dev)),
+                      ("demod", lambda: run_demod_variant(a, dev)),
+                      ("ingest", lambda: run_ingest_variant(a, w, dev, taps))):
+        if want(group):
+            res.update(fn())
     return res
 
 

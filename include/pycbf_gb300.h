@@ -469,9 +469,10 @@ int pycbf_gb_convert_i16(const short *src, long long n, float *dst, void *stream
 /* alias env.                                                              */
 /*                                                                         */
 /* pycbf_gb_log_compress_percentile: both -- ref[s] = the q-th percentile  */
-/* of segment s, out its log compression -- in one launch per call for     */
-/* segments of up to 2^18 values (one CTA per segment).  Workspace as for  */
-/* pycbf_gb_percentile; out may alias env.                                 */
+/* of segment s, out its log compression -- in one launch for segments of */
+/* up to 425,984 values (a cluster of 8 CTAs per segment holds it in       */
+/* shared memory).  Workspace as for pycbf_gb_percentile; out may alias    */
+/* env.                                                                    */
 /* ---------------------------------------------------------------------- */
 int pycbf_gb_demod(const float *x, long long ncols, int n, const float *W, int M, float *iq,
                    float *env, void *stream);

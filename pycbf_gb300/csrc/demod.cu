@@ -21,7 +21,11 @@
 // the float bits, both ranks at once), then interpolated in float64 as
 // numpy's _lerp does.  The log compression reads the percentile from device
 // memory, so the chain runs without a host round trip.
+#include <cooperative_groups.h>
+
 #include "common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace pgb {
 
@@ -155,16 +159,13 @@ __device__ __forceinline__ float pct_value(unsigned k) {
     return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
-// One warp: the bin holding rank k (0-based) of the counts h[0..255]; k
-// becomes the rank within that bin.
-__device__ int warp_pick(const unsigned *h, unsigned &k) {
+// One warp: the bin holding rank k (0-based) of 256 counts, lane l holding
+// bins 8l..8l+7 in c; k becomes the rank within that bin.
+__device__ int warp_pick_counts(const unsigned (&c)[8], unsigned &k) {
     const int lane = threadIdx.x & 31;
-    unsigned c[8], s = 0;
+    unsigned s = 0;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        c[i] = h[lane * 8 + i];
-        s += c[i];
-    }
+    for (int i = 0; i < 8; ++i) s += c[i];
     unsigned incl = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -191,6 +192,13 @@ __device__ int warp_pick(const unsigned *h, unsigned &k) {
     below = __shfl_sync(0xffffffffu, below, owner);
     k -= below;
     return bin;
+}
+__device__ int warp_pick(const unsigned *h, unsigned &k) {
+    const int lane = threadIdx.x & 31;
+    unsigned c[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) c[i] = h[lane * 8 + i];
+    return warp_pick_counts(c, k);
 }
 
 // One warp: the key prefixes (the top 8*passes bits) and in-prefix ranks of
@@ -277,12 +285,12 @@ __global__ void __launch_bounds__(32) pct_final_kernel(unsigned k0, unsigned k1,
     }
 }
 
-// Segments of up to kPctCtaMax values: one CTA per segment runs the four radix
+// Small segments: one CTA per segment runs the four radix
 // passes with its histograms in shared memory (no workspace, no replays),
 // writes the interpolated percentile to ref[seg] and, when out is given, the
 // segment's log compression with it.  v and out may be the same array.
 constexpr int kPctCta = 1024;
-constexpr long long kPctCtaMax = 1LL << 18;
+constexpr long long kPctCtaSmall = 8192;  // one CTA per segment up to this size
 
 __global__ void __launch_bounds__(kPctCta) pct_cta_kernel(const float *v, long long n, unsigned k0,
                                                           unsigned k1, double gamma,
@@ -354,6 +362,102 @@ __global__ void __launch_bounds__(kPctCta) pct_cta_kernel(const float *v, long l
         out[base + i] = 20.0f * log10f(__fadd_rn(__fdiv_rn(vs[i], r), floor_add));
 }
 
+// Segments of up to kCluMaxChunk * kClu values: a cluster of kClu CTAs per
+// segment, each holding a slice in its shared memory for all four passes.
+// After each CTA has counted its slice, every CTA sums the cluster's
+// histograms through distributed shared memory and makes the same pick, so
+// the passes need no global memory and no further launches; the log
+// compression then runs from the resident slices.  Two cluster barriers per
+// pass: one before the histograms are read, one before they are reset.
+constexpr int kClu = 8;
+constexpr int kCluThreads = 1024;
+constexpr long long kCluMaxChunk = 52 * 1024;  // floats per CTA (208 KB)
+
+__global__ void __cluster_dims__(kClu, 1, 1) __launch_bounds__(kCluThreads)
+    pct_cluster_kernel(const float *v, long long n, unsigned k0, unsigned k1, double gamma,
+                       float *__restrict__ ref, float floor_add, float *out) {
+    extern __shared__ float sv[];
+    __shared__ unsigned h[2][256];
+    __shared__ unsigned s_pre[2], s_kr[2];
+    __shared__ int s_nan, s_nan_all;
+    cg::cluster_group cl = cg::this_cluster();
+    const int tid = threadIdx.x;
+    const unsigned rank = cl.block_rank();
+    const long long seg = blockIdx.x / kClu;
+    const long long chunk = (n + kClu - 1) / kClu;
+    const long long lo = (long long)rank * chunk;
+    const int cnt = (int)max(0LL, min(n, lo + chunk) - lo);
+    const long long base = seg * n + lo;
+    bool nan_seen = false;
+    for (int i = tid; i < cnt; i += kCluThreads) {
+        const float x = v[base + i];
+        sv[i] = x;
+        nan_seen |= x != x;
+    }
+    const int any_nan = __syncthreads_or(nan_seen ? 1 : 0);
+    if (tid == 0) {
+        s_nan = any_nan;
+        s_pre[0] = s_pre[1] = 0;
+        s_kr[0] = k0;
+        s_kr[1] = k1;
+    }
+    for (int pass = 0; pass < 4; ++pass) {
+        if (tid < 512) h[tid >> 8][tid & 255] = 0;
+        __syncthreads();
+        const int shift = 24 - 8 * pass;
+        const unsigned p0 = s_pre[0], p1 = s_pre[1];
+        const bool split = p0 != p1;
+        for (int i = tid; i < cnt; i += kCluThreads) {
+            const unsigned key = pct_key(sv[i]);
+            const unsigned d = (key >> shift) & 255u;
+            if (pass == 0) {
+                atomicAdd(&h[0][d], 1u);
+            } else {
+                const int hi = shift + 8;
+                if ((key >> hi) == (p0 >> hi)) atomicAdd(&h[0][d], 1u);
+                if (split && (key >> hi) == (p1 >> hi)) atomicAdd(&h[1][d], 1u);
+            }
+        }
+        cl.sync();  // every slice counted
+        if (tid < 32) {
+            unsigned c0[8] = {}, c1[8] = {};
+            int nan_all = 0;
+            for (unsigned r = 0; r < (unsigned)kClu; ++r) {
+                const unsigned *rh = cl.map_shared_rank(&h[0][0], r);
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    c0[i] += rh[tid * 8 + i];
+                    if (split) c1[i] += rh[256 + tid * 8 + i];
+                }
+                if (pass == 3) nan_all |= *cl.map_shared_rank(&s_nan, r);
+            }
+            unsigned kr0 = s_kr[0], kr1 = s_kr[1];
+            const int b0 = warp_pick_counts(c0, kr0);
+            const int b1 = split ? warp_pick_counts(c1, kr1) : warp_pick_counts(c0, kr1);
+            if (tid == 0) {
+                s_pre[0] = p0 | ((unsigned)b0 << shift);
+                s_pre[1] = p1 | ((unsigned)b1 << shift);
+                s_kr[0] = kr0;
+                s_kr[1] = kr1;
+                if (pass == 3) s_nan_all = nan_all;
+            }
+        }
+        cl.sync();  // every CTA has read the histograms (and s_nan) before they change
+    }
+    float r;
+    if (s_nan_all) {
+        r = __int_as_float(0x7fc00000);
+    } else {
+        const double a = pct_value(s_pre[0]), b = pct_value(s_pre[1]);
+        const double d = b - a;
+        r = __double2float_rn((gamma >= 0.5) ? b - d * (1.0 - gamma) : a + d * gamma);
+    }
+    if (rank == 0 && tid == 0) ref[seg] = r;
+    if (!out) return;
+    for (int i = tid; i < cnt; i += kCluThreads)
+        out[base + i] = 20.0f * log10f(__fadd_rn(__fdiv_rn(sv[i], r), floor_add));
+}
+
 // env and out may be the same array (each element is read, then written, by one thread)
 __global__ void __launch_bounds__(256) log_compress_kernel(const float *env, long long nseg,
                                                            long long n,
@@ -365,6 +469,23 @@ __global__ void __launch_bounds__(256) log_compress_kernel(const float *env, lon
         const float r = __ldg(ref + i / n);
         out[i] = 20.0f * log10f(__fadd_rn(__fdiv_rn(env[i], r), floor_add));
     }
+}
+
+// whether a cluster of kClu CTAs of the cluster kernel fits on this GPU
+bool cluster_ok() {
+    static const bool ok = [] {
+        if (cudaFuncSetAttribute(pct_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(kCluMaxChunk * sizeof(float))) != cudaSuccess)
+            return false;
+        cudaLaunchConfig_t cfg = {};  // the cluster size is the kernel's compile-time one
+        cfg.gridDim = dim3(kClu);
+        cfg.blockDim = dim3(kCluThreads);
+        cfg.dynamicSmemBytes = kCluMaxChunk * sizeof(float);
+        int nclusters = 0;
+        return cudaOccupancyMaxActiveClusters(&nclusters, pct_cluster_kernel, &cfg) == cudaSuccess &&
+               nclusters > 0;
+    }();
+    return ok;
 }
 
 int sm_count() {
@@ -401,9 +522,16 @@ cudaError_t launch_percentile(const float *v, long long nseg, long long n, doubl
     const long long k1 = k0 + 1 < n ? k0 + 1 : n - 1;
     const double gamma = idx - (double)lo;
     cudaError_t e;
-    if (n <= kPctCtaMax) {
+    if (n <= kPctCtaSmall) {
         pct_cta_kernel<<<(unsigned)nseg, kPctCta, 0, s>>>(v, n, (unsigned)k0, (unsigned)k1, gamma, out,
                                                          floor_add, logout);
+        return cudaGetLastError();
+    }
+    if (n <= kCluMaxChunk * kClu && cluster_ok()) {
+        const long long chunk = (n + kClu - 1) / kClu;
+        const int smem = (int)(chunk * sizeof(float));  // within the limit cluster_ok() set
+        pct_cluster_kernel<<<(unsigned)(nseg * kClu), kCluThreads, smem, s>>>(
+            v, n, (unsigned)k0, (unsigned)k1, gamma, out, floor_add, logout);
         return cudaGetLastError();
     }
     if ((e = cudaMemsetAsync(ws, 0, percentile_workspace_bytes(nseg), s)) != cudaSuccess) return e;

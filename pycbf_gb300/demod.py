@@ -127,7 +127,7 @@ def bmode_compress(env: torch.Tensor, q: float = 99.0, floor: float = 1e-10, seg
                    out: torch.Tensor | None = None):
     """(20 log10(env / percentile(env, q) + floor), percentiles) per segment,
     the percentile and the compression in one launch for images of up to
-    2^18 values."""
+    425,984 values (a cluster of 8 CTAs holds each image in shared memory)."""
     env = _as_cuda_f32(env).contiguous()
     if segments <= 0 or env.numel() % segments:
         raise ValueError("env must split into `segments` equal parts")

@@ -116,7 +116,7 @@ def test_gpu_demod_matches_golden(g, case):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("n,nseg", [(1, 1), (2, 3), (1000, 1), (4097, 2), (100003, 3),
-                                    (300007, 2)])
+                                    (300007, 2), (500001, 1)])
 def test_gpu_percentile_is_numpys(n, nseg):
     import torch
     rng = np.random.default_rng(n + nseg)
@@ -161,10 +161,10 @@ def test_gpu_bmode_matches_display_line(g):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n,nseg", [(5000, 3), (300007, 2)])
+@pytest.mark.parametrize("n,nseg", [(5000, 3), (8, 5), (70001, 2), (425984, 1), (500001, 2)])
 def test_gpu_fused_percentile_and_compression(n, nseg):
-    """The one-launch path (segments up to 2^18 values) and the multi-CTA
-    path give the percentile of pycbf_gb_percentile and the compression of
+    """The one-CTA (small), cluster (up to 8 x 52K values) and multi-CTA
+    paths give the percentile of pycbf_gb_percentile and the compression of
     pycbf_gb_log_compress, bit for bit."""
     import torch
     rng = np.random.default_rng(n)
