@@ -35,7 +35,7 @@ constexpr int kDmC = 16;        // image lines per CTA
 constexpr int kDmM = 32;        // complex outputs per CTA
 constexpr int kDmK = 32;        // input samples per stage
 constexpr int kDmGroup = 128;   // threads of one K group: 8 x 16, each 2 lines x 2 outputs
-constexpr int kDmGroups = 2;    // K groups per CTA (stages g, g+2, ...), summed at the end
+constexpr int kDmGroups = 4;    // K groups per CTA (stages g, g+4, ...), summed at the end
 
 // Each K group stages its x and W tiles through registers: the next stage's
 // loads are issued before the current stage's products, so their latency
@@ -111,23 +111,28 @@ __global__ void __launch_bounds__(kDmGroup * kDmGroups) demod_kernel(
         group_sync();
     }
     __syncthreads();
-    // group 1 hands its partial sums to group 0 through its W tile
-    float4 *red = reinterpret_cast<float4 *>(&ws[1][0][0]);
-    if (grp == 1) {
+    // groups 1.. hand their partial sums to group 0 through their W tiles;
+    // group 0 adds them in group order
+    if (grp != 0) {
+        float4 *red = reinterpret_cast<float4 *>(&ws[grp][0][0]);
         red[2 * t] = make_float4(acc[0][0].x, acc[0][0].y, acc[0][1].x, acc[0][1].y);
         red[2 * t + 1] = make_float4(acc[1][0].x, acc[1][0].y, acc[1][1].x, acc[1][1].y);
     }
     __syncthreads();
     if (grp != 0) return;
-    const float4 r0 = red[2 * t], r1 = red[2 * t + 1];
-    acc[0][0].x += r0.x;
-    acc[0][0].y += r0.y;
-    acc[0][1].x += r0.z;
-    acc[0][1].y += r0.w;
-    acc[1][0].x += r1.x;
-    acc[1][0].y += r1.y;
-    acc[1][1].x += r1.z;
-    acc[1][1].y += r1.w;
+#pragma unroll
+    for (int g = 1; g < kDmGroups; ++g) {
+        const float4 *red = reinterpret_cast<const float4 *>(&ws[g][0][0]);
+        const float4 r0 = red[2 * t], r1 = red[2 * t + 1];
+        acc[0][0].x += r0.x;
+        acc[0][0].y += r0.y;
+        acc[0][1].x += r0.z;
+        acc[0][1].y += r0.w;
+        acc[1][0].x += r1.x;
+        acc[1][0].y += r1.y;
+        acc[1][1].x += r1.z;
+        acc[1][1].y += r1.w;
+    }
 #pragma unroll
     for (int i = 0; i < 2; ++i)
 #pragma unroll
@@ -157,6 +162,29 @@ __device__ __forceinline__ unsigned pct_key(float v) {
 }
 __device__ __forceinline__ float pct_value(unsigned k) {
     return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// Counts a key (when valid) into the pass's histograms: rank 0's, and rank
+// 1's once the two prefixes differ.  One shared-memory atomic per distinct
+// bin of the warp (most keys of an image share their top byte, and 32 lanes
+// adding to one bin one by one serialise).  Every lane of the warp calls it.
+__device__ __forceinline__ void count_key(unsigned (*h)[256], unsigned key, bool valid, int pass,
+                                          unsigned p0, unsigned p1, bool split) {
+    const int shift = 24 - 8 * pass;
+    const unsigned d = (key >> shift) & 255u;
+    bool t0 = valid, t1 = false;
+    if (pass > 0) {
+        const int hi = shift + 8;  // 8..24
+        t0 = valid && (key >> hi) == (p0 >> hi);
+        t1 = valid && split && (key >> hi) == (p1 >> hi);
+    }
+    const int lane = threadIdx.x & 31;
+    const unsigned m0 = __match_any_sync(0xffffffffu, t0 ? d : 0x100u);
+    if (t0 && lane == __ffs(m0) - 1) atomicAdd(&h[0][d], (unsigned)__popc(m0));
+    if (split) {  // uniform over the CTA
+        const unsigned m1 = __match_any_sync(0xffffffffu, t1 ? d : 0x100u);
+        if (t1 && lane == __ffs(m1) - 1) atomicAdd(&h[1][d], (unsigned)__popc(m1));
+    }
 }
 
 // One warp: the bin holding rank k (0-based) of 256 counts, lane l holding
@@ -241,24 +269,17 @@ __global__ void __launch_bounds__(256) pct_hist_kernel(const float *__restrict__
         }
     }
     __syncthreads();
-    const int shift = 24 - 8 * pass;
     const unsigned p0 = s_pre[0], p1 = s_pre[1];
     const bool split = s_split != 0;
     const float *vs = v + (long long)blockIdx.y * n;
     bool nan_seen = false;
-    for (long long i = (long long)blockIdx.x * blockDim.x + tid; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
-        const float val = __ldg(vs + i);
+    for (long long i0 = (long long)blockIdx.x * blockDim.x; i0 < n;
+         i0 += (long long)gridDim.x * blockDim.x) {  // i0 uniform: whole warps in count_key
+        const long long i = i0 + tid;
+        const bool valid = i < n;
+        const float val = valid ? __ldg(vs + i) : 0.f;
         nan_seen |= val != val;
-        const unsigned key = pct_key(val);
-        const unsigned d = (key >> shift) & 255u;
-        if (pass == 0) {
-            atomicAdd(&h[0][d], 1u);
-        } else {
-            const int hi = shift + 8;  // 8..24
-            if ((key >> hi) == (p0 >> hi)) atomicAdd(&h[0][d], 1u);
-            if (split && (key >> hi) == (p1 >> hi)) atomicAdd(&h[1][d], 1u);
-        }
+        count_key(h, pct_key(val), valid, pass, p0, p1, split);
     }
     const int any_nan = __syncthreads_or(nan_seen ? 1 : 0);
     if (h[0][tid]) atomicAdd(hs + (pass * 2 + 0) * 256 + tid, h[0][tid]);
@@ -316,18 +337,12 @@ __global__ void __launch_bounds__(kPctCta) pct_cta_kernel(const float *v, long l
         const unsigned p0 = s_pre[0], p1 = s_pre[1];
         const bool split = p0 != p1;
         bool nan_seen = false;
-        for (long long i = tid; i < n; i += kPctCta) {
-            const float val = vs[i];
+        for (long long i0 = 0; i0 < n; i0 += kPctCta) {
+            const long long i = i0 + tid;
+            const bool valid = i < n;
+            const float val = valid ? vs[i] : 0.f;
             nan_seen |= val != val;
-            const unsigned key = pct_key(val);
-            const unsigned d = (key >> shift) & 255u;
-            if (pass == 0) {
-                atomicAdd(&h[0][d], 1u);
-            } else {
-                const int hi = shift + 8;
-                if ((key >> hi) == (p0 >> hi)) atomicAdd(&h[0][d], 1u);
-                if (split && (key >> hi) == (p1 >> hi)) atomicAdd(&h[1][d], 1u);
-            }
+            count_key(h, pct_key(val), valid, pass, p0, p1, split);
         }
         if (__syncthreads_or(nan_seen ? 1 : 0) && tid == 0) s_nan = 1;
         if (tid < 32) {
@@ -407,16 +422,10 @@ __global__ void __cluster_dims__(kClu, 1, 1) __launch_bounds__(kCluThreads)
         const int shift = 24 - 8 * pass;
         const unsigned p0 = s_pre[0], p1 = s_pre[1];
         const bool split = p0 != p1;
-        for (int i = tid; i < cnt; i += kCluThreads) {
-            const unsigned key = pct_key(sv[i]);
-            const unsigned d = (key >> shift) & 255u;
-            if (pass == 0) {
-                atomicAdd(&h[0][d], 1u);
-            } else {
-                const int hi = shift + 8;
-                if ((key >> hi) == (p0 >> hi)) atomicAdd(&h[0][d], 1u);
-                if (split && (key >> hi) == (p1 >> hi)) atomicAdd(&h[1][d], 1u);
-            }
+        for (int i0 = 0; i0 < cnt; i0 += kCluThreads) {
+            const int i = i0 + tid;
+            const bool valid = i < cnt;
+            count_key(h, pct_key(valid ? sv[i] : 0.f), valid, pass, p0, p1, split);
         }
         cl.sync();  // every slice counted
         if (tid < 32) {
