@@ -300,8 +300,13 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt,
         const float x = px[k];
         const float apod = pa[k];
         const float q = pq[k];
-        // |q_fast - q_exact| <= 1.5 ulp(q) <= 1.5 |q| 2^-23; flag within |q| 2^-21
-        const float tol = fmaf(fabsf(q), 4.76837158e-7f, 1e-30f);
+        // q_fast = fl(fl(x - t0) * fl(1/dt)) and q_exact = fl(fl(x - t0) / dt) differ by at
+        // most 3 roundings: |q_fast - q_exact| <= 1.5 |q| 2^-23 (1 + 2^-22).  The floor of a
+        // quotient farther than that from every integer is the floor of q_exact.  Nearest
+        // rounds q + 0.5 once more (the sum's own rounding can move a q within half an ulp
+        // of the boundary across it), so it flags within 4 |q| 2^-23.
+        const float tol = fmaf(fabsf(q), KIND == PYCBF_GB_INTERP_NEAREST ? 4.76837158e-7f : 1.8e-7f,
+                               1e-30f);
         float flk;
         bool inr;
         if (KIND == PYCBF_GB_INTERP_NEAREST) {
@@ -311,7 +316,7 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt,
         } else {
             flk = floorf(q);
             inr = (x >= a.t0) && (x <= a.xmax);
-            nearb |= (q - flk < tol) || (flk + 1.f - q < tol);
+            nearb |= fabsf(q - rintf(q)) < tol;  // distance to the nearest integer (exact)
         }
         xs[k] = x;
         ap[k] = apod;

@@ -39,6 +39,35 @@ def c1_small():
 
 
 @pytest.mark.parametrize("name", CASES)
+def test_staged_decisions_near_boundaries():
+    """The staged kernel's fast quotient and its boundary tolerance, against
+    the global-gather kernel's exact decisions, bit for bit, on delays within
+    a few ulp of every knot and half-knot (random channel data, so a tap at
+    the wrong sample changes the image)."""
+    rng = np.random.default_rng(43)
+    nt, dt, t0 = 512, np.float32(1 / 31.25e6), np.float32(1.3e-6)
+    npx = 8192
+    k = rng.integers(-3, nt + 3, size=npx).astype(np.float32)
+    frac = rng.choice(np.array([0.0, 0.5], np.float32), size=npx)
+    tau = (t0 + dt * (k + frac)).astype(np.float32)
+    ulps = rng.integers(-6, 7, size=npx)
+    for i in range(npx):
+        for _ in range(abs(int(ulps[i]))):
+            tau[i] = np.nextafter(tau[i], np.float32(np.inf if ulps[i] > 0 else -np.inf))
+    nrx = 3
+    case = dict(tautx=tau[None, :].copy(), taurx=np.zeros((nrx, npx), np.float32),
+                apodtx=np.ones((1, npx), np.float32),
+                apodrx=rng.choice(np.array([1, 0.5, -0.25], np.float32), size=(nrx, npx)),
+                t0=t0, dt=dt, nt=nt)
+    rf = rng.normal(size=(1, nrx, nt)).astype(np.float32)
+    for kind in ("cubic", "linear", "nearest"):
+        staged = bf_for(case, kind, pixel_order="natural")
+        plain = bf_for(case, kind, pixel_order="natural", stage_channels=False)
+        assert staged._plan is not None
+        np.testing.assert_array_equal(staged(rf), plain(rf))
+        assert staged.kernel_status() == 0
+
+
 @pytest.mark.parametrize("sumtype", ["tx_and_rx", "tx_only", "rx_only", "none"])
 def test_cubic_vs_reference_golden(golden, name, sumtype):
     case = golden(f"tabbed_{name}.npz")
