@@ -38,7 +38,6 @@ def c1_small():
                 t0=w.t0, dt=w.dt, nt=w.nt)
 
 
-@pytest.mark.parametrize("name", CASES)
 def test_staged_decisions_near_boundaries():
     """The staged kernel's fast quotient and its boundary tolerance, against
     the global-gather kernel's exact decisions, bit for bit, on delays within
@@ -68,6 +67,7 @@ def test_staged_decisions_near_boundaries():
         assert staged.kernel_status() == 0
 
 
+@pytest.mark.parametrize("name", CASES)
 @pytest.mark.parametrize("sumtype", ["tx_and_rx", "tx_only", "rx_only", "none"])
 def test_cubic_vs_reference_golden(golden, name, sumtype):
     case = golden(f"tabbed_{name}.npz")
