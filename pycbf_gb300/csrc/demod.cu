@@ -21,6 +21,8 @@
 // the float bits, both ranks at once), then interpolated in float64 as
 // numpy's _lerp does.  The log compression reads the percentile from device
 // memory, so the chain runs without a host round trip.
+#include <algorithm>
+
 #include <cooperative_groups.h>
 
 #include "common.cuh"
@@ -31,120 +33,137 @@ namespace pgb {
 
 namespace {
 
-constexpr int kDmC = 16;        // image lines per CTA
-constexpr int kDmM = 32;        // complex outputs per CTA
-constexpr int kDmK = 32;        // input samples per stage
-constexpr int kDmGroup = 128;   // threads of one K group: 8 x 16, each 2 lines x 2 outputs
-constexpr int kDmGroups = 4;    // K groups per CTA (stages g, g+4, ...), summed at the end
+constexpr int kDmC = 32;         // image lines per CTA
+constexpr int kDmM = 64;         // complex outputs per CTA
+constexpr int kDmK = 32;         // input samples per stage
+constexpr int kDmThreads = 128;  // 8 x 16 threads, each 4 lines x 4 outputs
+constexpr int kDmXs = kDmC + 4;  // row length of the staged lines: float4 reads, 4-way stores
 
-// Each K group stages its x and W tiles through registers: the next stage's
-// loads are issued before the current stage's products, so their latency
-// hides behind the arithmetic.  The groups' partial sums are added in a fixed
-// order, so the result does not depend on scheduling.
-__global__ void __launch_bounds__(kDmGroup * kDmGroups) demod_kernel(
-    const float *__restrict__ x, long long ncols, int n, const float2 *__restrict__ W, int M,
-    float2 *__restrict__ iq, float *__restrict__ env) {
-    __shared__ float xs[kDmGroups][kDmK][kDmC + 1];  // [k][line]: odd rows, no bank conflicts
-    __shared__ __align__(16) float2 ws[kDmGroups][kDmK][kDmM];
-    const int tid = threadIdx.x, grp = tid / kDmGroup, t = tid % kDmGroup;
-    const int tx = t & 15, ty = t >> 4;
+// A cluster of `split` CTAs (1, 1, split) shares one output tile: rank r sums
+// its contiguous share of the input samples, ranks 1.. hand their partial
+// sums to rank 0 through distributed shared memory, and rank 0 adds them in
+// rank order (the result does not depend on scheduling) and writes the tile.
+// Each CTA stages its x and W tiles through registers: the next stage's loads
+// are issued before the current stage's products.  Per input sample a
+// thread's 32 multiply-adds take three shared-memory loads (4 lines of x as
+// one float4, 4 outputs of W as two).
+__global__ void __launch_bounds__(kDmThreads) demod_kernel(const float *__restrict__ x,
+                                                          long long ncols, int n,
+                                                          const float2 *__restrict__ W, int M,
+                                                          float2 *__restrict__ iq,
+                                                          float *__restrict__ env) {
+    __shared__ __align__(16) float xs[kDmK][kDmXs];
+    __shared__ __align__(16) float2 ws[kDmK][kDmM];
+    cg::cluster_group cl = cg::this_cluster();
+    const int split = (int)gridDim.z, rank = (int)blockIdx.z;  // the cluster spans z
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const long long c0 = (long long)blockIdx.x * kDmC;
     const int m0 = blockIdx.y * kDmM;
     const int nst = (n + kDmK - 1) / kDmK;
-    constexpr int XQ = kDmC * kDmK / kDmGroup;  // 4 x values per thread and stage
-    constexpr int WQ = kDmK * kDmM / kDmGroup;  // 8 W values
+    const int per = (nst + split - 1) / split;
+    const int st0 = rank * per, st1 = min(nst, st0 + per);
+    constexpr int XQ = kDmC * kDmK / kDmThreads;  // 8 x values per thread and stage
+    constexpr int WQ = kDmK * kDmM / kDmThreads;  // 16 W values
     float xr[XQ];
     float2 wr[WQ];
     auto fetch = [&](int st) {
         const int k0 = st * kDmK;
 #pragma unroll
         for (int q = 0; q < XQ; ++q) {
-            const int e = t + kDmGroup * q, r = e / kDmK, kk = e % kDmK;
+            const int e = tid + kDmThreads * q, r = e / kDmK, kk = e % kDmK;
             const long long c = c0 + r;
             const int k = k0 + kk;
             xr[q] = (c < ncols && k < n) ? __ldg(x + c * n + k) : 0.f;
         }
 #pragma unroll
         for (int q = 0; q < WQ; ++q) {
-            const int e = t + kDmGroup * q, kk = e / kDmM, mm = e % kDmM;
+            const int e = tid + kDmThreads * q, kk = e / kDmM, mm = e % kDmM;
             const int k = k0 + kk, m = m0 + mm;
             wr[q] = (k < n && m < M) ? __ldg(W + (long long)k * M + m) : make_float2(0.f, 0.f);
         }
     };
-    auto group_sync = [&]() {  // named barrier of this group's 128 threads
-        asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "r"(kDmGroup) : "memory");
-    };
-    float2 acc[2][2];
+    float2 acc[4][4];
 #pragma unroll
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 2; ++j) acc[i][j] = make_float2(0.f, 0.f);
+        for (int j = 0; j < 4; ++j) acc[i][j] = make_float2(0.f, 0.f);
 
-    int st = grp;
-    if (st < nst) fetch(st);
-    for (; st < nst; st += kDmGroups) {
+    if (st0 < st1) fetch(st0);
+    for (int st = st0; st < st1; ++st) {
 #pragma unroll
         for (int q = 0; q < XQ; ++q) {
-            const int e = t + kDmGroup * q;
-            xs[grp][e % kDmK][e / kDmK] = xr[q];
+            const int e = tid + kDmThreads * q;
+            xs[e % kDmK][e / kDmK] = xr[q];
         }
 #pragma unroll
         for (int q = 0; q < WQ; ++q) {
-            const int e = t + kDmGroup * q;
-            ws[grp][e / kDmM][e % kDmM] = wr[q];
+            const int e = tid + kDmThreads * q;
+            ws[e / kDmM][e % kDmM] = wr[q];
         }
-        group_sync();
-        if (st + kDmGroups < nst) fetch(st + kDmGroups);
-#pragma unroll 8
+        __syncthreads();
+        if (st + 1 < st1) fetch(st + 1);
+#pragma unroll 4
         for (int kk = 0; kk < kDmK; ++kk) {
-            const float a0 = xs[grp][kk][ty], a1 = xs[grp][kk][ty + 8];
-            const float2 b0 = ws[grp][kk][tx], b1 = ws[grp][kk][tx + 16];
-            acc[0][0].x = fmaf(a0, b0.x, acc[0][0].x);
-            acc[0][0].y = fmaf(a0, b0.y, acc[0][0].y);
-            acc[0][1].x = fmaf(a0, b1.x, acc[0][1].x);
-            acc[0][1].y = fmaf(a0, b1.y, acc[0][1].y);
-            acc[1][0].x = fmaf(a1, b0.x, acc[1][0].x);
-            acc[1][0].y = fmaf(a1, b0.y, acc[1][0].y);
-            acc[1][1].x = fmaf(a1, b1.x, acc[1][1].x);
-            acc[1][1].y = fmaf(a1, b1.y, acc[1][1].y);
+            const float4 a = *reinterpret_cast<const float4 *>(&xs[kk][ty * 4]);
+            const float4 b01 = *reinterpret_cast<const float4 *>(&ws[kk][tx * 4]);
+            const float4 b23 = *reinterpret_cast<const float4 *>(&ws[kk][tx * 4 + 2]);
+            const float av[4] = {a.x, a.y, a.z, a.w};
+            const float2 bv[4] = {make_float2(b01.x, b01.y), make_float2(b01.z, b01.w),
+                                  make_float2(b23.x, b23.y), make_float2(b23.z, b23.w)};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    acc[i][j].x = fmaf(av[i], bv[j].x, acc[i][j].x);
+                    acc[i][j].y = fmaf(av[i], bv[j].y, acc[i][j].y);
+                }
         }
-        group_sync();
+        __syncthreads();
     }
-    __syncthreads();
-    // groups 1.. hand their partial sums to group 0 through their W tiles;
-    // group 0 adds them in group order
-    if (grp != 0) {
-        float4 *red = reinterpret_cast<float4 *>(&ws[grp][0][0]);
-        red[2 * t] = make_float4(acc[0][0].x, acc[0][0].y, acc[0][1].x, acc[0][1].y);
-        red[2 * t + 1] = make_float4(acc[1][0].x, acc[1][0].y, acc[1][1].x, acc[1][1].y);
+    if (split > 1) {
+        float4 *mine = reinterpret_cast<float4 *>(&ws[0][0]) + tid * 8;  // 16 complex per thread
+        if (rank > 0) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                mine[2 * i] = make_float4(acc[i][0].x, acc[i][0].y, acc[i][1].x, acc[i][1].y);
+                mine[2 * i + 1] = make_float4(acc[i][2].x, acc[i][2].y, acc[i][3].x, acc[i][3].y);
+            }
+        }
+        cl.sync();  // every partial tile written
+        if (rank == 0) {
+            for (int r = 1; r < split; ++r) {
+                const float4 *rem = cl.map_shared_rank(mine, (unsigned)r);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float4 u = rem[2 * i], v = rem[2 * i + 1];
+                    acc[i][0].x += u.x;
+                    acc[i][0].y += u.y;
+                    acc[i][1].x += u.z;
+                    acc[i][1].y += u.w;
+                    acc[i][2].x += v.x;
+                    acc[i][2].y += v.y;
+                    acc[i][3].x += v.z;
+                    acc[i][3].y += v.w;
+                }
+            }
+        }
+        cl.sync();  // ranks 1.. keep their shared memory until rank 0 has read it
+        if (rank > 0) return;
     }
-    __syncthreads();
-    if (grp != 0) return;
 #pragma unroll
-    for (int g = 1; g < kDmGroups; ++g) {
-        const float4 *red = reinterpret_cast<const float4 *>(&ws[g][0][0]);
-        const float4 r0 = red[2 * t], r1 = red[2 * t + 1];
-        acc[0][0].x += r0.x;
-        acc[0][0].y += r0.y;
-        acc[0][1].x += r0.z;
-        acc[0][1].y += r0.w;
-        acc[1][0].x += r1.x;
-        acc[1][0].y += r1.y;
-        acc[1][1].x += r1.z;
-        acc[1][1].y += r1.w;
-    }
+    for (int i = 0; i < 4; ++i) {
+        const long long c = c0 + ty * 4 + i;
+        if (c >= ncols) continue;
 #pragma unroll
-    for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 2; ++j) {
-            const long long c = c0 + ty + 8 * i;
-            const int m = m0 + tx + 16 * j;
-            if (c < ncols && m < M) {
+        for (int j = 0; j < 4; ++j) {
+            const int m = m0 + tx * 4 + j;
+            if (m < M) {
                 const long long o = c * M + m;
                 if (iq) iq[o] = acc[i][j];
                 if (env) env[o] = sqrtf(fmaf(acc[i][j].x, acc[i][j].x, acc[i][j].y * acc[i][j].y));
             }
         }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -380,10 +399,11 @@ __global__ void __launch_bounds__(kPctCta) pct_cta_kernel(const float *v, long l
 // Segments of up to kCluMaxChunk * kClu values: a cluster of kClu CTAs per
 // segment, each holding a slice in its shared memory for all four passes.
 // After each CTA has counted its slice, every CTA sums the cluster's
-// histograms through distributed shared memory and makes the same pick, so
-// the passes need no global memory and no further launches; the log
-// compression then runs from the resident slices.  Two cluster barriers per
-// pass: one before the histograms are read, one before they are reset.
+// histograms through distributed shared memory (one warp per rank) and makes
+// the same pick, so the passes need no global memory and no further
+// launches; the log compression then runs from the resident slices.  Two
+// cluster barriers per pass: one before the histograms are read, one before
+// they are reset.
 constexpr int kClu = 8;
 constexpr int kCluThreads = 1024;
 constexpr long long kCluMaxChunk = 52 * 1024;  // floats per CTA (208 KB)
@@ -392,7 +412,8 @@ __global__ void __cluster_dims__(kClu, 1, 1) __launch_bounds__(kCluThreads)
     pct_cluster_kernel(const float *v, long long n, unsigned k0, unsigned k1, double gamma,
                        float *__restrict__ ref, float floor_add, float *out) {
     extern __shared__ float sv[];
-    __shared__ unsigned h[2][256];
+    __shared__ unsigned h[2][256];     // this slice's counts, read by the whole cluster
+    __shared__ unsigned hsum[2][256];  // the cluster's counts
     __shared__ unsigned s_pre[2], s_kr[2];
     __shared__ int s_nan, s_nan_all;
     cg::cluster_group cl = cg::this_cluster();
@@ -412,12 +433,16 @@ __global__ void __cluster_dims__(kClu, 1, 1) __launch_bounds__(kCluThreads)
     const int any_nan = __syncthreads_or(nan_seen ? 1 : 0);
     if (tid == 0) {
         s_nan = any_nan;
+        s_nan_all = 0;
         s_pre[0] = s_pre[1] = 0;
         s_kr[0] = k0;
         s_kr[1] = k1;
     }
     for (int pass = 0; pass < 4; ++pass) {
-        if (tid < 512) h[tid >> 8][tid & 255] = 0;
+        if (tid < 512) {
+            h[tid >> 8][tid & 255] = 0;
+            hsum[tid >> 8][tid & 255] = 0;
+        }
         __syncthreads();
         const int shift = 24 - 8 * pass;
         const unsigned p0 = s_pre[0], p1 = s_pre[1];
@@ -428,17 +453,31 @@ __global__ void __cluster_dims__(kClu, 1, 1) __launch_bounds__(kCluThreads)
             count_key(h, pct_key(valid ? sv[i] : 0.f), valid, pass, p0, p1, split);
         }
         cl.sync();  // every slice counted
-        if (tid < 32) {
-            unsigned c0[8] = {}, c1[8] = {};
-            int nan_all = 0;
-            for (unsigned r = 0; r < (unsigned)kClu; ++r) {
-                const unsigned *rh = cl.map_shared_rank(&h[0][0], r);
+        // warp r adds rank r's histograms into this CTA's sums (the remote
+        // reads of the ranks in flight at once, one warp each)
+        if (tid < 32 * kClu) {
+            const int r = tid >> 5, lane = tid & 31;
+            const unsigned *rh = cl.map_shared_rank(&h[0][0], (unsigned)r);
+            unsigned c0[8], c1[8];
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    c0[i] += rh[tid * 8 + i];
-                    if (split) c1[i] += rh[256 + tid * 8 + i];
-                }
-                if (pass == 3) nan_all |= *cl.map_shared_rank(&s_nan, r);
+            for (int i = 0; i < 8; ++i) {
+                c0[i] = rh[lane * 8 + i];
+                c1[i] = split ? rh[256 + lane * 8 + i] : 0u;
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                if (c0[i]) atomicAdd(&hsum[0][lane * 8 + i], c0[i]);
+                if (c1[i]) atomicAdd(&hsum[1][lane * 8 + i], c1[i]);
+            }
+            if (pass == 3 && lane == 0 && *cl.map_shared_rank(&s_nan, (unsigned)r)) s_nan_all = 1;
+        }
+        cl.sync();  // every CTA has read the histograms (and s_nan) before they change
+        if (tid < 32) {
+            unsigned c0[8], c1[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                c0[i] = hsum[0][tid * 8 + i];
+                c1[i] = hsum[1][tid * 8 + i];
             }
             unsigned kr0 = s_kr[0], kr1 = s_kr[1];
             const int b0 = warp_pick_counts(c0, kr0);
@@ -448,10 +487,9 @@ __global__ void __cluster_dims__(kClu, 1, 1) __launch_bounds__(kCluThreads)
                 s_pre[1] = p1 | ((unsigned)b1 << shift);
                 s_kr[0] = kr0;
                 s_kr[1] = kr1;
-                if (pass == 3) s_nan_all = nan_all;
             }
         }
-        cl.sync();  // every CTA has read the histograms (and s_nan) before they change
+        __syncthreads();  // the pick is made before the sums are reset
     }
     float r;
     if (s_nan_all) {
@@ -513,9 +551,23 @@ cudaError_t launch_demod(const float *x, long long ncols, int n, const float2 *W
     const long long gx = (ncols + kDmC - 1) / kDmC;
     const long long gy = ((long long)M + kDmM - 1) / kDmM;
     if (gx > 0x7fffffffLL || gy > 65535) return cudaErrorInvalidValue;
-    demod_kernel<<<dim3((unsigned)gx, (unsigned)gy), kDmGroup * kDmGroups, 0, s>>>(x, ncols, n, W, M,
-                                                                                iq, env);
-    return cudaGetLastError();
+    // split the input samples over a cluster until the grid covers the GPU twice
+    const long long tiles = gx * gy;
+    const int nst = (n + kDmK - 1) / kDmK;
+    int split = (int)std::min<long long>(8, (2LL * sm_count() + tiles - 1) / tiles);
+    split = std::max(1, std::min(split, nst));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)gx, (unsigned)gy, (unsigned)split);
+    cfg.blockDim = dim3(kDmThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = 1;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = (unsigned)split;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, demod_kernel, x, ncols, n, W, M, iq, env);
 }
 
 size_t percentile_workspace_bytes(long long nseg) {
