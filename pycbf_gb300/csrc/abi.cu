@@ -856,7 +856,7 @@ extern "C" int pycbf_gb_tables_2d(int txkind, int ntx, const double *tx_params, 
 extern "C" int pycbf_gb_demod(const float *x, long long ncols, int n, const float *W, int M,
                               float *iq, float *env, void *stream) {
     if (!x || !W || (!iq && !env) || ncols < 0 || n <= 0 || M <= 0) return PYCBF_GB_EINVAL;
-    if ((ncols + 31) / 32 > 0x7fffffffLL || ((long long)M + 63) / 64 > 65535) return PYCBF_GB_ERANGE;
+    if ((ncols + 15) / 16 > 0x7fffffffLL || ((long long)M + 31) / 32 > 65535) return PYCBF_GB_ERANGE;
     return cuda_status(launch_demod(x, ncols, n, reinterpret_cast<const float2 *>(W), M,
                                     reinterpret_cast<float2 *>(iq), env,
                                     static_cast<cudaStream_t>(stream)));

@@ -33,137 +33,120 @@ namespace pgb {
 
 namespace {
 
-constexpr int kDmC = 32;         // image lines per CTA
-constexpr int kDmM = 64;         // complex outputs per CTA
-constexpr int kDmK = 32;         // input samples per stage
-constexpr int kDmThreads = 128;  // 8 x 16 threads, each 4 lines x 4 outputs
-constexpr int kDmXs = kDmC + 4;  // row length of the staged lines: float4 reads, 4-way stores
+constexpr int kDmC = 16;        // image lines per CTA
+constexpr int kDmM = 32;        // complex outputs per CTA
+constexpr int kDmK = 32;        // input samples per stage
+constexpr int kDmGroup = 128;   // threads of one K group: 8 x 16, each 2 lines x 2 outputs
+constexpr int kDmGroups = 4;    // K groups per CTA (stages g, g+4, ...), summed at the end
 
-// A cluster of `split` CTAs (1, 1, split) shares one output tile: rank r sums
-// its contiguous share of the input samples, ranks 1.. hand their partial
-// sums to rank 0 through distributed shared memory, and rank 0 adds them in
-// rank order (the result does not depend on scheduling) and writes the tile.
-// Each CTA stages its x and W tiles through registers: the next stage's loads
-// are issued before the current stage's products.  Per input sample a
-// thread's 32 multiply-adds take three shared-memory loads (4 lines of x as
-// one float4, 4 outputs of W as two).
-__global__ void __launch_bounds__(kDmThreads) demod_kernel(const float *__restrict__ x,
-                                                          long long ncols, int n,
-                                                          const float2 *__restrict__ W, int M,
-                                                          float2 *__restrict__ iq,
-                                                          float *__restrict__ env) {
-    __shared__ __align__(16) float xs[kDmK][kDmXs];
-    __shared__ __align__(16) float2 ws[kDmK][kDmM];
-    cg::cluster_group cl = cg::this_cluster();
-    const int split = (int)gridDim.z, rank = (int)blockIdx.z;  // the cluster spans z
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+// Each K group stages its x and W tiles through registers: the next stage's
+// loads are issued before the current stage's products, so their latency
+// hides behind the arithmetic.  The groups' partial sums are added in a fixed
+// order, so the result does not depend on scheduling.
+__global__ void __launch_bounds__(kDmGroup * kDmGroups) demod_kernel(
+    const float *__restrict__ x, long long ncols, int n, const float2 *__restrict__ W, int M,
+    float2 *__restrict__ iq, float *__restrict__ env) {
+    __shared__ float xs[kDmGroups][kDmK][kDmC + 1];  // [k][line]: odd rows, no bank conflicts
+    __shared__ __align__(16) float2 ws[kDmGroups][kDmK][kDmM];
+    const int tid = threadIdx.x, grp = tid / kDmGroup, t = tid % kDmGroup;
+    const int tx = t & 15, ty = t >> 4;
     const long long c0 = (long long)blockIdx.x * kDmC;
     const int m0 = blockIdx.y * kDmM;
     const int nst = (n + kDmK - 1) / kDmK;
-    const int per = (nst + split - 1) / split;
-    const int st0 = rank * per, st1 = min(nst, st0 + per);
-    constexpr int XQ = kDmC * kDmK / kDmThreads;  // 8 x values per thread and stage
-    constexpr int WQ = kDmK * kDmM / kDmThreads;  // 16 W values
+    constexpr int XQ = kDmC * kDmK / kDmGroup;  // 4 x values per thread and stage
+    constexpr int WQ = kDmK * kDmM / kDmGroup;  // 8 W values
     float xr[XQ];
     float2 wr[WQ];
     auto fetch = [&](int st) {
         const int k0 = st * kDmK;
 #pragma unroll
         for (int q = 0; q < XQ; ++q) {
-            const int e = tid + kDmThreads * q, r = e / kDmK, kk = e % kDmK;
+            const int e = t + kDmGroup * q, r = e / kDmK, kk = e % kDmK;
             const long long c = c0 + r;
             const int k = k0 + kk;
             xr[q] = (c < ncols && k < n) ? __ldg(x + c * n + k) : 0.f;
         }
 #pragma unroll
         for (int q = 0; q < WQ; ++q) {
-            const int e = tid + kDmThreads * q, kk = e / kDmM, mm = e % kDmM;
+            const int e = t + kDmGroup * q, kk = e / kDmM, mm = e % kDmM;
             const int k = k0 + kk, m = m0 + mm;
             wr[q] = (k < n && m < M) ? __ldg(W + (long long)k * M + m) : make_float2(0.f, 0.f);
         }
     };
-    float2 acc[4][4];
+    auto group_sync = [&]() {  // named barrier of this group's 128 threads
+        asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "r"(kDmGroup) : "memory");
+    };
+    float2 acc[2][2];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 2; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = make_float2(0.f, 0.f);
+        for (int j = 0; j < 2; ++j) acc[i][j] = make_float2(0.f, 0.f);
 
-    if (st0 < st1) fetch(st0);
-    for (int st = st0; st < st1; ++st) {
+    int st = grp;
+    if (st < nst) fetch(st);
+    for (; st < nst; st += kDmGroups) {
 #pragma unroll
         for (int q = 0; q < XQ; ++q) {
-            const int e = tid + kDmThreads * q;
-            xs[e % kDmK][e / kDmK] = xr[q];
+            const int e = t + kDmGroup * q;
+            xs[grp][e % kDmK][e / kDmK] = xr[q];
         }
 #pragma unroll
         for (int q = 0; q < WQ; ++q) {
-            const int e = tid + kDmThreads * q;
-            ws[e / kDmM][e % kDmM] = wr[q];
+            const int e = t + kDmGroup * q;
+            ws[grp][e / kDmM][e % kDmM] = wr[q];
         }
-        __syncthreads();
-        if (st + 1 < st1) fetch(st + 1);
-#pragma unroll 4
+        group_sync();
+        if (st + kDmGroups < nst) fetch(st + kDmGroups);
+#pragma unroll 8
         for (int kk = 0; kk < kDmK; ++kk) {
-            const float4 a = *reinterpret_cast<const float4 *>(&xs[kk][ty * 4]);
-            const float4 b01 = *reinterpret_cast<const float4 *>(&ws[kk][tx * 4]);
-            const float4 b23 = *reinterpret_cast<const float4 *>(&ws[kk][tx * 4 + 2]);
-            const float av[4] = {a.x, a.y, a.z, a.w};
-            const float2 bv[4] = {make_float2(b01.x, b01.y), make_float2(b01.z, b01.w),
-                                  make_float2(b23.x, b23.y), make_float2(b23.z, b23.w)};
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    acc[i][j].x = fmaf(av[i], bv[j].x, acc[i][j].x);
-                    acc[i][j].y = fmaf(av[i], bv[j].y, acc[i][j].y);
-                }
+            const float a0 = xs[grp][kk][ty], a1 = xs[grp][kk][ty + 8];
+            const float2 b0 = ws[grp][kk][tx], b1 = ws[grp][kk][tx + 16];
+            acc[0][0].x = fmaf(a0, b0.x, acc[0][0].x);
+            acc[0][0].y = fmaf(a0, b0.y, acc[0][0].y);
+            acc[0][1].x = fmaf(a0, b1.x, acc[0][1].x);
+            acc[0][1].y = fmaf(a0, b1.y, acc[0][1].y);
+            acc[1][0].x = fmaf(a1, b0.x, acc[1][0].x);
+            acc[1][0].y = fmaf(a1, b0.y, acc[1][0].y);
+            acc[1][1].x = fmaf(a1, b1.x, acc[1][1].x);
+            acc[1][1].y = fmaf(a1, b1.y, acc[1][1].y);
         }
-        __syncthreads();
+        group_sync();
     }
-    if (split > 1) {
-        float4 *mine = reinterpret_cast<float4 *>(&ws[0][0]) + tid * 8;  // 16 complex per thread
-        if (rank > 0) {
+    __syncthreads();
+    // groups 1.. hand their partial sums to group 0 through their W tiles;
+    // group 0 adds them in group order
+    if (grp != 0) {
+        float4 *red = reinterpret_cast<float4 *>(&ws[grp][0][0]);
+        red[2 * t] = make_float4(acc[0][0].x, acc[0][0].y, acc[0][1].x, acc[0][1].y);
+        red[2 * t + 1] = make_float4(acc[1][0].x, acc[1][0].y, acc[1][1].x, acc[1][1].y);
+    }
+    __syncthreads();
+    if (grp != 0) return;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                mine[2 * i] = make_float4(acc[i][0].x, acc[i][0].y, acc[i][1].x, acc[i][1].y);
-                mine[2 * i + 1] = make_float4(acc[i][2].x, acc[i][2].y, acc[i][3].x, acc[i][3].y);
-            }
-        }
-        cl.sync();  // every partial tile written
-        if (rank == 0) {
-            for (int r = 1; r < split; ++r) {
-                const float4 *rem = cl.map_shared_rank(mine, (unsigned)r);
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const float4 u = rem[2 * i], v = rem[2 * i + 1];
-                    acc[i][0].x += u.x;
-                    acc[i][0].y += u.y;
-                    acc[i][1].x += u.z;
-                    acc[i][1].y += u.w;
-                    acc[i][2].x += v.x;
-                    acc[i][2].y += v.y;
-                    acc[i][3].x += v.z;
-                    acc[i][3].y += v.w;
-                }
-            }
-        }
-        cl.sync();  // ranks 1.. keep their shared memory until rank 0 has read it
-        if (rank > 0) return;
+    for (int g = 1; g < kDmGroups; ++g) {
+        const float4 *red = reinterpret_cast<const float4 *>(&ws[g][0][0]);
+        const float4 r0 = red[2 * t], r1 = red[2 * t + 1];
+        acc[0][0].x += r0.x;
+        acc[0][0].y += r0.y;
+        acc[0][1].x += r0.z;
+        acc[0][1].y += r0.w;
+        acc[1][0].x += r1.x;
+        acc[1][0].y += r1.y;
+        acc[1][1].x += r1.z;
+        acc[1][1].y += r1.w;
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const long long c = c0 + ty * 4 + i;
-        if (c >= ncols) continue;
+    for (int i = 0; i < 2; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int m = m0 + tx * 4 + j;
-            if (m < M) {
+        for (int j = 0; j < 2; ++j) {
+            const long long c = c0 + ty + 8 * i;
+            const int m = m0 + tx + 16 * j;
+            if (c < ncols && m < M) {
                 const long long o = c * M + m;
                 if (iq) iq[o] = acc[i][j];
                 if (env) env[o] = sqrtf(fmaf(acc[i][j].x, acc[i][j].x, acc[i][j].y * acc[i][j].y));
             }
         }
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -551,23 +534,9 @@ cudaError_t launch_demod(const float *x, long long ncols, int n, const float2 *W
     const long long gx = (ncols + kDmC - 1) / kDmC;
     const long long gy = ((long long)M + kDmM - 1) / kDmM;
     if (gx > 0x7fffffffLL || gy > 65535) return cudaErrorInvalidValue;
-    // split the input samples over a cluster until the grid covers the GPU twice
-    const long long tiles = gx * gy;
-    const int nst = (n + kDmK - 1) / kDmK;
-    int split = (int)std::min<long long>(8, (2LL * sm_count() + tiles - 1) / tiles);
-    split = std::max(1, std::min(split, nst));
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)gx, (unsigned)gy, (unsigned)split);
-    cfg.blockDim = dim3(kDmThreads);
-    cfg.stream = s;
-    cudaLaunchAttribute attr;
-    attr.id = cudaLaunchAttributeClusterDimension;
-    attr.val.clusterDim.x = 1;
-    attr.val.clusterDim.y = 1;
-    attr.val.clusterDim.z = (unsigned)split;
-    cfg.attrs = &attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, demod_kernel, x, ncols, n, W, M, iq, env);
+    demod_kernel<<<dim3((unsigned)gx, (unsigned)gy), kDmGroup * kDmGroups, 0, s>>>(x, ncols, n, W, M,
+                                                                                iq, env);
+    return cudaGetLastError();
 }
 
 size_t percentile_workspace_bytes(long long nseg) {

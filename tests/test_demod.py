@@ -76,7 +76,7 @@ def test_abi_validates_first():
     assert L.pycbf_gb_demod(None, 4, 8, p, 3, p, None, None) == _lib.EINVAL
     assert L.pycbf_gb_demod(p, 4, 8, p, 3, None, None, None) == _lib.EINVAL
     assert L.pycbf_gb_demod(p, 4, 0, p, 3, p, None, None) == _lib.EINVAL
-    assert L.pycbf_gb_demod(p, 4, 8, p, 70000 * 64, p, None, None) == _lib.ERANGE
+    assert L.pycbf_gb_demod(p, 4, 8, p, 70000 * 32, p, None, None) == _lib.ERANGE
     assert L.pycbf_gb_percentile_workspace_bytes(0) == 0
     assert L.pycbf_gb_percentile_workspace_bytes(3) == 3 * (4 * 2 * 256 + 32) * 4
     assert L.pycbf_gb_percentile(p, 1, 10, 101.0, p, p, 1 << 20, None) == _lib.EINVAL
