@@ -250,6 +250,23 @@ int pycbf_gb_tables_2d(int txkind, int ntx, const double *tx_params, int nele,
                        const double *zout, double cm, double fnum, int hann, float *tautx,
                        float *apodtx, float *taurx, float *apodrx, void *stream);
 
+/* Failure-path test hook (no counterpart in the reference): the cubic     */
+/* staged delay-and-sum of pycbf_gb_das_tabbed_prefiltered (sum over tx    */
+/* and rx) with the first receive of every tile announcing its bytes      */
+/* without issuing its copies, so that receive's mbarrier wait runs out    */
+/* (nothing is in flight for it) after                                     */
+/* wait_cycles SM cycles (1e3 .. 2^31).  Each CTA that gives up writes NaN */
+/* to its pixels, drains its copies (bounded), sets the plan's status word */
+/* (int32 word 0 of the plan, sticky until the caller clears it) and       */
+/* returns; the context stays usable.  No fault, trap or unbounded wait is */
+/* involved.  Requires a plan; PYCBF_GB_EUNSUPPORTED if the staged kernel  */
+/* does not apply.                                                         */
+int pycbf_gb_das_tabbed_stall_test(const pycbf_gb_rfinfo *rf, const void *coef,
+                                   const float *tautx, const float *apodtx, const float *taurx,
+                                   const float *apodrx, long long np, const int *pixel_index,
+                                   float thresh, const void *plan, float *out,
+                                   long long wait_cycles, void *stream);
+
 /* ---------------------------------------------------------------------- */
 /* Synthetic-point delay-and-sum: delays and masks computed per pixel on   */
 /* the fly.  Replaces das_bmode_synthetic_korder_cubic /                   */

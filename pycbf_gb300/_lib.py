@@ -35,7 +35,7 @@ EXPORTS = (
     "pycbf_gb_poly_workspace_bytes", "pycbf_gb_poly_coefficients", "pycbf_gb_das_tabbed_poly",
     "pycbf_gb_das_synthetic_poly", "pycbf_gb_tables_2d", "pycbf_gb_demod",
     "pycbf_gb_percentile_workspace_bytes", "pycbf_gb_percentile", "pycbf_gb_log_compress",
-    "pycbf_gb_convert_i16", "pycbf_gb_log_compress_percentile",
+    "pycbf_gb_convert_i16", "pycbf_gb_log_compress_percentile", "pycbf_gb_das_tabbed_stall_test",
 )
 NOALLOC_SCRATCH_BYTES = 64 << 20
 
@@ -144,6 +144,8 @@ def load() -> ct.CDLL:
         L.pycbf_gb_log_compress.argtypes = [vp, ll, ll, vp, f, vp, vp]
         L.pycbf_gb_convert_i16.argtypes = [vp, ll, vp, vp]
         L.pycbf_gb_log_compress_percentile.argtypes = [vp, ll, ll, d, f, vp, vp, vp, sz, vp]
+        L.pycbf_gb_das_tabbed_stall_test.argtypes = [P(RFInfo), vp, vp, vp, vp, vp, ll, vp, f, vp,
+                                                     vp, ll, vp]
         for name in EXPORTS:
             if name not in ("pycbf_gb_abi_version", "pycbf_gb_status_string",
                             "pycbf_gb_last_cuda_error", "pycbf_gb_workspace_bytes",

@@ -512,10 +512,15 @@ class TabbedBeamformer(Tabbed, _GPUBeamformer):
         return self._nat_tables
 
     def kernel_status(self) -> int:
-        """0, or 1 if a staged launch gave up a bounded wait (its outputs are NaN)."""
+        """0, or 1 if a staged launch gave up a bounded wait (its outputs are
+        NaN).  Sticky until reset_kernel_status()."""
         if self._plan is None:
             return 0
         return int(self._plan[:4].view(torch.int32)[0].item())
+
+    def reset_kernel_status(self) -> None:
+        if self._plan is not None:
+            self._plan[:4].zero_()
 
     def tap_census(self):
         """Per pixel (original order): contributing taps and the sum of their sample indices."""

@@ -298,6 +298,37 @@ int pycbf_gb_das_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef,
                          static_cast<cudaStream_t>(stream));
 }
 
+int pycbf_gb_das_tabbed_stall_test(const pycbf_gb_rfinfo *rf, const void *coef,
+                                   const float *tautx, const float *apodtx, const float *taurx,
+                                   const float *apodrx, long long np, const int *pixel_index,
+                                   float thresh, const void *plan, float *out,
+                                   long long wait_cycles, void *stream) {
+    int st = check_rf(rf, false);
+    if (st) return st;
+    if (!coef || !tautx || !apodtx || !taurx || !apodrx || !out || !plan) return PYCBF_GB_EINVAL;
+    if (reinterpret_cast<uintptr_t>(coef) % 16) return PYCBF_GB_EINVAL;
+    if (np <= 0 || np >= (1LL << 31) || wait_cycles < 1000 || wait_cycles > (1LL << 31))
+        return PYCBF_GB_ERANGE;
+    if (std::isnan(thresh)) return PYCBF_GB_EINVAL;
+    DasArgs a = {};
+    fill_time_axis(a, rf);
+    a.data = coef;
+    a.tautx = tautx;
+    a.apodtx = apodtx;
+    a.taurx = taurx;
+    a.apodrx = apodrx;
+    a.pixel_index = pixel_index;
+    a.out = out;
+    a.np = np;
+    a.thresh = thresh;
+    a.wait_cycles = wait_cycles;
+    a.stall_test = 1;
+    if (!staged_ok(rf, PYCBF_GB_INTERP_CUBIC, PYCBF_GB_SUM_TX_AND_RX, coef))
+        return PYCBF_GB_EUNSUPPORTED;
+    return launch_tabbed(rf, a, PYCBF_GB_INTERP_CUBIC, PYCBF_GB_SUM_TX_AND_RX, plan,
+                         static_cast<cudaStream_t>(stream));
+}
+
 int pycbf_gb_das_synthetic(const pycbf_gb_rfinfo *rf, const void *rfdata,
                            const pycbf_gb_synthetic *geo, const int *pixel_index, int interp,
                            int sumtype, float *out, void *workspace, size_t workspace_bytes,

@@ -160,6 +160,12 @@ struct DasArgs {
     float t0, dt, inv_dt, xmax, xend, thresh, eps;
     const float *slow;  // GEOM_SYNTH_SLOW: slowness per pixel (s/m), kernel pixel order
     float xfma;         // fma(dt, nt-1, t0): the last knot as the reference's CUDA kernels round it
+    // staged kernel: SM cycles after which an mbarrier wait gives up (0: 2^31,
+    // about a second); stall_test: the first receive of every tile announces
+    // its bytes and issues no copy, so its wait runs out (the failure path,
+    // exercised without a fault)
+    long long wait_cycles;
+    int stall_test;
 };
 
 // gather kinds of the polynomial-record interpolators (records from poly.cu)

@@ -68,14 +68,15 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned 
         : "memory");
     return ok != 0;
 }
-// Bounded wait: gives up after kWaitLimit polls or ~1 s of SM clock (2^31
-// cycles at ~2 GHz), whichever comes first.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity) {
+// Bounded wait: gives up after kWaitLimit polls or `limit` SM cycles (by
+// default 2^31, ~1 s at ~2 GHz), whichever comes first.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity,
+                                                  long long limit = 1LL << 31) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     for (unsigned it = 0; it < kWaitLimit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (clock64() - t0 > (1LL << 31)) break;
+        if (clock64() - t0 > limit) break;
     }
     return false;
 }
@@ -391,6 +392,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     const int *order = plan + kPlanHeaderWords + tiles * tile_words;
     unsigned *queue = reinterpret_cast<unsigned *>(plan + 1);
     const long long chs = (long long)nrx * a.nt;
+    const long long wait_lim = a.wait_cycles > 0 ? a.wait_cycles : (1LL << 31);
 
     if (tid < kStages) {
         mbar_init(&full[tid], 1);
@@ -452,9 +454,13 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             if (lane < kTxReg) sbase[slot][lane] = (staged && lane < ntx) ? off - e0 : 0;
             if (lane == 0) sstaged[slot] = staged ? 1 : 0;
             __syncwarp();
-            if (lane == 0) mbar_arrive_expect_tx(&full[slot], staged ? (unsigned)(total * sizeof(E)) : 0u);
+            // stall test: the tile's first receive announces its bytes (at least 16)
+            // and issues no copy, so its phase never completes and nothing is in flight
+            const bool stall = a.stall_test && it == 0;
+            const unsigned bytes = staged ? (unsigned)(total * sizeof(E)) : 0u;
+            if (lane == 0) mbar_arrive_expect_tx(&full[slot], stall ? max(bytes, 16u) : bytes);
             __syncwarp();
-            if (staged && lane < ntx && cnt > 0) {
+            if (staged && lane < ntx && cnt > 0 && !stall) {
                 const E *src = static_cast<const E *>(a.data) + (frame_ch + (long long)lane * nrx + r) * a.nt + e0;
                 E *dst = reinterpret_cast<E *>(smem_raw + (size_t)slot * kStageBytes) + off;
                 tma_bulk_load(dst, src, (unsigned)(cnt * sizeof(E)), &full[slot]);
@@ -503,7 +509,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             trx1 = trx2;
             arx1 = arx2;
             if (it + 2 < nlive) rx_load(it + 2, trx2, arx2);
-            if (!mbar_wait_bounded(&full[slot], (unsigned)(gi / kStages) & 1u)) failed = true;
+            if (!mbar_wait_bounded(&full[slot], (unsigned)(gi / kStages) & 1u, wait_lim)) failed = true;
             if (failed || *(volatile int *)&s_failed) {
                 failed = true;
                 s_failed = 1;
@@ -558,7 +564,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             // warp left it
             if (w == it % kWarps && it >= 1 && it - 1 + kStages < nlive) {
                 const long long pg = gi - 1;
-                if (!mbar_wait_bounded(&empty[pg % kStages], (unsigned)(pg / kStages) & 1u)) {
+                if (!mbar_wait_bounded(&empty[pg % kStages], (unsigned)(pg / kStages) & 1u, wait_lim)) {
                     failed = true;
                     s_failed = 1;
                     break;
@@ -588,7 +594,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         atomicExch(plan, 1);
         const long long produced = *(volatile long long *)&s_produced;
         for (long long j = max(0LL, produced - kStages); j < produced; ++j)
-            (void)mbar_wait_bounded(&full[j % kStages], (unsigned)(j / kStages) & 1u);
+            (void)mbar_wait_bounded(&full[j % kStages], (unsigned)(j / kStages) & 1u, wait_lim);
     }
 }
 
