@@ -409,25 +409,7 @@ class _GPUBeamformer(Beamformer):
 
     def __call__(self, txrxt, out_as_numpy: bool = True, buffer=None):
         out = self._beamform(txrxt, buffer)
-        return self._host(out) if out_as_numpy else out
-
-    _PINNED_MAX = 64 << 20
-
-    def _host(self, out: torch.Tensor) -> np.ndarray:
-        """A NumPy copy of a device result: through a pinned staging buffer of
-        this beamformer (a pageable device-to-host copy is several times
-        slower), then one host copy, so results of earlier calls are never
-        overwritten.  Results above 64 MiB go straight to pageable memory."""
-        nbytes = out.numel() * out.element_size()
-        if nbytes > self._PINNED_MAX or not out.is_cuda or out.dtype != torch.float32:
-            return out.cpu().numpy()
-        buf = getattr(self, "_pinned", None)
-        if buf is None or buf.numel() < out.numel():
-            buf = self._pinned = torch.empty(out.numel(), dtype=torch.float32, pin_memory=True)
-        stage = buf[: out.numel()]
-        stage.copy_(out.reshape(-1), non_blocking=True)
-        torch.cuda.current_stream().synchronize()
-        return stage.numpy().reshape(tuple(out.shape)).copy()
+        return out.cpu().numpy() if out_as_numpy else out
 
 
 # ---------------------------------------------------------------------------
@@ -704,7 +686,7 @@ class _DMASMixin:
                                          len(self._lags_host), 0 if self.dmastype == "ssr" else 1,
                                          int(bool(self.sumlags)), _ptr(out), _stream_ptr())
             _lib.check(st, "pycbf_gb_dmas")
-        return self._host(out) if out_as_numpy else out
+        return out.cpu().numpy() if out_as_numpy else out
 
 
 @dataclass(kw_only=True)
@@ -756,7 +738,7 @@ class _SLSCMixin:
         st = self._lib.pycbf_gb_slsc(_ptr(sep), _ptr(self._mask), nframes or 1, self.nrx, nx, nz,
                                      int(self.nlag), int(self.nkern), _ptr(out), _stream_ptr())
         _lib.check(st, "pycbf_gb_slsc")
-        return self._host(out) if out_as_numpy else out
+        return out.cpu().numpy() if out_as_numpy else out
 
 
 @dataclass(kw_only=True)
