@@ -54,7 +54,12 @@ __device__ __forceinline__ void batch_tile(const DasArgs &a, long long tile) {
             }
         }
         const int nk_chunk = min(TXC, ntx - t0);
+        float bacc = 0.f;  // blocks of kRxBlockSum receives, as the other kernels sum
         for (int r = 0; r < nrx; ++r) {
+            if (r > 0 && r % kRxBlockSum == 0) {
+                acc += bacc;
+                bacc = 0.f;
+            }
             float trx, arx;
             bool live;
             if (GEOM == GEOM_TABBED) {
@@ -119,8 +124,9 @@ __device__ __forceinline__ void batch_tile(const DasArgs &a, long long tile) {
                     if ((hit >> k) & 1u)
                         accr = fmaf(ap[k], K::value(pv[k], xs[k], (float)ix[k], a), accr);
             }
-            acc += accr;
+            bacc += accr;
         }
+        acc += bacc;
     }
     a.out[op] = acc;
 }

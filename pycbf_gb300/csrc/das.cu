@@ -17,8 +17,7 @@ cudaError_t launch_staged_f16(const DasArgs &, int, int, const int *, int *, cud
 cudaError_t launch_staged_bf16(const DasArgs &, int, int, const int *, int *, cudaStream_t);
 
 long long tabbed_plan_words(long long np, int ntx, int nrx) {
-    const long long tiles = (np + kBlock - 1) / kBlock;
-    return kPlanHeaderWords + tiles * plan_tile_words(ntx, nrx) + tiles;
+    return plan_layout(np, ntx, nrx).total;
 }
 
 cudaError_t launch_tabbed_plan(const DasArgs &a, int interp, int dtype, int *plan, cudaStream_t s) {

@@ -28,6 +28,11 @@
 namespace pgb {
 
 constexpr int kTxReg = 12;
+// Over receives, TX_AND_RX images are summed in blocks of kRxBlockSum consecutive
+// receive indices: the sum over blocks, in order, of each block's sequential
+// sum.  Every kernel (generic, staged, batched) sums this way, so they agree
+// bit for bit, and the staged kernel can hand a tile's blocks to different CTAs.
+constexpr int kRxBlockSum = 32;
 constexpr float kDxMin = 1e-12f;
 
 // (int)fl for an integral float 0 <= fl < 2^23 without a conversion instruction
@@ -371,6 +376,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ 
     }
 
     float acc = 0.f, s1 = 0.f;
+    float bacc = 0.f;  // TX_AND_RX: sequential sum of the current block of kRxBlockSum receives
     int cnt = 0;
     long long isum = 0;
 
@@ -393,6 +399,10 @@ __global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ 
     if (GEOM == GEOM_TABBED && nrx > 0) rx_side(0, trx_next, arx_next);
 
     for (int r = 0; r < nrx; ++r) {
+        if (SUM == PYCBF_GB_SUM_TX_AND_RX && r > 0 && r % kRxBlockSum == 0) {
+            acc += bacc;  // the image is the sum of the blocks' sums, in block order
+            bacc = 0.f;
+        }
         float trx, arx;
         if (GEOM == GEOM_TABBED) {
             trx = trx_next;
@@ -507,7 +517,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ 
             }
         }
 
-        if (SUM == PYCBF_GB_SUM_TX_AND_RX) acc += accr;
+        if (SUM == PYCBF_GB_SUM_TX_AND_RX) bacc += accr;
         if (!CENSUS && SUM == PYCBF_GB_SUM_TX_ONLY) a.out[((long long)f * nrx + r) * np + op] = accr;
         if (SUM == PYCBF_GB_SUM_DMAS_SSR || SUM == PYCBF_GB_SUM_DMAS_POWER) {
             // pairwise sum over receives i<j of s_i s_j as sum_j s_j * (sum_{i<j} s_i):
@@ -518,6 +528,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ 
         }
     }
 
+    if (SUM == PYCBF_GB_SUM_TX_AND_RX) acc += bacc;
     // census launches carry no image buffer (out is NULL): they store counts only
     if (!CENSUS && (SUM == PYCBF_GB_SUM_TX_AND_RX || SUM == PYCBF_GB_SUM_DMAS_SSR ||
                     SUM == PYCBF_GB_SUM_DMAS_POWER))

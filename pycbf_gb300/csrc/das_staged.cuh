@@ -30,14 +30,43 @@ constexpr int kStageBytes = 12 * 1024;
 constexpr unsigned kWaitLimit = 1u << 30;  // polls; the ~1 s clock bound ends a wait first
 
 // plan layout (int32 words): [0] status, [1] work-queue head of the staged
-// kernel, [2..3] pad, then per tile a record of plan_tile_words(ntx, nrx) words:
+// kernel, [2] number of block items, [3] pad, then per tile a record of
+// plan_tile_words(ntx, nrx) words:
 //   nlive | rx index per live receive (nrx) | rx lo,hi per live receive (2*nrx floats)
 //   | tx lo,hi per transmit (2*ntx floats)
-// and last the tile order (one int per tile, most live receives first).
+// then the tile order (one int per tile, most live receives first), a
+// per-tile counter, the block items (int4 each: tile, first and one-past-last
+// position in the tile's live list, block ordinal << 16 | blocks of the
+// tile; largest first) and the partial sums of multi-block tiles (kBlock
+// floats per tile and block).
+//
+// Receives are summed in blocks of kRxBlock consecutive receive indices:
+// the image is sum over blocks (in order) of the block's sequential sum, in
+// every kernel (staged, generic, batched), so all of them give the same bits.
+// A single-frame staged launch makes each (tile, block with live receives)
+// one work item -- the heaviest tiles (every receive live) no longer outlast
+// the average CTA's share -- and the last item of a tile to finish adds the
+// tile's block sums in block order.
+constexpr int kRxBlock = kRxBlockSum;
 __host__ __device__ inline long long plan_tile_words(int ntx, int nrx) {
     return 1 + (long long)nrx + 2LL * nrx + 2LL * ntx;
 }
 constexpr int kPlanHeaderWords = 4;
+struct PlanLayout {
+    long long tiles, tile_words, max_blocks, order, counters, items, partials, total;
+};
+__host__ __device__ inline PlanLayout plan_layout(long long np, int ntx, int nrx) {
+    PlanLayout L;
+    L.tiles = (np + kBlock - 1) / kBlock;
+    L.tile_words = plan_tile_words(ntx, nrx);
+    L.max_blocks = (nrx + kRxBlock - 1) / kRxBlock;
+    L.order = kPlanHeaderWords + L.tiles * L.tile_words;
+    L.counters = L.order + L.tiles;
+    L.items = (L.counters + L.tiles + 3) & ~3LL;  // int4: 16-byte aligned
+    L.partials = L.items + 4 * L.tiles * L.max_blocks;
+    L.total = L.partials + L.tiles * L.max_blocks * kBlock;
+    return L;
+}
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
     return static_cast<unsigned>(__cvta_generic_to_shared(p));
@@ -379,6 +408,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     __shared__ int s_failed;
     __shared__ long long s_produced;  // items (over all tiles) whose copies have been issued
     __shared__ long long s_item;
+    __shared__ int s_last;
     // the tile's plan: live receive indices and their delay bounds
     int *s_rx = reinterpret_cast<int *>(smem_raw + kStages * kStageBytes);
     float *s_rxlh = reinterpret_cast<float *>(s_rx + a.nrx);
@@ -386,10 +416,17 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int ntx = a.ntx, nrx = a.nrx;
     const long long np = a.np;
-    const long long tiles = (np + kBlock - 1) / kBlock;
-    const long long tile_words = plan_tile_words(ntx, nrx);
-    const long long nitems = tiles * a.nframes;
-    const int *order = plan + kPlanHeaderWords + tiles * tile_words;
+    const PlanLayout L = plan_layout(np, ntx, nrx);
+    const long long tiles = L.tiles;
+    const long long tile_words = L.tile_words;
+    // one frame summed over receives: (tile, receive block) items; otherwise (frame, tile)
+    constexpr bool kBlockSum = SUM == PYCBF_GB_SUM_TX_AND_RX || SUM == PYCBF_GB_SUM_TX_ONLY;
+    const bool by_block = kBlockSum && a.nframes == 1;
+    const long long nitems = by_block ? (long long)__ldg(plan + 2) : tiles * a.nframes;
+    const int *order = plan + L.order;
+    const int4 *bitems = reinterpret_cast<const int4 *>(plan + L.items);
+    int *counters = plan + L.counters;
+    float *partials = reinterpret_cast<float *>(plan + L.partials);
     unsigned *queue = reinterpret_cast<unsigned *>(plan + 1);
     const long long chs = (long long)nrx * a.nt;
     const long long wait_lim = a.wait_cycles > 0 ? a.wait_cycles : (1LL << 31);
@@ -410,19 +447,32 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         __syncthreads();  // also: every warp is done with the previous tile's ring and plan data
         const long long item = s_item;
         if (item >= nitems || s_failed) break;
-        const int f = (int)(item / tiles);
-        const long long tile = __ldg(order + (item - (long long)f * tiles));
+        int f = 0, first = 0, bord = 0, nblocks = 1;
+        long long tile;
+        int nlive;
+        if (by_block) {
+            const int4 it4 = __ldg(bitems + item);
+            tile = it4.x;
+            first = it4.y;
+            nlive = it4.z - it4.y;
+            bord = it4.w >> 16;
+            nblocks = it4.w & 0xffff;
+        } else {
+            f = (int)(item / tiles);
+            tile = __ldg(order + (item - (long long)f * tiles));
+        }
         const long long i = tile * kBlock + tid;
         const bool valid = i < np;
         const int *rec = plan + kPlanHeaderWords + tile * tile_words;
-        const int nlive = __ldg(rec);
+        if (!by_block) nlive = __ldg(rec);
         const long long frame_ch = (long long)f * ntx * nrx;
         const long long op = valid ? (a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i) : 0;
         {
+            // this item's live receives: the whole list, or one block of it
             const float *txlh = reinterpret_cast<const float *>(rec + 1 + 3 * nrx);
             if (tid < 2 * ntx) s_txlh[tid] = __ldg(txlh + tid);
-            for (int k = tid; k < nlive; k += kBlock) s_rx[k] = __ldg(rec + 1 + k);
-            const float *rxlh = reinterpret_cast<const float *>(rec + 1 + nrx);
+            for (int k = tid; k < nlive; k += kBlock) s_rx[k] = __ldg(rec + 1 + first + k);
+            const float *rxlh = reinterpret_cast<const float *>(rec + 1 + nrx) + 2 * first;
             for (int k = tid; k < 2 * nlive; k += kBlock) s_rxlh[k] = __ldg(rxlh + k);
         }
         __syncthreads();
@@ -490,6 +540,8 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         }
 
         float acc = 0.f, s1 = 0.f;
+        float bacc = 0.f;  // the current receive block's sequential sum (TX_AND_RX)
+        int cur_block = -1;
         bool failed = false;
         // receive-side values, fetched two receives ahead
         auto rx_load = [&](int it, float &trx, float &arx) {
@@ -516,6 +568,11 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
                 break;
             }
 
+            if (SUM == PYCBF_GB_SUM_TX_AND_RX && r / kRxBlock != cur_block) {
+                acc += bacc;  // blocks without a live receive add exact zeros elsewhere
+                bacc = 0.f;
+                cur_block = r / kRxBlock;
+            }
             const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh);
             float accr = 0.f;
             if (live) {
@@ -550,7 +607,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
                     }
                 }
             }
-            if (SUM == PYCBF_GB_SUM_TX_AND_RX) acc += accr;
+            if (SUM == PYCBF_GB_SUM_TX_AND_RX) bacc += accr;
             if (SUM == PYCBF_GB_SUM_TX_ONLY && valid) a.out[((long long)f * nrx + r) * np + op] = accr;
             if (SUM == PYCBF_GB_SUM_DMAS_SSR || SUM == PYCBF_GB_SUM_DMAS_POWER) {
                 const float sv = (SUM == PYCBF_GB_SUM_DMAS_SSR) ? copysignf(sqrtf(fabsf(accr)), accr) : accr;
@@ -584,7 +641,28 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             }
             break;
         }
-        if (valid && SUM != PYCBF_GB_SUM_TX_ONLY) a.out[(long long)f * np + op] = acc;
+        if (SUM == PYCBF_GB_SUM_TX_AND_RX) acc += bacc;
+        if (SUM != PYCBF_GB_SUM_TX_ONLY) {
+            if (!by_block || nblocks == 1) {
+                if (valid) a.out[(long long)f * np + op] = acc;
+            } else {
+                // one block of a multi-block tile: the last block to finish adds the
+                // tile's block sums in block order (the same bits whatever the order
+                // the blocks finish in)
+                float *pt = partials + tile * L.max_blocks * kBlock + tid;
+                pt[(long long)bord * kBlock] = acc;
+                __threadfence();
+                __syncthreads();
+                if (tid == 0) s_last = atomicAdd(counters + tile, 1) == nblocks - 1;
+                __syncthreads();
+                if (s_last) {
+                    __threadfence();
+                    float sum = __ldcg(pt);
+                    for (int c = 1; c < nblocks; ++c) sum += __ldcg(pt + (long long)c * kBlock);
+                    if (valid) a.out[op] = sum;
+                }
+            }
+        }
         g0 += nlive;
     }
     __syncthreads();
@@ -609,7 +687,8 @@ static __global__ void __launch_bounds__(1024) plan_order_kernel(int *plan, long
                                                           int nrx) {
     extern __shared__ int bins[];  // nrx + 1 bins, nlive = nrx first
     const long long tw = plan_tile_words(ntx, nrx);
-    int *order = plan + kPlanHeaderWords + tiles * tw;
+    const PlanLayout L = plan_layout(tiles * kBlock, ntx, nrx);
+    int *order = plan + L.order;
     for (int b = threadIdx.x; b <= nrx; b += blockDim.x) bins[b] = 0;
     __syncthreads();
     for (long long t = threadIdx.x; t < tiles; t += blockDim.x)
@@ -628,6 +707,51 @@ static __global__ void __launch_bounds__(1024) plan_order_kernel(int *plan, long
         const int b = nrx - min(max(plan[kPlanHeaderWords + t * tw], 0), nrx);
         order[atomicAdd(&bins[b], 1)] = (int)t;
     }
+    __syncthreads();
+
+    // block items: every (tile, block of kRxBlock receive indices with a live
+    // receive), a tile without live receives as one empty item; counting sort
+    // on the item's receive count, largest first
+    int *sz = bins;  // kRxBlock + 1 bins
+    for (int b = threadIdx.x; b <= kRxBlock; b += blockDim.x) sz[b] = 0;
+    __syncthreads();
+    // walk the blocks of tile t's live list: f(first, last, ordinal, count)
+    auto blocks = [&](long long t, auto &&f) {
+        const int *rec = plan + kPlanHeaderWords + t * tw;
+        const int nlive = min(max(rec[0], 0), nrx);
+        if (nlive == 0) {
+            f(0, 0, 0, 1);
+            return;
+        }
+        int nb = 0;
+        for (int k = 0; k < nlive; ++k)
+            if (k == 0 || ((rec[1 + k] & 0x3fffffff) / kRxBlock) != ((rec[k] & 0x3fffffff) / kRxBlock)) ++nb;
+        int first = 0, ord = 0;
+        for (int k = 1; k <= nlive; ++k) {
+            if (k == nlive || ((rec[1 + k] & 0x3fffffff) / kRxBlock) != ((rec[k] & 0x3fffffff) / kRxBlock)) {
+                f(first, k, ord++, nb);
+                first = k;
+            }
+        }
+    };
+    for (long long t = threadIdx.x; t < tiles; t += blockDim.x)
+        blocks(t, [&](int b0, int b1, int, int) { atomicAdd(&sz[kRxBlock - (b1 - b0)], 1); });
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int b = 0; b <= kRxBlock; ++b) {
+            const int c = sz[b];
+            sz[b] = run;
+            run += c;
+        }
+        plan[2] = run;
+    }
+    __syncthreads();
+    int4 *items = reinterpret_cast<int4 *>(plan + L.items);
+    for (long long t = threadIdx.x; t < tiles; t += blockDim.x)
+        blocks(t, [&](int b0, int b1, int ord, int nb) {
+            items[atomicAdd(&sz[kRxBlock - (b1 - b0)], 1)] = make_int4((int)t, b0, b1, (ord << 16) | nb);
+        });
 }
 
 template <int KIND, typename T>
@@ -636,7 +760,7 @@ cudaError_t launch_plan_one(const DasArgs &a, int *plan, cudaStream_t s) {
     tabbed_plan_kernel<KIND, T><<<(unsigned)tiles, kBlock, 0, s>>>(a, plan);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
-    const size_t smem = sizeof(int) * ((size_t)a.nrx + 1);
+    const size_t smem = sizeof(int) * ((size_t)max(a.nrx, kRxBlock) + 1);
     plan_order_kernel<<<1, 1024, smem, s>>>(plan, tiles, a.ntx, a.nrx);
     return cudaGetLastError();
 }
@@ -654,11 +778,18 @@ cudaError_t launch_staged_one(const DasArgs &a, const int *plan, int *status, cu
     if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, smem)) !=
         cudaSuccess)
         return err;
-    const long long items = (a.np + kBlock - 1) / kBlock * (long long)a.nframes;
+    const PlanLayout L = plan_layout(a.np, a.ntx, a.nrx);
+    constexpr bool kBlockSum = SUM == PYCBF_GB_SUM_TX_AND_RX || SUM == PYCBF_GB_SUM_TX_ONLY;
+    const bool by_block = kBlockSum && a.nframes == 1;
+    const long long items = by_block ? L.tiles * L.max_blocks : L.tiles * (long long)a.nframes;
     const long long grid = std::min<long long>(items, (long long)std::max(1, per_sm) * nsm);
-    // the queue head, plan[1], starts at zero
+    // the queue head, plan[1], and the tiles' block counters start at zero
     err = cudaMemsetAsync(status + 1, 0, sizeof(int), s);
     if (err != cudaSuccess) return err;
+    if (by_block && SUM == PYCBF_GB_SUM_TX_AND_RX) {
+        err = cudaMemsetAsync(const_cast<int *>(plan) + L.counters, 0, sizeof(int) * L.tiles, s);
+        if (err != cudaSuccess) return err;
+    }
     kern<<<(unsigned)grid, kBlock, smem, s>>>(a, const_cast<int *>(plan));
     return cudaGetLastError();
 }
