@@ -32,7 +32,7 @@ constexpr int kTxReg = 12;
 // receive indices: the sum over blocks, in order, of each block's sequential
 // sum.  Every kernel (generic, staged, batched) sums this way, so they agree
 // bit for bit, and the staged kernel can hand a tile's blocks to different CTAs.
-constexpr int kRxBlockSum = 32;
+constexpr int kRxBlockSum = 64;
 constexpr float kDxMin = 1e-12f;
 
 // (int)fl for an integral float 0 <= fl < 2^23 without a conversion instruction
