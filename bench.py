@@ -28,6 +28,7 @@ from __future__ import annotations
 import argparse
 import ctypes as ct
 import json
+import re
 import os
 import statistics
 import subprocess
@@ -300,10 +301,13 @@ def main_ours(a):
                 "kernel_ms": 1e3 * das_s, "spline_ms": statistics.mean(spline_ms),
                 "peak_source": "measured" if peaks.get("hbm_gbs") else "fallback",
                 "algorithmic_bytes": alg_bytes}
-    traffic_file = os.path.join(ROOT, "profiles", "das_tabbed_cubic_c1.traffic.json")
-    if os.path.exists(traffic_file):
-        with open(traffic_file) as fp:
-            roofline["traffic"] = json.load(fp).get("dram_bytes_per_launch")
+    # DRAM bytes of one launch from the committed ncu summary of this kernel and workload
+    prof = os.path.join(ROOT, "profiles", "das_tabbed_cubic_c1.md")
+    if os.path.exists(prof):
+        with open(prof) as fp:
+            m = re.search(r"dram bytes per launch \(read \+ write\): (\d+)", fp.read())
+        if m:
+            roofline["traffic"] = int(m.group(1))
     # FP32 roofline: algorithmic FLOPs (20 per contributing cubic tap, 2 per tap for the
     # weight product and threshold) over the kernel time, against the FMA probe
     probe_out = torch.empty(152 * 8 * 256, device=dev)
