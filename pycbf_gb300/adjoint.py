@@ -88,7 +88,7 @@ def _out_shape(rf4, np_, sumtype):
 
 class _TabbedDAS(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, rf4, tautx, taurx, apodtx, apodrx, pixel_index, spec):
+    def forward(ctx, rf4, tautx, taurx, apodtx, apodrx, pixel_index, spec, plan=None):
         L = _lib.load()
         info = _info(rf4, spec)
         coef = _coefficients(L, rf4, info)
@@ -97,7 +97,7 @@ class _TabbedDAS(torch.autograd.Function):
                           device=rf4.device)
         st = L.pycbf_gb_das_tabbed_prefiltered(
             ct.byref(info), _ptr(coef), _ptr(tautx), _ptr(apodtx), _ptr(taurx), _ptr(apodrx), np_,
-            _ptr(pixel_index), float(np.float32(spec.thresh)), spec.sumtype, None, _ptr(out),
+            _ptr(pixel_index), float(np.float32(spec.thresh)), spec.sumtype, _ptr(plan), _ptr(out),
             _stream())
         _lib.check(st, "pycbf_gb_das_tabbed_prefiltered")
         ctx.save_for_backward(coef, tautx, taurx, apodtx, apodrx)
@@ -133,7 +133,7 @@ class _TabbedDAS(torch.autograd.Function):
             _lib.check(st, "pycbf_gb_das_tabbed_adjoint")
         if g_rf is not None and dtype != torch.float32:
             g_rf = g_rf.to(dtype)
-        return g_rf, g_ttx, g_trx, None, None, None, None
+        return g_rf, g_ttx, g_trx, None, None, None, None, None
 
 
 class _SyntheticDAS(torch.autograd.Function):
@@ -197,13 +197,16 @@ def _as4(rf):
 
 def das_tabbed(rf: torch.Tensor, tautx: torch.Tensor, taurx: torch.Tensor, apodtx: torch.Tensor,
                apodrx: torch.Tensor, *, t0: float, dt: float, thresh: float = 1e-2,
-               sumtype: str = "tx_and_rx", pixel_index: torch.Tensor | None = None) -> torch.Tensor:
+               sumtype: str = "tx_and_rx", pixel_index: torch.Tensor | None = None,
+               plan: torch.Tensor | None = None) -> torch.Tensor:
     """Differentiable cubic Tabbed delay-and-sum.
 
     rf (ntx, nrx, nt) or (nframes, ntx, nrx, nt), float32/float16/bfloat16 on
     CUDA; tautx/apodtx (ntx, np), taurx/apodrx (nrx, np) float32.  Returns
     (np,) / (nframes, np) for 'tx_and_rx', (nrx, np) / (nframes, nrx, np) for
     'tx_only'.  Values equal TabbedBeamformer(interp cubic) on the same inputs.
+    plan: a staging plan built for exactly these tables and thresh
+    (pycbf_gb_tabbed_plan): the forward then runs the staged kernel.
     """
     _check_rf(rf)
     rf4, squeeze = _as4(rf)
@@ -216,7 +219,7 @@ def das_tabbed(rf: torch.Tensor, tautx: torch.Tensor, taurx: torch.Tensor, apodt
     if pixel_index is not None:
         pixel_index = pixel_index.to(device=rf.device, dtype=torch.int32).contiguous()
     spec = _Spec(float(t0), float(dt), float(thresh), _sumtype_code(sumtype))
-    out = _TabbedDAS.apply(rf4, *tables, pixel_index, spec)
+    out = _TabbedDAS.apply(rf4, *tables, pixel_index, spec, plan)
     return out[0] if squeeze else out
 
 

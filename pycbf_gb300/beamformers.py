@@ -487,7 +487,7 @@ class TabbedBeamformer(Tabbed, _GPUBeamformer):
             ktx, kap_tx, krx, kap_rx = self._tables
             return adjoint.das_tabbed(rf, ktx, krx, kap_tx, kap_rx, t0=self.t0, dt=self.dt,
                                       thresh=self.thresh, sumtype=sumtype or self.sumtype,
-                                      pixel_index=self._pixel_index)
+                                      pixel_index=self._pixel_index, plan=self._plan)
         # caller-owned delay tables: run in the caller's pixel order, so that
         # no permutation (and no scatter of its gradient) is needed
         ntx_, nap_tx, nrx_, nap_rx = self._natural_tables()
