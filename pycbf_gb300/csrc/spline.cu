@@ -1,15 +1,17 @@
-// Natural cubic spline coefficients for every channel, one warp per channel.
+// Natural cubic spline coefficients for every channel, one pair of warps per
+// channel.
 //
 // The reference builds the knots of each channel with a serial Thomas solve
 // (tie_knots1D_fixed, pycbf/cpu/pycbf.c:114-166): a forward sweep
 //   u_i = (6 (y_{i+1} - 2 y_i + y_{i-1}) / (2 dx^2) - 0.5 u_{i-1}) / p_i
 // and a back-substitution y2_k = c_k y2_{k+1} + u_k.  Both recurrences
 // contract by |0.5/p| -> 2 - sqrt(3) = 0.268 per step, so a lane can start
-// either sweep 32 samples before its chunk from zero: the start error has
-// shrunk by 0.268^32 ~ 5e-19 when the chunk begins.  Each of the 32 lanes
+// either sweep kWarm = 16 samples before its chunk from zero: the start error
+// has shrunk by 0.268^16 ~ 7e-10 when the chunk begins.  Each of the 64 lanes
 // owns a contiguous chunk of the channel (of odd length, so that the lanes'
-// sequential sweeps fall in distinct shared-memory banks); the channel, u and
-// y2 sit in shared memory.  Output per sample j: (y_j, y_j+1, z_j, z_j+1), z = y2 dx^2 / 6,
+// sequential sweeps fall in distinct shared-memory banks; 33 samples at nt =
+// 2048, so each lane's serial chain is 49 steps); the channel, u and y2 sit in
+// shared memory.  Output per sample j: (y_j, y_j+1, z_j, z_j+1), z = y2 dx^2 / 6,
 // with y_nt = z_nt = 0, so the forward kernel does one 16-byte (or 8-byte)
 // load per tap.
 #include <algorithm>
@@ -18,7 +20,9 @@
 
 namespace pgb {
 
-constexpr int kWarm = 32;
+// warm-up of each lane's sweeps: 0.268^16 = 7e-10 of the start error is left,
+// below float32 rounding
+constexpr int kWarm = 16;
 
 void make_spline_table(SplineTable *t) {
     float y2f = 0.0f;
@@ -33,15 +37,23 @@ void make_spline_table(SplineTable *t) {
     }
 }
 
-// One channel by one warp: src (nt samples) -> dst (nt records); smem holds
-// two arrays of (nt + 4) & ~3 floats: the channel, and u overwritten in place
-// by z (each lane first runs its back-substitution warm-up over the next
-// lanes' u, then all lanes overwrite their own chunks).
-template <typename T>
+// One channel by LANES threads (one warp, or a pair of warps: 64 lanes halve
+// each lane's serial recurrences): src (nt samples) -> dst (nt records); smem
+// holds two arrays of (nt + 4) & ~3 floats: the channel, and u overwritten in
+// place by z (each lane first runs its back-substitution warm-up over the next
+// lanes' u, then all lanes overwrite their own chunks).  A pair synchronises on
+// named barrier `bar` (1..15).
+template <int LANES>
+__device__ __forceinline__ void lanes_sync(int bar) {
+    if (LANES == 32) __syncwarp();
+    else asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(LANES) : "memory");
+}
+template <typename T, int LANES = 32>
 __device__ __forceinline__ void spline_channel(const T *__restrict__ src,
                                                typename CoefRec<T>::raw *__restrict__ dst, int nt,
-                                               float dt, const SplineTable &tab, float *smem) {
-    const int lane = threadIdx.x & 31;
+                                               float dt, const SplineTable &tab, float *smem,
+                                               int bar = 0) {
+    const int lane = threadIdx.x & (LANES - 1);
     const int stride = (nt + 4) & ~3;  // >= nt+1, keeps every array 16-byte aligned
     float *y = smem;
     float *uz = y + stride;  // u, then z
@@ -51,14 +63,14 @@ __device__ __forceinline__ void spline_channel(const T *__restrict__ src,
     if ((nt % V) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
         const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
 #pragma unroll 8
-        for (int k = lane; k < nt / V; k += 32) {
+        for (int k = lane; k < nt / V; k += LANES) {
             const uint4 v = __ldg(s4 + k);
             const T *e = reinterpret_cast<const T *>(&v);
 #pragma unroll
             for (int m = 0; m < V; ++m) y[k * V + m] = load_sample_reg(e[m]);
         }
     } else {
-        for (int k = lane; k < nt; k += 32) y[k] = load_sample(src + k);
+        for (int k = lane; k < nt; k += LANES) y[k] = load_sample(src + k);
     }
     if (lane == 0) {
         y[nt] = 0.f;
@@ -66,13 +78,13 @@ __device__ __forceinline__ void spline_channel(const T *__restrict__ src,
         uz[nt] = 0.f;
         uz[nt - 1] = 0.f;
     }
-    __syncwarp();
+    lanes_sync<LANES>(bar);
 
     const float inv_dt = 1.0f / dt;
     const float cscale = 6.0f / (2.0f * dt);
     const float zscale = dt * dt / 6.0f;
     // chunk length odd: lane l then reads word l*C + i, a distinct bank per lane
-    const int C = ((nt + 31) >> 5) | 1;
+    const int C = ((nt + LANES - 1) / LANES) | 1;
     const int s = lane * C;
     const int e = min(s + C, nt);
 
@@ -90,7 +102,7 @@ __device__ __forceinline__ void spline_channel(const T *__restrict__ src,
             }
         }
     }
-    __syncwarp();
+    lanes_sync<LANES>(bar);
     // back-substitution: y2_k for k in [s, min(e, nt-1)), y2_{nt-1} = 0; the
     // warm-up over the next lanes' u first, then this lane's chunk in place
     const int kb = s, ke = min(e, nt - 1);
@@ -98,7 +110,7 @@ __device__ __forceinline__ void spline_channel(const T *__restrict__ src,
     if (kb < ke)
         for (int k = min(nt - 2, ke - 1 + kWarm); k >= ke; --k)
             yn = fmaf(tab.c[min(k, kSplineTab - 1)], yn, uz[k]);
-    __syncwarp();
+    lanes_sync<LANES>(bar);
     if (kb < ke)
         for (int k = ke - 1; k >= kb; --k) {
             const float uk = (k == 0) ? 0.f : uz[k];
@@ -106,44 +118,46 @@ __device__ __forceinline__ void spline_channel(const T *__restrict__ src,
             uz[k] = y2k * zscale;
             yn = y2k;
         }
-    __syncwarp();
-    for (int k = lane; k < nt; k += 32) dst[k] = CoefRec<T>::pack(y[k], y[k + 1], uz[k], uz[k + 1]);
+    lanes_sync<LANES>(bar);
+    for (int k = lane; k < nt; k += LANES) dst[k] = CoefRec<T>::pack(y[k], y[k + 1], uz[k], uz[k + 1]);
 }
 
+// one channel per pair of warps (named barrier 1 + pair index)
 template <typename T>
 __global__ void __launch_bounds__(256)
 spline_coef_kernel(const T *__restrict__ rf, typename CoefRec<T>::raw *__restrict__ coef,
                    long long nch, int nt, float dt, const __grid_constant__ SplineTable tab) {
     extern __shared__ float smem[];
-    const int w = threadIdx.x >> 5;
-    const int wpb = blockDim.x >> 5;
-    const long long ch = (long long)blockIdx.x * wpb + w;
-    if (ch >= nch) return;
+    const int pr = threadIdx.x >> 6;
+    const int ppb = blockDim.x >> 6;
+    const long long ch = (long long)blockIdx.x * ppb + pr;
+    if (ch >= nch) return;  // both warps of a pair leave together
     const int stride = (nt + 4) & ~3;
-    spline_channel<T>(rf + ch * (long long)nt, coef + ch * (long long)nt, nt, dt, tab,
-                      smem + (size_t)w * 2 * stride);
+    spline_channel<T, 64>(rf + ch * (long long)nt, coef + ch * (long long)nt, nt, dt, tab,
+                          smem + (size_t)pr * 2 * stride, 1 + pr);
 }
 
 // Batched: one warp per channel of any job (jobs' channels numbered
 // consecutively from BatchJob::ch0); smem per warp sized for the longest.
+// one channel per pair of warps, as spline_coef_kernel (the same records)
 template <typename T>
 __device__ __forceinline__ void batch_spline_one(const BatchJob &j, long long ch, float *sm,
-                                                 const SplineTable &tab) {
+                                                 const SplineTable &tab, int bar) {
     using raw = typename CoefRec<T>::raw;
     const int nt = j.a.nt;
-    spline_channel<T>(static_cast<const T *>(j.rf) + ch * (long long)nt,
-                      static_cast<raw *>(const_cast<void *>(j.a.data)) + ch * (long long)nt, nt,
-                      j.a.dt, tab, sm);
+    spline_channel<T, 64>(static_cast<const T *>(j.rf) + ch * (long long)nt,
+                          static_cast<raw *>(const_cast<void *>(j.a.data)) + ch * (long long)nt, nt,
+                          j.a.dt, tab, sm, bar);
 }
 
 __global__ void __launch_bounds__(256)
 batch_spline_kernel(const BatchJob *__restrict__ jobs, int njobs, long long nch_total,
                     int max_stride, const __grid_constant__ SplineTable tab) {
     extern __shared__ float smem[];
-    const int w = threadIdx.x >> 5;
-    const int wpb = blockDim.x >> 5;
+    const int w = threadIdx.x >> 6;  // pair
+    const int wpb = blockDim.x >> 6;
     const long long gc = (long long)blockIdx.x * wpb + w;
-    if (gc >= nch_total) return;
+    if (gc >= nch_total) return;  // both warps of a pair leave together
     // the job whose channel range holds gc (jobs sorted by ch0)
     int lo = 0, hi = njobs - 1;
     while (lo < hi) {
@@ -155,17 +169,17 @@ batch_spline_kernel(const BatchJob *__restrict__ jobs, int njobs, long long nch_
     const long long ch = gc - j.ch0;
     float *sm = smem + (size_t)w * 2 * max_stride;
     switch (j.dtype) {
-        case PYCBF_GB_F32: batch_spline_one<float>(j, ch, sm, tab); break;
-        case PYCBF_GB_F16: batch_spline_one<__half>(j, ch, sm, tab); break;
-        default: batch_spline_one<__nv_bfloat16>(j, ch, sm, tab); break;
+        case PYCBF_GB_F32: batch_spline_one<float>(j, ch, sm, tab, 1 + w); break;
+        case PYCBF_GB_F16: batch_spline_one<__half>(j, ch, sm, tab, 1 + w); break;
+        default: batch_spline_one<__nv_bfloat16>(j, ch, sm, tab, 1 + w); break;
     }
 }
 
 template <typename T>
 static cudaError_t launch_spline_t(const SplineArgs &a, cudaStream_t s) {
-    const size_t per_warp = sizeof(float) * 2 * (size_t)((a.nt + 4) & ~3);
-    int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (72 * 1024) / per_warp));
-    const size_t smem = per_warp * wpb;
+    const size_t per_pair = sizeof(float) * 2 * (size_t)((a.nt + 4) & ~3);
+    const int ppb = (int)std::min<size_t>(4, std::max<size_t>(1, (72 * 1024) / per_pair));
+    const size_t smem = per_pair * ppb;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     static SplineTable tab = [] {
         SplineTable t;
@@ -175,9 +189,9 @@ static cudaError_t launch_spline_t(const SplineArgs &a, cudaStream_t s) {
     cudaError_t err = cudaFuncSetAttribute(spline_coef_kernel<T>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    const long long blocks = (a.nch + wpb - 1) / wpb;
+    const long long blocks = (a.nch + ppb - 1) / ppb;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
-    spline_coef_kernel<T><<<(unsigned)blocks, 32 * wpb, smem, s>>>(
+    spline_coef_kernel<T><<<(unsigned)blocks, 64 * ppb, smem, s>>>(
         static_cast<const T *>(a.rf), static_cast<typename CoefRec<T>::raw *>(a.coef), a.nch, a.nt,
         a.dt, tab);
     return cudaGetLastError();
@@ -186,9 +200,9 @@ static cudaError_t launch_spline_t(const SplineArgs &a, cudaStream_t s) {
 cudaError_t launch_batch_spline(const BatchJob *jobs, int njobs, long long nch_total, int max_nt,
                                 cudaStream_t s, bool set_attr) {
     const int stride = (max_nt + 4) & ~3;
-    const size_t per_warp = sizeof(float) * 2 * (size_t)stride;
-    const int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (72 * 1024) / per_warp));
-    const size_t smem = per_warp * wpb;
+    const size_t per_pair = sizeof(float) * 2 * (size_t)stride;
+    const int ppb = (int)std::min<size_t>(4, std::max<size_t>(1, (72 * 1024) / per_pair));
+    const size_t smem = per_pair * ppb;
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     static SplineTable tab = [] {
         SplineTable t;
@@ -201,9 +215,9 @@ cudaError_t launch_batch_spline(const BatchJob *jobs, int njobs, long long nch_t
         if (err != cudaSuccess) return err;
     }
     if (nch_total <= 0) return cudaSuccess;
-    const long long blocks = (nch_total + wpb - 1) / wpb;
+    const long long blocks = (nch_total + ppb - 1) / ppb;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
-    batch_spline_kernel<<<(unsigned)blocks, 32 * wpb, smem, s>>>(jobs, njobs, nch_total, stride, tab);
+    batch_spline_kernel<<<(unsigned)blocks, 64 * ppb, smem, s>>>(jobs, njobs, nch_total, stride, tab);
     return cudaGetLastError();
 }
 
