@@ -147,6 +147,15 @@ def das_tabbed(rf, tautx, apodtx, taurx, apodrx, t0, dt, nt, interp="cubic", usf
     assert rf.shape == (ntx, nrx, nt)
     size = out_size(sumtype, ntx, nrx, np_)
     if use_ref:
+        if threads > 1 and ntx > 1 and sumtype == "tx_and_rx":
+            # the reference's beamform_* are reentrant: transmits on threads with
+            # private images (ctypes releases the GIL), summed at the end
+            with ThreadPoolExecutor(min(threads, ntx)) as ex:
+                parts = list(ex.map(
+                    lambda t: _das_tabbed_ref(rf[t:t + 1], tautx[t:t + 1], apodtx[t:t + 1], taurx,
+                                              apodrx, t0, dt, nt, interp, usf, thresh, sumtype,
+                                              size), range(ntx)))
+            return np.sum(parts, axis=0, dtype=np.float32)
         return _das_tabbed_ref(rf, tautx, apodtx, taurx, apodrx, t0, dt, nt, interp, usf,
                                thresh, sumtype, size)
     L = lib()

@@ -61,6 +61,20 @@ def test_restatement_matches_compiled_reference(golden, name):
     np.testing.assert_array_equal(_run(case, "nearest"), _run(case, "nearest", use_ref=True))
 
 
+def test_threaded_reference_matches_serial(golden):
+    """The reference arm runs the compiled reference on threads over transmits
+    (private images, summed at the end): the same taps, another rounding order."""
+    if oracle.ref_lib() is None:
+        pytest.skip("the reference C library is not built here")
+    case = golden("tabbed_pw_small.npz")
+    args = (case["rf"], case["tautx"], case["apodtx"], case["taurx"], case["apodrx"],
+            float(case["t0"]), float(case["dt"]), int(case["nt"]))
+    serial = oracle.das_tabbed(*args, use_ref=True)
+    threaded = oracle.das_tabbed(*args, use_ref=True, threads=4)
+    ok = np.isfinite(serial)
+    assert oracle.rel_l2(threaded[ok], serial[ok]) <= 1e-6
+
+
 def test_threaded_oracle_same_taps(golden):
     case = golden("tabbed_pw_small.npz")
     one = _run(case, "cubic")
