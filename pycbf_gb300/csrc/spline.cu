@@ -137,9 +137,9 @@ spline_coef_kernel(const T *__restrict__ rf, typename CoefRec<T>::raw *__restric
                           smem + (size_t)pr * 2 * stride, 1 + pr);
 }
 
-// Batched: one warp per channel of any job (jobs' channels numbered
-// consecutively from BatchJob::ch0); smem per warp sized for the longest.
-// one channel per pair of warps, as spline_coef_kernel (the same records)
+// Batched: one pair of warps per channel of any job (jobs' channels numbered
+// consecutively from BatchJob::ch0), as spline_coef_kernel (the same
+// records); shared memory per pair sized for the longest channel.
 template <typename T>
 __device__ __forceinline__ void batch_spline_one(const BatchJob &j, long long ch, float *sm,
                                                  const SplineTable &tab, int bar) {
