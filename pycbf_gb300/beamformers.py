@@ -411,6 +411,66 @@ class _GPUBeamformer(Beamformer):
         out = self._beamform(txrxt, buffer)
         return out.cpu().numpy() if out_as_numpy else out
 
+    def beamform_stream(self, frames, sumtype=None):
+        """Beamform a sequence of frames held in host memory; yields NumPy
+        images in order (the images of __call__).
+
+        While frame k is beamformed, frame k+1 is copied to the device and the
+        image of frame k-1 back to the host, on a second stream: two device
+        slots for inputs and outputs, pinned host slots for the images (pinned
+        host frames make the input copies asynchronous too).  Each frame is
+        (ntx, nrx, nt) or (nframes, ntx, nrx, nt), NumPy or CPU torch, float or
+        int16.  Sustained throughput is that of the GPU work alone once the
+        copies are shorter than the beamform.
+        """
+        main = torch.cuda.current_stream()
+        copy = torch.cuda.Stream()
+        dev_in, dev_out, host_out = [None, None], [None, None], [None, None]
+        in_free = [None, None]    # main is done reading the input slot
+        out_home = [None, None]   # the slot's image has reached host memory
+        pending = None
+        for k, fr in enumerate(frames):
+            s = k % 2
+            t = fr if isinstance(fr, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(fr))
+            if t.is_cuda:
+                raise BeamformerException("beamform_stream takes frames in host memory")
+            if dev_in[s] is None or dev_in[s].shape != t.shape or dev_in[s].dtype != t.dtype:
+                torch.cuda.synchronize()  # no copy may still use a slot being replaced
+                dev_in[s] = torch.empty(t.shape, dtype=t.dtype, device="cuda")
+            with torch.cuda.stream(copy):
+                if in_free[s] is not None:
+                    copy.wait_event(in_free[s])
+                dev_in[s].copy_(t, non_blocking=True)
+                ready = torch.cuda.Event()
+                ready.record(copy)
+            main.wait_event(ready)
+            if out_home[s] is not None:
+                main.wait_event(out_home[s])  # frame k-2's image has left the output slot
+            nframes = t.shape[0] if t.ndim == 4 else None
+            shape = self._out_shape(nframes, sumtype)
+            if dev_out[s] is None or tuple(dev_out[s].shape) != tuple(shape):
+                dev_out[s] = torch.empty(shape, dtype=torch.float32, device="cuda")
+                host_out[s] = torch.empty(shape, dtype=torch.float32, pin_memory=True)
+            out = self._beamform(dev_in[s], dev_out[s], sumtype)
+            done = torch.cuda.Event()
+            done.record(main)
+            in_free[s] = done
+            with torch.cuda.stream(copy):
+                copy.wait_event(done)
+                host_out[s].copy_(out, non_blocking=True)
+                home = torch.cuda.Event()
+                home.record(copy)
+                out_home[s] = home
+            if pending is not None:
+                ps, pev = pending
+                pev.synchronize()
+                yield host_out[ps].numpy().copy()
+            pending = (s, out_home[s])
+        if pending is not None:
+            ps, pev = pending
+            pev.synchronize()
+            yield host_out[ps].numpy().copy()
+
 
 # ---------------------------------------------------------------------------
 # Tabbed
@@ -662,6 +722,9 @@ class _DMASMixin:
     the delay-and-sum kernel and the (nrx, np) intermediate never exists.
     """
 
+    def beamform_stream(self, frames, sumtype=None):
+        raise BeamformerException("beamform_stream is available for delay-and-sum beamformers")
+
     def _dmas_setup(self):
         self._lags_host = np.asarray(self.lags, dtype=np.int64).ravel()
         self._lags_dev = torch.as_tensor(self._lags_host.astype(np.int32), device="cuda")
@@ -720,6 +783,9 @@ class _SLSCMixin:
     mask is on for the whole axial kernel [iz-nkern, iz+nkern]; the result is
     the mean over lags 1..nlag of the nan-mean pair correlation.
     """
+
+    def beamform_stream(self, frames, sumtype=None):
+        raise BeamformerException("beamform_stream is available for delay-and-sum beamformers")
 
     def _slsc_setup(self):
         nx, nz = (int(v) for v in self.grid_shape)

@@ -359,3 +359,30 @@ def test_korder_large_k_and_edges(golden):
                               case["apodrx"], float(case["t0"]), float(case["dt"]), nt,
                               "korder_cubic", k=k)
         assert_image_close(out, ref, what=f"{name} k={k}")
+
+
+def test_beamform_stream_equals_calls(c1_small):
+    """Frames streamed from host memory with overlapped copies give the images
+    of one call per frame, bit for bit (float32 pinned and pageable, int16,
+    4-D frames)."""
+    bf = bf_for(c1_small, "cubic")
+    rng = np.random.default_rng(7)
+    rf = c1_small["rf"]
+    frames = [rf, (rf * 0.5).astype(np.float32), torch.from_numpy(rf[::-1].copy()).pin_memory(),
+              rng.normal(size=rf.shape).astype(np.float32)]
+    got = list(bf.beamform_stream(frames))
+    assert len(got) == len(frames)
+    for g, f in zip(got, frames):
+        np.testing.assert_array_equal(g, bf(f))
+    counts = [np.round(rf / np.abs(rf).max() * 30000).astype(np.int16)] * 3
+    for g, f in zip(bf.beamform_stream(counts), counts):
+        np.testing.assert_array_equal(g, bf(f))
+    four = np.stack([rf, rf[::-1].copy()])
+    (g,) = list(bf.beamform_stream([four]))
+    np.testing.assert_array_equal(g, bf(four))
+    dm = pg.TabbedDMASBeamformer(tautx=c1_small["tautx"], taurx=c1_small["taurx"],
+                                 apodtx=c1_small["apodtx"], apodrx=c1_small["apodrx"],
+                                 t0=float(c1_small["t0"]), dt=float(c1_small["dt"]),
+                                 nt=int(c1_small["nt"]))
+    with pytest.raises(pg.BeamformerException):
+        list(dm.beamform_stream([rf]))
