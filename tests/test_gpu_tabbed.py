@@ -383,6 +383,6 @@ def test_beamform_stream_equals_calls(c1_small):
     dm = pg.TabbedDMASBeamformer(tautx=c1_small["tautx"], taurx=c1_small["taurx"],
                                  apodtx=c1_small["apodtx"], apodrx=c1_small["apodrx"],
                                  t0=float(c1_small["t0"]), dt=float(c1_small["dt"]),
-                                 nt=int(c1_small["nt"]))
+                                 nt=int(c1_small["nt"]), lags=np.arange(1, 4))
     with pytest.raises(pg.BeamformerException):
         list(dm.beamform_stream([rf]))
