@@ -416,15 +416,17 @@ class _GPUBeamformer(Beamformer):
         images in order (the images of __call__).
 
         While frame k is beamformed, frame k+1 is copied to the device and the
-        image of frame k-1 back to the host, on a second stream: two device
-        slots for inputs and outputs, pinned host slots for the images (pinned
-        host frames make the input copies asynchronous too).  Each frame is
+        image of frame k-1 back to the host, each direction on a stream of its
+        own (an image copy waits for its beamform, and must not hold up the
+        next frame's input copy): two device slots for inputs and outputs,
+        pinned host slots for the images (pinned host frames make the input
+        copies asynchronous too).  Each frame is
         (ntx, nrx, nt) or (nframes, ntx, nrx, nt), NumPy or CPU torch, float or
         int16.  Sustained throughput is that of the GPU work alone once the
         copies are shorter than the beamform.
         """
         main = torch.cuda.current_stream()
-        copy = torch.cuda.Stream()
+        copy, back = torch.cuda.Stream(), torch.cuda.Stream()
         dev_in, dev_out, host_out = [None, None], [None, None], [None, None]
         in_free = [None, None]    # main is done reading the input slot
         out_home = [None, None]   # the slot's image has reached host memory
@@ -455,11 +457,11 @@ class _GPUBeamformer(Beamformer):
             done = torch.cuda.Event()
             done.record(main)
             in_free[s] = done
-            with torch.cuda.stream(copy):
-                copy.wait_event(done)
+            with torch.cuda.stream(back):
+                back.wait_event(done)
                 host_out[s].copy_(out, non_blocking=True)
                 home = torch.cuda.Event()
-                home.record(copy)
+                home.record(back)
                 out_home[s] = home
             if pending is not None:
                 ps, pev = pending
