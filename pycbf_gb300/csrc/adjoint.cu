@@ -99,11 +99,14 @@ __global__ void __launch_bounds__(kBlock) adj_delay_kernel(const __grid_constant
         for (int k = 0; k < a.ndim; ++k) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
         slow = __ldg(a.slow + i);
     }
+    float amax = 0.f;
     for (int t = 0; t < ntx; ++t) {
         if (GEOM == GEOM_TABBED) {
             stau[(size_t)t * kBlock] = __ldg(a.tautx + (long long)t * np + i);
-            sw[(size_t)t * kBlock] = __ldg(a.apodtx + (long long)t * np + i);
+            const float at = __ldg(a.apodtx + (long long)t * np + i);
+            sw[(size_t)t * kBlock] = at;
             sg[(size_t)t * kBlock] = 0.f;
+            amax = fmaxf(amax, fabsf(at));
         } else {
             float D, t0add;
             const bool ok = synth_tx_path(a, t, pnt, D, t0add);
@@ -118,6 +121,11 @@ __global__ void __launch_bounds__(kBlock) adj_delay_kernel(const __grid_constant
         if (GEOM == GEOM_TABBED) {
             trx = __ldg(a.taurx + (long long)r * np + i);
             arx = __ldg(a.apodrx + (long long)r * np + i);
+            // the forward's exact reject: no tap of this receive passes the threshold
+            if (__fmul_rn(amax, fabsf(arx)) < a.thresh) {
+                if (g.grad_taurx) g.grad_taurx[(long long)r * np + i] = 0.f;
+                continue;
+            }
         } else {
             const bool ok = synth_rx_path(a, r, pnt, Drx);
             if (!ok) continue;
