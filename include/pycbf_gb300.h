@@ -415,9 +415,12 @@ int pycbf_gb_das_synthetic_adjoint(const pycbf_gb_rfinfo *rf, const void *coef,
 /* (order 1).  It fills *info, which pycbf_gb_batch_run needs.             */
 /* pycbf_gb_batch_run queues the prefilter and the delay-and-sum on the   */
 /* stream: tx_chunk (4, 8 or 12) transmits are held in registers at a      */
-/* time; ctas CTAs of 128 threads serve the queue.  With ntx <= tx_chunk   */
-/* a job's image is bitwise the one pycbf_gb_das_tabbed /                  */
-/* pycbf_gb_das_synthetic give for its frame.  run allocates nothing and   */
+/* time, or (tx_chunk 0) each pixel runs the single-frame kernel's own     */
+/* body (transmits in registers up to 12, in shared memory beyond:         */
+/* info->max_ntx sizes it); ctas CTAs of 128 threads serve the queue.      */
+/* With tx_chunk 0, or ntx <= tx_chunk, a job's image is bitwise the one   */
+/* pycbf_gb_das_tabbed / pycbf_gb_das_synthetic give for its frame.  run   */
+/* allocates nothing and                                                   */
 /* makes no host-blocking call, so it can be captured in a CUDA graph once */
 /* plan has run; rerunning it (or the graph) reuses the plan's buffers.    */
 /* ---------------------------------------------------------------------- */
@@ -440,6 +443,7 @@ typedef struct pycbf_gb_batch_info {
     int njobs;
     int max_nt;
     int tiles_per_item;
+    int max_ntx;
 } pycbf_gb_batch_info;
 
 size_t pycbf_gb_batch_plan_bytes(const pycbf_gb_batch_job *jobs, int njobs, int tiles_per_item);

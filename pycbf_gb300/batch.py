@@ -35,11 +35,11 @@ __all__ = ["BatchBeamformer", "BatchConfig", "beamformers_for"]
 class BatchConfig:
     tiles_per_item: int = 1      # 128-pixel tiles per work item
     order: int = 1               # 0 frame order, 1 largest estimated cost first
-    tx_chunk: int = 12           # transmits per register chunk (4, 8, 12)
+    tx_chunk: int = 12           # transmits per register chunk (4, 8, 12); 0: the single-frame body
     ctas_per_sm: int = 4         # CTAs of 128 threads per SM serving the queue
 
 
-SEARCH_SPACE = dict(tx_chunk=(12, 8, 4), tiles_per_item=(1, 2, 4), order=(1, 0),
+SEARCH_SPACE = dict(tx_chunk=(12, 0, 8, 4), tiles_per_item=(1, 2, 4), order=(1, 0),
                     ctas_per_sm=(4, 3, 2))
 _TUNED: dict = {}
 

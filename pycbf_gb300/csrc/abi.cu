@@ -618,7 +618,7 @@ int pycbf_gb_batch_plan(const pycbf_gb_batch_job *jobs, int njobs, int tiles_per
     std::vector<int2> items;
     std::vector<double> cost;
     long long ch0 = 0;
-    int max_nt = 1;
+    int max_nt = 1, max_ntx = 1;
     for (int k = 0; k < njobs; ++k) {
         const pycbf_gb_batch_job &j = jobs[k];
         BatchJob &b = desc[(size_t)k];
@@ -645,6 +645,7 @@ int pycbf_gb_batch_plan(const pycbf_gb_batch_job *jobs, int njobs, int tiles_per
         b.dtype = j.rf.dtype;
         ch0 += j.rf.ntx * j.rf.nrx;
         max_nt = std::max(max_nt, j.rf.nt);
+        max_ntx = std::max(max_ntx, (int)j.rf.ntx);
         const long long n = job_items(j, tiles_per_item);
         // relative cost of an item: its taps, synthetic delays weighted up
         const double c = (double)j.rf.ntx * (double)j.rf.nrx * (j.geom == 1 ? 1.3 : 1.0);
@@ -679,7 +680,10 @@ int pycbf_gb_batch_plan(const pycbf_gb_batch_job *jobs, int njobs, int tiles_per
     info->njobs = njobs;
     info->max_nt = max_nt;
     info->tiles_per_item = tiles_per_item;
-    // shared-memory size of the batched prefilter, set outside any capture
+    info->max_ntx = max_ntx;
+    // shared-memory sizes of the batched prefilter and delay-and-sum, set outside any capture
+    st = cuda_status(prepare_batch_das(max_ntx));
+    if (st) return st;
     return cuda_status(launch_batch_spline(reinterpret_cast<const BatchJob *>(base + kBatchHeader),
                                            njobs, 0, max_nt, s, true));
 }
@@ -688,7 +692,8 @@ int pycbf_gb_batch_run(const void *plan, const pycbf_gb_batch_info *info, int tx
                        void *stream) {
     if (!plan || !info || info->njobs <= 0 || info->nitems < 0 || info->max_nt <= 0)
         return PYCBF_GB_EINVAL;
-    if (tx_chunk != 4 && tx_chunk != 8 && tx_chunk != 12) return PYCBF_GB_EINVAL;
+    if (tx_chunk != 0 && tx_chunk != 4 && tx_chunk != 8 && tx_chunk != 12) return PYCBF_GB_EINVAL;
+    if (tx_chunk == 0 && (info->max_ntx < 1 || info->max_ntx > (1 << 20))) return PYCBF_GB_EINVAL;
     if (ctas < 1 || ctas > (1 << 20) || info->tiles_per_item < 1 || info->tiles_per_item > 8)
         return PYCBF_GB_EINVAL;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -702,7 +707,7 @@ int pycbf_gb_batch_run(const void *plan, const pycbf_gb_batch_info *info, int tx
                                              false));
     if (st) return st;
     return cuda_status(launch_batch_das(jobs, items, info->nitems, info->tiles_per_item, counter,
-                                        tx_chunk, ctas, s));
+                                        tx_chunk, ctas, s, info->max_ntx));
 }
 
 }  // extern "C"

@@ -8,11 +8,11 @@
 // CTAs takes them from a queue head in global memory until it runs dry, so
 // frames of very different cost share the GPU without a launch per frame.
 //
-// Per pixel the transmits are taken TXC at a time into registers (TXC is
-// the transmit-chunk shape the autotuner picks among 4, 8 and 12); for each
-// chunk every receive adds its chunk sum to the pixel's accumulator.  With
-// one chunk (ntx <= TXC) the order of operations and the tap decisions are
-// those of the single-frame kernel, so the images are bitwise the same.
+// Two per-pixel forms, which the autotuner chooses between: the transmits
+// taken TXC at a time into registers (TXC 4, 8 or 12; for each chunk every
+// receive adds its chunk sum to the pixel's accumulator, so with one chunk,
+// ntx <= TXC, the images are bitwise the single-frame ones), or (tx_chunk 0)
+// the single-frame kernel's own body, bitwise the same for every ntx.
 #include "das_impl.cuh"
 
 namespace pgb {
@@ -165,15 +165,70 @@ batch_das_kernel(const BatchJob *__restrict__ jobs, const int2 *__restrict__ ite
     }
 }
 
+// The same queue, each pixel run by the single-frame kernel's body
+// (das_pixel): transmits in registers up to kTxReg, in the thread's column of
+// shared memory beyond, every receive's delay and reject computed once.  The
+// images are bitwise those of the single-frame calls for every ntx.
+__global__ void __launch_bounds__(kBlock, 4)
+batch_das_full_kernel(const BatchJob *__restrict__ jobs, const int2 *__restrict__ items,
+                      long long nitems, int tiles_per_item, unsigned long long *counter) {
+    extern __shared__ float sm[];
+    __shared__ __align__(16) BatchJob s_job;
+    __shared__ long long s_k;
+    constexpr int kWords = (int)(sizeof(BatchJob) / sizeof(int));
+    constexpr int CUB = PYCBF_GB_INTERP_CUBIC, SUM = PYCBF_GB_SUM_TX_AND_RX;
+    for (;;) {
+        if (threadIdx.x == 0) s_k = (long long)atomicAdd(counter, 1ULL);
+        __syncthreads();
+        const long long k = s_k;
+        if (k >= nitems) break;
+        const int2 it = __ldg(items + k);
+        const int *src = reinterpret_cast<const int *>(jobs + it.x);
+        int *dst = reinterpret_cast<int *>(&s_job);
+        for (int w = threadIdx.x; w < kWords; w += blockDim.x) dst[w] = __ldg(src + w);
+        __syncthreads();
+        const int geom = s_job.geom, dtype = s_job.dtype;
+        for (int sub = 0; sub < tiles_per_item; ++sub) {
+            const long long i = ((long long)it.y * tiles_per_item + sub) * kBlock + threadIdx.x;
+            if (geom == GEOM_TABBED) {
+                if (dtype == PYCBF_GB_F32) das_pixel<GEOM_TABBED, CUB, SUM, float, false>(s_job.a, i, 0, sm);
+                else if (dtype == PYCBF_GB_F16) das_pixel<GEOM_TABBED, CUB, SUM, __half, false>(s_job.a, i, 0, sm);
+                else das_pixel<GEOM_TABBED, CUB, SUM, __nv_bfloat16, false>(s_job.a, i, 0, sm);
+            } else {
+                if (dtype == PYCBF_GB_F32) das_pixel<GEOM_SYNTH, CUB, SUM, float, false>(s_job.a, i, 0, sm);
+                else if (dtype == PYCBF_GB_F16) das_pixel<GEOM_SYNTH, CUB, SUM, __half, false>(s_job.a, i, 0, sm);
+                else das_pixel<GEOM_SYNTH, CUB, SUM, __nv_bfloat16, false>(s_job.a, i, 0, sm);
+            }
+        }
+        __syncthreads();  // every thread is done with s_job and s_k
+    }
+}
+
 }  // namespace
+
+size_t batch_full_smem_bytes(int max_ntx) {
+    return das_smem_bytes(GEOM_TABBED, PYCBF_GB_SUM_TX_AND_RX, max_ntx);
+}
+
+cudaError_t prepare_batch_das(int max_ntx) {
+    const size_t smem = batch_full_smem_bytes(max_ntx);
+    if (smem > 227 * 1024) return cudaErrorInvalidValue;
+    return cudaFuncSetAttribute(batch_das_full_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)std::max<size_t>(smem, 48 * 1024));
+}
 
 cudaError_t launch_batch_das(const BatchJob *jobs, const int2 *items, long long nitems,
                              int tiles_per_item, unsigned long long *counter, int tx_chunk,
-                             int ctas, cudaStream_t s) {
+                             int ctas, cudaStream_t s, int max_ntx) {
     cudaError_t err = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
     if (err != cudaSuccess) return err;
     if (nitems <= 0) return cudaSuccess;
     const unsigned grid = (unsigned)std::max(1, ctas);
+    if (tx_chunk == 0) {  // shared-memory size set by prepare_batch_das, outside any capture
+        batch_das_full_kernel<<<grid, kBlock, batch_full_smem_bytes(max_ntx), s>>>(
+            jobs, items, nitems, tiles_per_item, counter);
+        return cudaGetLastError();
+    }
     switch (tx_chunk) {
         case 4: batch_das_kernel<4><<<grid, kBlock, 0, s>>>(jobs, items, nitems, tiles_per_item, counter); break;
         case 8: batch_das_kernel<8><<<grid, kBlock, 0, s>>>(jobs, items, nitems, tiles_per_item, counter); break;

@@ -313,14 +313,14 @@ __device__ __forceinline__ float synth_rx_delay(const DasArgs &a, int r, const f
 // ---------------------------------------------------------------------------
 constexpr int kGroup = 6;  // taps whose gathers a thread keeps in flight together
 
+// One pixel (table column i of frame f) of the generic delay-and-sum: the
+// body of das_kernel, also run by the batched kernel for each of its jobs.
+// sm: the CTA's dynamic shared memory (das_smem_bytes), a column per thread.
 template <int GEOM, int KIND, int SUM, typename T, bool CENSUS>
-__global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ DasArgs a) {
+__device__ __forceinline__ void das_pixel(const DasArgs &a, long long i, int f, float *sm) {
     using K = Kind<KIND, T>;
-    extern __shared__ float sm[];
     const int tid = threadIdx.x;
-    const long long i = (long long)blockIdx.x * kBlock + tid;
     if (i >= a.np) return;
-    const int f = blockIdx.y;
     const long long np = a.np;
     const int ntx = a.ntx, nrx = a.nrx;
     const long long op = a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i;
@@ -546,6 +546,13 @@ __global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ 
         a.census_count[i] = cnt;
         a.census_isum[i] = isum;
     }
+}
+
+template <int GEOM, int KIND, int SUM, typename T, bool CENSUS>
+__global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ DasArgs a) {
+    extern __shared__ float sm[];
+    das_pixel<GEOM, KIND, SUM, T, CENSUS>(a, (long long)blockIdx.x * kBlock + threadIdx.x,
+                                          (int)blockIdx.y, sm);
 }
 
 inline size_t das_smem_bytes(int geom, int sum, int ntx) {
