@@ -1,20 +1,23 @@
-"""Uneven batches of frames in one persistent launch, replayed as a CUDA graph
-(no counterpart in the reference, whose beamformers take one frame shape per
-instance and launch per call).
+"""Uneven batches of frames replayed as one CUDA graph (no counterpart in the
+reference, whose beamformers take one frame shape per instance and launch per
+call).
 
 ``BatchBeamformer(beamformers)`` takes a list of Tabbed / Synthetic
 beamformers, one entry per frame (an instance may appear several times for
 several frames); frames may differ in ntx, nrx, nt, pixel count and channel
 data storage type.  It owns one input buffer per frame, the spline workspaces
-and the output images; a call copies the frames in, replays a CUDA graph of
-two launches (the batched prefilter and the persistent delay-and-sum of
-pycbf_gb_batch_run) and returns the images (cubic interpolation, summed over
-transmits and receives, the 'tx_and_rx' image of each beamformer).
+and the output images; a call copies the frames in, replays a CUDA graph and
+returns the images (cubic interpolation, summed over transmits and receives,
+the 'tx_and_rx' image of each beamformer).  The graph holds either two
+launches -- the batched prefilter and the persistent delay-and-sum of
+pycbf_gb_batch_run, every frame's tiles taken from one queue -- or every
+frame's own single-frame launches (the staged kernel for Tabbed frames with a
+plan) on a few concurrent branches.
 
-The launch shape -- pixel tiles per work item, work order, transmits held in
-registers per chunk, CTAs per SM -- is chosen by ``autotune``: a coordinate
-search timed with CUDA events on the batch itself, cached per batch
-signature for the life of the process.
+The form and its launch shape -- branches, pixel tiles per work item, work
+order, transmits held in registers per chunk, CTAs per SM -- are chosen by
+``autotune``: a coordinate search timed with CUDA events on the batch
+itself, cached per batch signature for the life of the process.
 """
 from __future__ import annotations
 
@@ -37,10 +40,12 @@ class BatchConfig:
     order: int = 1               # 0 frame order, 1 largest estimated cost first
     tx_chunk: int = 12           # transmits per register chunk (4, 8, 12); 0: the single-frame body
     ctas_per_sm: int = 4         # CTAs of 128 threads per SM serving the queue
+    branches: int = 0            # > 0: instead of the queue, each frame's own single-frame
+                                 # launches, on this many concurrent graph branches
 
 
-SEARCH_SPACE = dict(tx_chunk=(12, 0, 8, 4), tiles_per_item=(1, 2, 4), order=(1, 0),
-                    ctas_per_sm=(4, 3, 2))
+SEARCH_SPACE = dict(branches=(0, 4, 8), tx_chunk=(12, 0, 8, 4), tiles_per_item=(1, 2, 4),
+                    order=(1, 0), ctas_per_sm=(4, 3, 2))
 _TUNED: dict = {}
 
 
@@ -96,6 +101,7 @@ class BatchBeamformer:
         self._jobs = (_lib.BatchJob * len(jobs))(*jobs)
         self.taps = sum(bf.ntx * bf.nrx * bf.nop for bf in self.beamformers)
         self._plans: dict = {}
+        self._streams: list = []
         self._graph = None
         if config is None:
             config = self.autotune() if autotune else BatchConfig()
@@ -119,14 +125,70 @@ class BatchBeamformer:
             self._plans[key] = (buf, info)
         return self._plans[key]
 
+    def _launch_frame(self, k: int):
+        """Frame k with the single-frame launches of its beamformer (the staged
+        kernel for Tabbed frames with a plan), on the current stream."""
+        bf = self.beamformers[k]
+        rf, coef, out = self.inputs[k], self._coef[k], self.outputs[k]
+        L, stream = self._lib, _stream()
+        tabbed = isinstance(bf, TabbedBeamformer)
+        info = bf._rfinfo(1, 0 if tabbed else bf.ndimp)
+        if tabbed:
+            tautx, apodtx, taurx, apodrx = bf._tables
+            st = L.pycbf_gb_spline_coefficients(ct.byref(info), _ptr(rf), _ptr(coef), coef.numel(),
+                                                stream)
+            _lib.check(st, "pycbf_gb_spline_coefficients")
+            st = L.pycbf_gb_das_tabbed_prefiltered(
+                ct.byref(info), _ptr(coef), _ptr(tautx), _ptr(apodtx), _ptr(taurx), _ptr(apodrx),
+                bf.nop, _ptr(bf._pixel_index), float(np.float32(bf.thresh)), 3, _ptr(bf._plan),
+                _ptr(out), stream)
+            _lib.check(st, "pycbf_gb_das_tabbed_prefiltered")
+        else:
+            st = L.pycbf_gb_das_synthetic(ct.byref(info), _ptr(rf), ct.byref(bf._geom),
+                                          _ptr(bf._pixel_index), _lib.INTERP["cubic"], 3, _ptr(out),
+                                          _ptr(coef), coef.numel(), stream)
+            _lib.check(st, "pycbf_gb_das_synthetic")
+
+    def _run_branches(self, nbranch: int):
+        """Every frame's own launches, frames of one beamformer in order on one
+        branch (they share its plan), beamformers spread over nbranch streams by
+        their taps (largest first onto the least loaded branch)."""
+        while len(self._streams) < nbranch:
+            self._streams.append(torch.cuda.Stream())
+        streams = self._streams[:nbranch]
+        groups: dict = {}
+        for k, bf in enumerate(self.beamformers):
+            groups.setdefault(id(bf), []).append(k)
+        cost = {g: sum(self.beamformers[k].ntx * self.beamformers[k].nrx * self.beamformers[k].nop
+                       for k in ks) for g, ks in groups.items()}
+        load = [0] * nbranch
+        cur = torch.cuda.current_stream()
+        fork = torch.cuda.Event()
+        fork.record(cur)
+        for st in streams:
+            st.wait_event(fork)
+        for g in sorted(groups, key=lambda g: -cost[g]):
+            b = min(range(nbranch), key=lambda i: load[i])
+            load[b] += cost[g]
+            with torch.cuda.stream(streams[b]):
+                for k in groups[g]:
+                    self._launch_frame(k)
+        for st in streams:
+            join = torch.cuda.Event()
+            join.record(st)
+            cur.wait_event(join)
+
     def _run(self, cfg: BatchConfig):
+        if cfg.branches > 0:
+            self._run_branches(cfg.branches)
+            return
         buf, info = self._plan(cfg.tiles_per_item, cfg.order)
         st = self._lib.pycbf_gb_batch_run(_ptr(buf), ct.byref(info), cfg.tx_chunk,
                                           cfg.ctas_per_sm * self.n_sm, _stream())
         _lib.check(st, "pycbf_gb_batch_run")
 
     def set_config(self, cfg: BatchConfig):
-        """Use cfg and capture the CUDA graph of its two launches."""
+        """Use cfg and capture the CUDA graph of its launches."""
         self.config = cfg
         self._run(cfg)  # warm (plans, attributes) outside the capture
         torch.cuda.synchronize()

@@ -48,13 +48,14 @@ def _rel(a, b):
 
 
 @pytest.mark.parametrize("cfg", [BatchConfig(), BatchConfig(2, 0, 8, 2), BatchConfig(4, 1, 4, 3),
-                                 BatchConfig(1, 1, 0, 4), BatchConfig(2, 0, 0, 2)])
+                                 BatchConfig(1, 1, 0, 4), BatchConfig(2, 0, 0, 2),
+                                 BatchConfig(branches=4), BatchConfig(branches=1)])
 def test_batch_matches_single_frames(batch, cfg):
     bfs, frames, singles = batch
     bb = BatchBeamformer(bfs, config=cfg)
     outs = bb(frames)
     for k, (o, s, bf) in enumerate(zip(outs, singles, bfs)):
-        if cfg.tx_chunk == 0 or bf.ntx <= cfg.tx_chunk:
+        if cfg.branches > 0 or cfg.tx_chunk == 0 or bf.ntx <= cfg.tx_chunk:
             assert torch.equal(o, s), (k, _rel(o, s))  # same operations in the same order
         else:
             assert _rel(o, s) <= 1e-6, (k, _rel(o, s))
