@@ -217,13 +217,15 @@ class BatchBeamformer:
             self.timings = _TUNED[sig][1]
             return _TUNED[sig][0]
         space = space or SEARCH_SPACE
+        # with branches the queue's fields do not apply: one config per branch count
+        canon = lambda c: BatchConfig(branches=c.branches) if c.branches > 0 else c
         best = BatchConfig()
         best_t = self.time_config(best, reps)
         timings = {best: best_t}
         for _ in range(2):
             for name, values in space.items():
                 for v in values:
-                    cand = BatchConfig(**{**best.__dict__, name: v})
+                    cand = canon(BatchConfig(**{**best.__dict__, name: v}))
                     if cand not in timings:
                         timings[cand] = self.time_config(cand, reps)
                     if timings[cand] < best_t:
