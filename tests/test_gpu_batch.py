@@ -77,7 +77,9 @@ def test_graph_replay_follows_the_inputs(batch):
 def test_autotuner_picks_and_caches(batch):
     bfs, frames, singles = batch
     bb = BatchBeamformer(bfs)  # autotunes
-    assert isinstance(bb.config, BatchConfig) and len(bb.timings) >= 6
+    # the queue form and two branch counts at least
+    assert isinstance(bb.config, BatchConfig) and len(bb.timings) >= 3
+    assert {c.branches for c in bb.timings} >= {0, 4, 8}
     assert bb.config == min(bb.timings, key=bb.timings.get)
     bb2 = BatchBeamformer(bfs)
     assert bb2.config == bb.config
