@@ -158,12 +158,16 @@ int pycbf_gb_das_tabbed(const pycbf_gb_rfinfo *rf, const void *rfdata, const flo
 
 /* Staging plan of a Tabbed table set (no counterpart in the reference: it  */
 /* precomputes, per tile of 128 table columns, the receives that can        */
-/* contribute and the delay bounds that size each channel window).  plan    */
-/* needs pycbf_gb_tabbed_plan_bytes bytes, 16-byte aligned; ntx <= 12.      */
-/* Its first int32 is a status word: 0, or 1 after a kernel gave up a       */
-/* bounded wait (its outputs are then NaN).  Its second is the work-queue   */
-/* head of the staged kernel, reset by every call that uses the plan: calls */
-/* sharing one plan must not overlap on the GPU.                           */
+/* contribute and the delay bounds that size each channel window, the tile  */
+/* order, and the (tile, block of 64 receives) work items of single-frame   */
+/* calls).  plan needs pycbf_gb_tabbed_plan_bytes bytes, 16-byte aligned;   */
+/* ntx <= 12.  Its first int32 is a status word: 0, or 1 after a kernel     */
+/* gave up a bounded wait (its outputs are then NaN).  Its second is the    */
+/* work-queue head of the staged kernel; the plan also holds per-tile       */
+/* counters and one frame's block partial sums, all reset or rewritten by   */
+/* every call that uses the plan: calls sharing one plan must not overlap   */
+/* on the GPU.  Images are sums over blocks of 64 receives (in order) of    */
+/* each block's sequential sum, with or without a plan.                     */
 size_t pycbf_gb_tabbed_plan_bytes(long long np, int ntx, int nrx);
 int pycbf_gb_tabbed_plan(const pycbf_gb_rfinfo *rf, const float *tautx, const float *apodtx,
                          const float *taurx, const float *apodrx, long long np, int interp,
