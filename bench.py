@@ -322,13 +322,25 @@ def main_ours(a):
                 "kernel_ms": 1e3 * das_s, "spline_ms": statistics.mean(spline_ms),
                 "peak_source": "measured" if peaks.get("hbm_gbs") else "fallback",
                 "algorithmic_bytes": alg_bytes}
-    # DRAM bytes of one launch from the committed ncu summary of this kernel and workload
+    # DRAM bytes and warp instructions of one launch from the committed ncu summary
+    # of this kernel and workload; the kernel is issue-bound, so the share of the
+    # schedulers' issue slots it uses is reported beside the HBM fraction
     prof = os.path.join(ROOT, "profiles", "das_tabbed_cubic_c1.md")
     if os.path.exists(prof):
         with open(prof) as fp:
-            m = re.search(r"dram bytes per launch \(read \+ write\): (\d+)", fp.read())
+            text = fp.read()
+        m = re.search(r"dram bytes per launch \(read \+ write\): (\d+)", text)
         if m:
             roofline["traffic"] = int(m.group(1))
+        m = re.search(r"\| smsp__inst_executed\.sum \| ([0-9.]+) M \|", text)
+        sm_mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
+        if m and sm_mhz:
+            n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+            slots = 4 * n_sm * sm_mhz * 1e6 * das_s
+            roofline["issue"] = {"warp_instructions": float(m.group(1)) * 1e6,
+                                 "frac": float(m.group(1)) * 1e6 / slots,
+                                 "note": "instructions from the profile, one issue per scheduler "
+                                         "per cycle at the sampled SM clock"}
     # FP32 roofline: algorithmic FLOPs (20 per contributing cubic tap, 2 per tap for the
     # weight product and threshold) over the kernel time, against the FMA probe
     probe_out = torch.empty(152 * 8 * 256, device=dev)
