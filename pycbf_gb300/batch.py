@@ -44,7 +44,7 @@ class BatchConfig:
                                  # launches, on this many concurrent graph branches
 
 
-SEARCH_SPACE = dict(branches=(0, 4, 8), tx_chunk=(12, 0, 8, 4), tiles_per_item=(1, 2, 4),
+SEARCH_SPACE = dict(branches=(0, 4, 8, 16), tx_chunk=(12, 0, 8, 4), tiles_per_item=(1, 2, 4),
                     order=(1, 0), ctas_per_sm=(4, 3, 2))
 _TUNED: dict = {}
 
