@@ -276,46 +276,46 @@ __global__ void __launch_bounds__(128) adj_scatter_kernel(const __grid_constant_
         while (b < i1 && !rx_live[b / kBlock]) b += blockDim.x;
         return b;
     };
-    In cur = {{0.f, 0.f, 0.f, 0.f}, 0.f}, nxt = cur;
-    long long nbase = next_live(i0);
-    if (nbase < i1) fetch(nbase + threadIdx.x, cur);
-    for (long long base = nbase; base < i1; base = nbase) {  // `continue` advances too
+    // one live step's tap of this lane: knot, fractions and the weighted gradient
+    struct Tap {
+        bool hit;
+        int j;
+        float am, b, v;
+    };
+    auto tap_of = [&](long long base, const In &in) {
+        Tap tp = {false, 0, 0.f, 0.f, 0.f};
         const long long i = base + threadIdx.x;
-        nbase = next_live(base + blockDim.x);
-        if (nbase < i1) fetch(nbase + threadIdx.x, nxt);
-        bool hit = false;
-        int j = 0;
-        float am = 0.f, b = 0.f, v = 0.f;
-        if (i < i1) {
-            float x = 0.f, apod = 1.f;
-            bool live;
-            if (GEOM == GEOM_TABBED) {
-                apod = __fmul_rn(cur.v[0], cur.v[1]);
-                live = fabsf(apod) >= a.thresh;
-                x = __fadd_rn(cur.v[2], cur.v[3]);
-            } else {
-                const float pnt[3] = {cur.v[0], cur.v[1], cur.v[2]};
-                float Dt, t0add, Dr;
-                const bool okt = synth_tx_path(a, t, pnt, Dt, t0add);
-                const bool okr = synth_rx_path(a, r, pnt, Dr);
-                live = okt && okr;
-                x = __fadd_rn(slow_delay(true, Dt, cur.v[3], t0add),
-                              slow_delay(true, Dr, cur.v[3], 0.f));
-            }
-            if (live && cubic_tap(x, a, j, am, b)) {
-                hit = true;
-                v = (GEOM == GEOM_TABBED) ? cur.gp * apod : cur.gp;
-            }
+        if (base >= i1 || i >= i1) return tp;
+        float x = 0.f, apod = 1.f;
+        bool live;
+        if (GEOM == GEOM_TABBED) {
+            apod = __fmul_rn(in.v[0], in.v[1]);
+            live = fabsf(apod) >= a.thresh;
+            x = __fadd_rn(in.v[2], in.v[3]);
+        } else {
+            const float pnt[3] = {in.v[0], in.v[1], in.v[2]};
+            float Dt, t0add, Dr;
+            const bool okt = synth_tx_path(a, t, pnt, Dt, t0add);
+            const bool okr = synth_rx_path(a, r, pnt, Dr);
+            live = okt && okr;
+            x = __fadd_rn(slow_delay(true, Dt, in.v[3], t0add), slow_delay(true, Dr, in.v[3], 0.f));
         }
-        cur = nxt;
-        if (!__any_sync(kFull, hit)) continue;
-        // group the warp's taps by knot; the lowest lane of a group sums the
-        // group's weights in lane order
-        const unsigned grp = __match_any_sync(kFull, hit ? j : -1);
+        if (live && cubic_tap(x, a, tp.j, tp.am, tp.b)) {
+            tp.hit = true;
+            tp.v = (GEOM == GEOM_TABBED) ? in.gp * apod : in.gp;
+        }
+        return tp;
+    };
+    // the warp's taps of one step into its rows: grouped by knot, the lowest
+    // lane of a group sums the group's weights in lane order
+    auto scatter = [&](const Tap &tp) {
+        if (!__any_sync(kFull, tp.hit)) return;
+        const unsigned grp = __match_any_sync(kFull, tp.hit ? tp.j : -1);
         const int n = __popc(grp);
-        const int nmax = (int)__reduce_max_sync(kFull, hit ? (unsigned)n : 0u);
-        const float wa = v * am, wb = v * b;
-        const float wc = v * fmaf(am * am, am, -am), wd = v * fmaf(b * b, b, -b);
+        const int nmax = (int)__reduce_max_sync(kFull, tp.hit ? (unsigned)n : 0u);
+        const float wa = tp.v * tp.am, wb = tp.v * tp.b;
+        const float wc = tp.v * fmaf(tp.am * tp.am, tp.am, -tp.am);
+        const float wd = tp.v * fmaf(tp.b * tp.b, tp.b, -tp.b);
         float A = wa, B = wb, C = wc, D = wd;
         unsigned rest = grp & (grp - 1u);
         for (int k = 1; k < nmax; ++k) {
@@ -330,17 +330,39 @@ __global__ void __launch_bounds__(128) adj_scatter_kernel(const __grid_constant_
                 D += xd;
             }
         }
-        const bool leader = hit && (lane == __ffs(grp) - 1);
+        const bool leader = tp.hit && (lane == __ffs(grp) - 1);
         if (leader) {
-            ry[j] += A;
-            rz[j] += C;
+            ry[tp.j] += A;
+            rz[tp.j] += C;
         }
         __syncwarp();
         if (leader) {
-            ry[j + 1] += B;
-            rz[j + 1] += D;
+            ry[tp.j + 1] += B;
+            rz[tp.j + 1] += D;
         }
         __syncwarp();
+    };
+    // live steps two at a time (their taps computed together, their rows
+    // updated in step order: the sums of one step at a time), the next two
+    // fetched meanwhile
+    In c0 = {{0.f, 0.f, 0.f, 0.f}, 0.f}, c1 = c0, n0 = c0, n1 = c0;
+    long long b0 = next_live(i0);
+    long long b1 = b0 < i1 ? next_live(b0 + blockDim.x) : i1;
+    if (b0 < i1) fetch(b0 + threadIdx.x, c0);
+    if (b1 < i1) fetch(b1 + threadIdx.x, c1);
+    while (b0 < i1) {
+        const long long nb0 = b1 < i1 ? next_live(b1 + blockDim.x) : i1;
+        const long long nb1 = nb0 < i1 ? next_live(nb0 + blockDim.x) : i1;
+        if (nb0 < i1) fetch(nb0 + threadIdx.x, n0);
+        if (nb1 < i1) fetch(nb1 + threadIdx.x, n1);
+        const Tap t0 = tap_of(b0, c0);
+        const Tap t1 = tap_of(b1, c1);
+        scatter(t0);
+        scatter(t1);
+        b0 = nb0;
+        b1 = nb1;
+        c0 = n0;
+        c1 = n1;
     }
     __syncthreads();
     float *dst = g.partial + ((size_t)q * nch + c) * 2 * Lp;
