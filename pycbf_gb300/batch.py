@@ -31,7 +31,7 @@ import torch
 from . import _lib
 from .beamformers import BeamformerException, SyntheticBeamformer, TabbedBeamformer
 
-__all__ = ["BatchBeamformer", "BatchConfig", "beamformers_for"]
+__all__ = ["BatchBeamformer", "BatchConfig", "beamformers_for", "assign_branches"]
 
 
 @dataclass(frozen=True)
@@ -51,6 +51,18 @@ _TUNED: dict = {}
 
 def _ptr(t):
     return ct.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def assign_branches(costs: Sequence[float], nbranch: int) -> list:
+    """Branch of each group: largest cost first onto the least loaded branch
+    (ties to the lowest branch index)."""
+    load = [0.0] * nbranch
+    out = [0] * len(costs)
+    for g in sorted(range(len(costs)), key=lambda g: -costs[g]):
+        b = min(range(nbranch), key=lambda i: load[i])
+        load[b] += costs[g]
+        out[g] = b
+    return out
 
 
 def _stream():
@@ -159,19 +171,18 @@ class BatchBeamformer:
         groups: dict = {}
         for k, bf in enumerate(self.beamformers):
             groups.setdefault(id(bf), []).append(k)
-        cost = {g: sum(self.beamformers[k].ntx * self.beamformers[k].nrx * self.beamformers[k].nop
-                       for k in ks) for g, ks in groups.items()}
-        load = [0] * nbranch
+        members = list(groups.values())
+        costs = [sum(self.beamformers[k].ntx * self.beamformers[k].nrx * self.beamformers[k].nop
+                     for k in ks) for ks in members]
+        branch = assign_branches(costs, nbranch)
         cur = torch.cuda.current_stream()
         fork = torch.cuda.Event()
         fork.record(cur)
         for st in streams:
             st.wait_event(fork)
-        for g in sorted(groups, key=lambda g: -cost[g]):
-            b = min(range(nbranch), key=lambda i: load[i])
-            load[b] += cost[g]
-            with torch.cuda.stream(streams[b]):
-                for k in groups[g]:
+        for g in sorted(range(len(members)), key=lambda g: -costs[g]):
+            with torch.cuda.stream(streams[branch[g]]):
+                for k in members[g]:
                     self._launch_frame(k)
         for st in streams:
             join = torch.cuda.Event()

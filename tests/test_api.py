@@ -98,3 +98,16 @@ def test_morton_keeps_neighbours_close():
     blocks = pts.numpy()[order].reshape(-1, 32, 2)
     spans = blocks.max(1) - blocks.min(1)
     assert np.all(spans <= 8)       # 32 consecutive keys form an 8x4 or 4x8 block
+
+
+def test_batch_branch_assignment():
+    """Graph branches of the batch's frame-launch form: largest group first onto
+    the least loaded branch."""
+    from pycbf_gb300.batch import assign_branches
+    assert assign_branches([5, 3, 3, 2, 1], 2) == [0, 1, 1, 0, 1]  # loads 7, 7
+    assert assign_branches([1, 1, 1], 4) == [0, 1, 2]
+    costs = [9, 7, 6, 5, 4, 3, 2, 1]
+    b = assign_branches(costs, 3)
+    loads = [sum(c for c, x in zip(costs, b) if x == k) for k in range(3)]
+    assert max(loads) - min(loads) <= max(costs) and sum(loads) == sum(costs)
+    assert assign_branches([], 3) == []
