@@ -67,6 +67,24 @@ def rank_info():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def max_over_ranks(x: float, device) -> float:
+    """The largest x over the ranks of the process group (x itself when there
+    is no group or one rank): the slowest replica's time."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_rate(world: int, units_per_rank: float, seconds: float) -> float:
+    """Whole-job throughput of `world` replicas, each processing units_per_rank,
+    timed by the slowest one (weak scaling)."""
+    return world * units_per_rank / seconds
+
+
 def c1_workload(device):
     from pycbf_gb300 import phantom
     return phantom.linear_pw_tabbed(device=device)
@@ -256,12 +274,8 @@ def main_ours(a):
     clk = clocks.stop()
     spline_ms = [e[0].elapsed_time(e[1]) for e in evs]
     das_ms = [e[1].elapsed_time(e[2]) for e in evs]
-    total_ms = sum(s + d for s, d in zip(spline_ms, das_ms))
-    if world > 1:
-        tt = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
-    value = world * taps * a.steps / (total_ms * 1e-3)
+    total_ms = max_over_ranks(sum(s + d for s, d in zip(spline_ms, das_ms)), dev)
+    value = replicas_rate(world, taps * a.steps, total_ms * 1e-3)
 
     # end to end through the public API, pinned host input, numpy output
     rf_host = torch.from_numpy(w.rf).pin_memory()
@@ -273,12 +287,8 @@ def main_ours(a):
     t = time.perf_counter()
     for _ in range(a.steps):
         img = bf(rf_host)
-    e2e_s = time.perf_counter() - t
-    if world > 1:
-        tt = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e = {"value": world * taps * a.steps / e2e_s, "unit": UNIT,
+    e2e_s = max_over_ranks(time.perf_counter() - t, dev)
+    e2e = {"value": replicas_rate(world, taps * a.steps, e2e_s), "unit": UNIT,
            "h2d_bytes_per_step": int(rf_host.numel() * rf_host.element_size()),
            "d2h_bytes_per_step": int(img.size * img.itemsize),
            "ms_per_step": 1e3 * e2e_s / a.steps}
@@ -292,12 +302,8 @@ def main_ours(a):
         dist.barrier()
     t = time.perf_counter()
     imgs = list(bf.beamform_stream([rf_host] * a.steps))
-    es = time.perf_counter() - t
-    if world > 1:
-        tt = torch.tensor([es], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        es = float(tt.item())
-    e2e_stream = {"value": world * taps * a.steps / es, "unit": UNIT,
+    es = max_over_ranks(time.perf_counter() - t, dev)
+    e2e_stream = {"value": replicas_rate(world, taps * a.steps, es), "unit": UNIT,
                   "h2d_bytes_per_step": int(rf_host.numel() * rf_host.element_size()),
                   "d2h_bytes_per_step": int(imgs[-1].size * imgs[-1].itemsize),
                   "ms_per_step": 1e3 * es / a.steps,
