@@ -8,11 +8,15 @@ lag-1 short-lag spatial coherence of the per-element images plus an image
 sharpness term, so gradients reach c, the map and the channel data through
 the hand-written adjoint kernels.
 
-The coherence is the SLSC of examples/advanced_beamforming.ipynb (cell 2,
-calc_lagn_coherence) at lag 1, written with torch ops so that it is
-differentiable: per pixel, for each pair of adjacent elements that both
-accept the pixel, the normalised correlation of their axial kernels, averaged
-over the pairs.
+The coherence follows the lag-1 term of the SLSC of
+examples/advanced_beamforming.ipynb (cell 2, calc_lagn_coherence), written
+with torch ops so that it is differentiable: per pixel, for each pair of
+adjacent elements that both accept the pixel, the normalised correlation
+sum(a b) / sqrt(sum(a^2) sum(b^2)) of their axial kernels, averaged over the
+pairs.  Unlike the notebook (and TabbedSLSCBeamformer) it does not subtract
+the kernels' means and takes an element by its mask at the pixel itself, not
+over the whole kernel: a smooth objective for optimisation, not the display
+quantity.
 """
 from __future__ import annotations
 
