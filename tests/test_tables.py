@@ -69,3 +69,20 @@ def test_gpu_tables_at_benchmark_size_and_hann():
     b = TabbedBeamformer(tautx=w.tautx, taurx=w.taurx, apodtx=w.apodtx, apodrx=w.apodrx,
                          **args)(w.rf)
     assert np.max(np.abs(a - b)) <= 1e-5 * np.max(np.abs(b))
+
+
+def test_host_helpers_match_reference_golden(golden):
+    """helpers.pw_tx_tables / rx_tables (the NumPy builders the phantoms and the
+    bench use) give the reference helper's plane-wave tables, rounded to
+    float32, bit for bit."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_tables_golden as mk
+
+    from pycbf_gb300 import helpers
+    g = golden("tables_2d.npz")
+    steers, ctx, cm, xele, xout, zout, fnum = mk.inputs()
+    tt, at = helpers.pw_tx_tables(steers, ctx, cm, xele, xout, zout)
+    tr, ar = helpers.rx_tables(cm, xele, xout, zout, fnum)
+    for name, v in (("tautx", tt), ("apodtx", at), ("taurx", tr), ("apodrx", ar)):
+        np.testing.assert_array_equal(v.astype(np.float32), g[f"pw_{name}"], err_msg=name)
