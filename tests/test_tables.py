@@ -86,3 +86,19 @@ def test_host_helpers_match_reference_golden(golden):
     tr, ar = helpers.rx_tables(cm, xele, xout, zout, fnum)
     for name, v in (("tautx", tt), ("apodtx", at), ("taurx", tr), ("apodrx", ar)):
         np.testing.assert_array_equal(v.astype(np.float32), g[f"pw_{name}"], err_msg=name)
+
+
+def test_synthetic_point_parameters_match_reference_golden(golden):
+    """helpers.pw_synthetic_points equals the reference's
+    calc_tx_synthetic_points_pw_2D + calc_rx_synthetic_points (golden made by
+    them, tests/golden/make_synth_points_golden.py) bit for bit."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_synth_points_golden as mk
+
+    from pycbf_gb300 import helpers
+    g = golden("synth_points.npz")
+    steers, ctx, cm, xele, fnum, rpw = mk.inputs()
+    p = helpers.pw_synthetic_points(steers, ctx, cm, xele, fnum, rpw)
+    for k in g:
+        np.testing.assert_array_equal(np.asarray(p[k], np.float64), g[k].astype(np.float64), err_msg=k)
