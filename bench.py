@@ -85,7 +85,7 @@ def replicas_rate(world: int, units_per_rank: float, seconds: float) -> float:
     return world * units_per_rank / seconds
 
 
-def c1_workload(device):
+def tabbed_workload(device):
     from pycbf_gb300 import phantom
     return phantom.linear_pw_tabbed(device=device)
 
@@ -130,7 +130,7 @@ def run_reference_arm(a):
     rank, world, _ = rank_info()
     if rank != 0:
         return
-    w = c1_workload("cpu")
+    w = tabbed_workload("cpu")
     from oracle import oracle
     threads = max(1, len(os.sched_getaffinity(0)))
     use_ref = oracle.ref_lib() is not None
@@ -225,7 +225,7 @@ def main_ours(a):
     dev = torch.device("cuda", local)
     L = _lib.load()
 
-    w = c1_workload(dev)
+    w = tabbed_workload(dev)
     taps = taps_of(w)
     bf = pg.TabbedBeamformer(tautx=w.tautx, taurx=w.taurx, apodtx=w.apodtx, apodrx=w.apodrx,
                              t0=w.t0, dt=w.dt, nt=w.nt, interp={"kind": "cubic"},
@@ -331,7 +331,7 @@ def main_ours(a):
     # DRAM bytes and warp instructions of one launch from the committed ncu summary
     # of this kernel and workload; the kernel is issue-bound, so the share of the
     # schedulers' issue slots it uses is reported beside the HBM fraction
-    prof = os.path.join(ROOT, "profiles", "das_tabbed_cubic_c1.md")
+    prof = os.path.join(ROOT, "profiles", "das_tabbed_cubic_11x128x2048.md")
     if os.path.exists(prof):
         with open(prof) as fp:
             text = fp.read()
@@ -367,7 +367,7 @@ def main_ours(a):
     variants = {}
     if not a.no_variants:
         variants = run_variants(a, w, dev, taps)
-        for k in ("demod_c1", "demod_512x1024"):
+        for k in ("demod_256x512", "demod_512x1024"):
             if k in variants:
                 variants[k]["iq_fp32_frac"] = variants[k]["iq_tflops"] / fp32_peak
 
@@ -493,7 +493,7 @@ def run_demod_variant(a, dev):
     from pycbf_gb300.demod import Demodulator
     res = {}
     stream = torch.cuda.current_stream()
-    for name, nx, nz in (("demod_c1", 256, 512), ("demod_512x1024", 512, 1024)):
+    for name, nx, nz in (("demod_256x512", 256, 512), ("demod_512x1024", 512, 1024)):
         dz = 40e-3 / (nz - 1)
         d = Demodulator(nz, 2 * 1e6 / 1540.0, 2 * 9e6 / 1540.0, 1 / dz)
         img = torch.as_tensor(np.random.default_rng(nz).standard_normal((nx, nz)).astype(np.float32),
@@ -565,9 +565,10 @@ def run_table_variant(a, dev):
     torch.cuda.synchronize()
     host_s = time.perf_counter() - t
     nbytes = 4 * (2 * 11 + 2 * 128) * 256 * 512
-    return {"tables_c1": {"gpu_ms": statistics.median(times), "host_numpy_and_copy_ms": 1e3 * host_s,
-                          "table_bytes": nbytes,
-                          "gpu_write_gbs": nbytes / (statistics.median(times) * 1e-3) / 1e9}}
+    return {"tables_11pw_128el_256x512": {
+        "gpu_ms": statistics.median(times), "host_numpy_and_copy_ms": 1e3 * host_s,
+        "table_bytes": nbytes,
+        "gpu_write_gbs": nbytes / (statistics.median(times) * 1e-3) / 1e9}}
 
 
 def _synthetic(cls, w, **kw):
@@ -579,11 +580,11 @@ def _synthetic(cls, w, **kw):
 def run_synthetic_variants(a, dev):
     """Synthetic-point workloads with delays computed on the fly.
 
-    c2_*: 192 elements at 0.2 mm, 75 plane waves over -18..18 deg (far
+    synthetic_*: 192 elements at 0.2 mm, 75 plane waves over -18..18 deg (far
     virtual sources), fs 31.25 MHz, Nt 4096, 40 000 speckle + 30 points,
     512 x 1024 pixels: DAS, DMAS (signed square root over all receive
     pairs, fused) and SLSC (lags 1..16, axial kernel 7 pixels = 1 wavelength).
-    c5_3d_fp16: 32 x 32 matrix, 25 diverging waves, Nt 2048, float16 channel
+    matrix_3d_fp16: 32 x 32 matrix, 25 diverging waves, Nt 2048, float16 channel
     data, 128 x 128 x 256 voxels, 8 frames per call (2 000 speckle + 50
     points: the content does not change the work)."""
     import numpy as np
@@ -600,10 +601,10 @@ def run_synthetic_variants(a, dev):
     cub = {"kind": "cubic"}
     nrx = w.geometry["ovecrx"].shape[0]
     cases = {
-        "c2_das": _synthetic(pg.SyntheticBeamformer, w, interp=cub, sumtype="tx_and_rx"),
-        "c2_dmas": _synthetic(pg.SyntheticDMASBeamformer, w, interp=cub,
+        "synthetic_das": _synthetic(pg.SyntheticBeamformer, w, interp=cub, sumtype="tx_and_rx"),
+        "synthetic_dmas": _synthetic(pg.SyntheticDMASBeamformer, w, interp=cub,
                               lags=np.arange(1, nrx), lagaxis="rx", sumlags=True, dmastype="ssr"),
-        "c2_slsc": _synthetic(pg.SyntheticSLSCBeamformer, w, interp=cub, grid_shape=(nx, nz),
+        "synthetic_slsc": _synthetic(pg.SyntheticSLSCBeamformer, w, interp=cub, grid_shape=(nx, nz),
                               nlag=16, nkern=3),
     }
     for name, bf in cases.items():
@@ -624,7 +625,7 @@ def run_synthetic_variants(a, dev):
     call()
     t = _event_time(call, 2, flush, stream)
     taps = 8 * bf.ntx * bf.nrx * bf.nop
-    res["c5_3d_fp16"] = {"value": taps / t, "unit": UNIT, "ms_per_call": 1e3 * t,
+    res["matrix_3d_fp16"] = {"value": taps / t, "unit": UNIT, "ms_per_call": 1e3 * t,
                          "frames_per_call": 8, "taps": taps, "storage": "float16",
                          "workload": "synthetic 3-D 32x32 matrix 25dw 2048s 128x128x256"}
     return res

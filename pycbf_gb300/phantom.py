@@ -6,14 +6,14 @@ bandwidth at -6 dB) at the two-way delays of point scatterers, plus white
 noise at a fixed level below the signal RMS.  Each echo is evaluated only on
 the samples where its envelope exceeds 1e-9, with torch on the given device.
 
-Workloads (sizes as named by the benchmark configurations):
+Workloads (the defaults of the builders below):
 
-* ``tabbed_c1``: 128-element linear array, 0.3 mm pitch, 11 plane waves over
+* ``linear_pw_tabbed``: 128-element linear array, 0.3 mm pitch, 11 plane waves over
   -10..+10 deg, fs 25 MHz, 5 MHz pulse at 60 % bandwidth, Nt 2048, c 1540 m/s,
   20 bright points + 5000 N(0,1) speckle in x in [-19, 19] mm, z in [5, 45] mm,
   -40 dB noise; grid 256 x 512; tautx/taurx from the plane-wave geometry,
   apodtx all ones, apodrx a Hann window inside an F#1.5 mask.
-* ``synthetic_c2``: 192 elements, 0.2 mm pitch, 75 plane waves over -18..+18
+* ``linear_pw_synthetic``: 192 elements, 0.2 mm pitch, 75 plane waves over -18..+18
   deg, fs 31.25 MHz, f0 6.25 MHz, Nt 4096, 40 000 speckle + 30 points, grid
   512 x 1024 over x in [-19.2, 19.2] mm, z in [5, 45] mm, synthetic-point
   geometry (virtual sources 10 m behind the array), F#1.5 receive.

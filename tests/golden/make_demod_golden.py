@@ -67,7 +67,7 @@ def cases():
     dz = 40e-3 / 511
     out = []
     # the examples' DAS band (1-9 MHz) on 512-sample lines
-    out.append(dict(name="c1", x=rf_image(rng, 24, 512, dz, 5e6), kmin=2 * 1e6 / c0,
+    out.append(dict(name="das_band", x=rf_image(rng, 24, 512, dz, 5e6), kmin=2 * 1e6 / c0,
                     kmax=2 * 9e6 / c0, ks=1 / dz, alpha=0.25, axis=-1, shiftit=True))
     # the DMAS band (5-12 MHz) on a finer grid, no shift
     dzf = 10e-3 / 511
@@ -102,11 +102,11 @@ def main(ref):
                                        float(c["shiftit"])])
         out[f"{p}_iq"] = np.asarray(iq, np.complex128)
     zout = 5e-3 + np.arange(512) * dz
-    out["c1_zout"] = zout
-    out["c1_zout_demod"] = zdemod(zout, 2 * 1e6 / 1540.0, 2 * 9e6 / 1540.0)
-    ns = {"np": np, "env": np.abs(out["c1_iq"])}
+    out["das_band_zout"] = zout
+    out["das_band_zout_demod"] = zdemod(zout, 2 * 1e6 / 1540.0, 2 * 9e6 / 1540.0)
+    ns = {"np": np, "env": np.abs(out["das_band_iq"])}
     exec(logline, ns)
-    out["c1_logged"] = ns["logged"]
+    out["das_band_logged"] = ns["logged"]
     np.savez_compressed(os.path.join(HERE, "demod.npz"), **out)
     print("wrote demod.npz:", {k: v.shape for k, v in out.items()})
 

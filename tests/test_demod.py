@@ -16,7 +16,7 @@ from oracle import demod_ref
 from pycbf_gb300 import _lib
 from pycbf_gb300 import demod as dm
 
-CASES = ("c1", "noshift", "nyq", "axis0", "frames")
+CASES = ("das_band", "noshift", "nyq", "axis0", "frames")
 
 
 def _params(g, p):
@@ -38,12 +38,12 @@ def test_oracle_matches_reference_golden(g, case):
 
 
 def test_oracle_zout_and_display_line(g):
-    z = demod_ref.zout_fft_tukey_demod(g["c1_zout"], 2 * 1e6 / 1540.0, 2 * 9e6 / 1540.0)
-    assert np.array_equal(z, g["c1_zout_demod"])
-    assert np.array_equal(dm.zout_fft_tukey_demod(g["c1_zout"], 2 * 1e6 / 1540.0,
-                                                  2 * 9e6 / 1540.0), g["c1_zout_demod"])
-    logged = demod_ref.log_compress(np.abs(g["c1_iq"]))
-    assert np.abs(logged - g["c1_logged"]).max() <= 1e-9
+    z = demod_ref.zout_fft_tukey_demod(g["das_band_zout"], 2 * 1e6 / 1540.0, 2 * 9e6 / 1540.0)
+    assert np.array_equal(z, g["das_band_zout_demod"])
+    assert np.array_equal(dm.zout_fft_tukey_demod(g["das_band_zout"], 2 * 1e6 / 1540.0,
+                                                  2 * 9e6 / 1540.0), g["das_band_zout_demod"])
+    logged = demod_ref.log_compress(np.abs(g["das_band_iq"]))
+    assert np.abs(logged - g["das_band_logged"]).max() <= 1e-9
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -143,10 +143,10 @@ def test_gpu_percentile_nan_and_signed_zero():
 
 @pytest.mark.gpu
 def test_gpu_bmode_matches_display_line(g):
-    p = _params(g, "c1")
-    d = dm.Demodulator(g["c1_x"].shape[-1], p["kmin"], p["kmax"], p["ks"], p["alpha"], p["shiftit"])
-    db = d.bmode(g["c1_x"]).cpu().numpy()
-    ref = g["c1_logged"]
+    p = _params(g, "das_band")
+    d = dm.Demodulator(g["das_band_x"].shape[-1], p["kmin"], p["kmax"], p["ks"], p["alpha"], p["shiftit"])
+    db = d.bmode(g["das_band_x"]).cpu().numpy()
+    ref = g["das_band_logged"]
     shown = ref > -60.0                        # the displayed range (examples: -45..5 dB)
     assert np.abs(db - ref)[shown].max() <= 2e-3
     # frames: one percentile per image

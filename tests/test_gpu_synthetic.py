@@ -20,7 +20,7 @@ GEO_KEYS = ("ovectx", "nvectx", "doftx", "alatx", "t0tx", "ovecrx", "nvecrx", "a
 
 
 @pytest.fixture(scope="module")
-def c2_small():
+def synthetic_small():
     w = phantom.linear_pw_synthetic(nele=48, nsteer=9, nt=1536, nx=48, nz=96, n_speckle=2000,
                                     xlim=(-4.8e-3, 4.8e-3), zlim=(5e-3, 20e-3), device="cuda")
     return w
@@ -44,13 +44,13 @@ def oracle_image(w, tables, kind="cubic", sumtype="tx_and_rx", rf=None):
 
 
 @pytest.mark.parametrize("kind", ["cubic", "nearest", "linear"])
-def test_synthetic_das_vs_oracle(c2_small, kind):
-    w = c2_small
+def test_synthetic_das_vs_oracle(synthetic_small, kind):
+    w = synthetic_small
     tables = oracle_tables(w)
     bf = synth_bf(w, interp={"kind": kind})
     out = bf(w.rf)
     r, m = assert_image_close(out, oracle_image(w, tables, kind), what=kind)
-    report(f"synthetic_c2small_{kind}", rel_l2=r, max_abs_peak=m)
+    report(f"synthetic_small_{kind}", rel_l2=r, max_abs_peak=m)
     cnt, isum = bf.tap_census()
     ok_cnt, ok_isum = oracle.tap_census(*tables, w.t0, w.dt, w.nt,
                                         interp="nearest" if kind == "nearest" else "cubic",
@@ -59,8 +59,8 @@ def test_synthetic_das_vs_oracle(c2_small, kind):
     np.testing.assert_array_equal(isum.cpu().numpy(), ok_isum)
 
 
-def test_synthetic_nearest_upsampled_vs_oracle(c2_small):
-    w = c2_small
+def test_synthetic_nearest_upsampled_vs_oracle(synthetic_small):
+    w = synthetic_small
     tables = oracle_tables(w)
     bf = synth_bf(w, interp={"kind": "nearest", "usf": 3})
     out = bf(w.rf)
@@ -68,7 +68,7 @@ def test_synthetic_nearest_upsampled_vs_oracle(c2_small):
     ref = oracle.das_tabbed(w.rf, tt, at, tr, ar, w.t0, w.dt, w.nt, interp="nearest", usf=3,
                             thresh=0.01, threads=NCPU)
     r, m = assert_image_close(out, ref, what="usf 3")
-    report("synthetic_c2small_nearest_usf3", rel_l2=r, max_abs_peak=m)
+    report("synthetic_small_nearest_usf3", rel_l2=r, max_abs_peak=m)
     cnt, isum = bf.tap_census()
     ok_cnt, ok_isum = oracle.tap_census(*tables, w.t0, w.dt, w.nt, interp="nearest", usf=3,
                                         thresh=0.01)
@@ -77,25 +77,25 @@ def test_synthetic_nearest_upsampled_vs_oracle(c2_small):
 
 
 @pytest.mark.parametrize("interp", [dict(kind="korder_cubic", k=8), dict(kind="makima")])
-def test_synthetic_gpu_only_interpolators_vs_oracle(c2_small, interp):
-    w = c2_small
+def test_synthetic_gpu_only_interpolators_vs_oracle(synthetic_small, interp):
+    w = synthetic_small
     tt, at, tr, ar = oracle_tables(w)
     out = synth_bf(w, interp=interp)(w.rf)
     ref = oracle.das_poly(w.rf, tt, at, tr, ar, w.t0, w.dt, w.nt, interp["kind"],
                           k=interp.get("k", 8), thresh=0.01)
     r, m = assert_image_close(out, ref, what=str(interp))
-    report(f"synthetic_c2small_{interp['kind']}", rel_l2=r, max_abs_peak=m)
+    report(f"synthetic_small_{interp['kind']}", rel_l2=r, max_abs_peak=m)
 
 
 @pytest.mark.parametrize("sumtype", ["tx_only", "rx_only", "none"])
-def test_synthetic_sumtypes(c2_small, sumtype):
-    w = c2_small
+def test_synthetic_sumtypes(synthetic_small, sumtype):
+    w = synthetic_small
     out = synth_bf(w, sumtype=sumtype)(w.rf)
     assert_image_close(out, oracle_image(w, oracle_tables(w), "cubic", sumtype), what=sumtype)
 
 
-def test_synthetic_receive_mask(c2_small):
-    w = c2_small
+def test_synthetic_receive_mask(synthetic_small):
+    w = synthetic_small
     _, _, _, ar = oracle_tables(w)
     m = synth_bf(w).rx_mask().cpu().numpy()
     np.testing.assert_array_equal(m, (ar != 0).astype(np.uint8))
@@ -151,8 +151,8 @@ def test_synthetic_delay_branches(ndim, dof, behind):
 
 
 @pytest.mark.parametrize("dmastype", ["ssr", "power"])
-def test_fused_dmas_all_pairs(c2_small, dmastype):
-    w = c2_small
+def test_fused_dmas_all_pairs(synthetic_small, dmastype):
+    w = synthetic_small
     nrx = w.geometry["ovecrx"].shape[0]
     bf = synth_bf(w, cls=pg.SyntheticDMASBeamformer, lags=np.arange(1, nrx), dmastype=dmastype)
     assert bf._fused
@@ -160,11 +160,11 @@ def test_fused_dmas_all_pairs(c2_small, dmastype):
     sep = oracle_image(w, oracle_tables(w), "cubic", "tx_only").reshape(nrx, -1)
     ref = oracle.dmas(sep, np.arange(1, nrx), power=(dmastype == "power"))
     r, m = assert_image_close(out, ref, rel=1e-4, peak=1e-4, what=dmastype)
-    report(f"synthetic_c2small_dmas_{dmastype}", rel_l2=r, max_abs_peak=m)
+    report(f"synthetic_small_dmas_{dmastype}", rel_l2=r, max_abs_peak=m)
 
 
-def test_dmas_lag_list_unfused(c2_small):
-    w = c2_small
+def test_dmas_lag_list_unfused(synthetic_small):
+    w = synthetic_small
     nrx = w.geometry["ovecrx"].shape[0]
     lags = np.array([1, 2, 5])
     bf = synth_bf(w, cls=pg.SyntheticDMASBeamformer, lags=lags, sumlags=False)
@@ -176,8 +176,8 @@ def test_dmas_lag_list_unfused(c2_small):
     assert_image_close(out, ref, rel=1e-4, peak=1e-4, what="lag list")
 
 
-def test_slsc_vs_oracle(c2_small):
-    w = c2_small
+def test_slsc_vs_oracle(synthetic_small):
+    w = synthetic_small
     nx, nz = w.grid
     tables = oracle_tables(w)
     nrx = tables[2].shape[0]
@@ -188,7 +188,7 @@ def test_slsc_vs_oracle(c2_small):
     assert np.array_equal(np.isnan(out), np.isnan(ref))
     ok = ~np.isnan(ref)
     err = np.max(np.abs(out[ok] - ref[ok]))
-    report("synthetic_c2small_slsc", max_abs=err)
+    report("synthetic_small_slsc", max_abs=err)
     assert err < 2e-4
 
 

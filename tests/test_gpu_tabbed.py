@@ -32,20 +32,20 @@ def oracle_for(case, kind="cubic", sumtype="tx_and_rx", threads=1):
 
 
 @pytest.fixture(scope="module")
-def c1_small():
+def tabbed_small():
     w = phantom.linear_pw_tabbed(nx=64, nz=128, n_speckle=1500, device="cuda")
     return dict(rf=w.rf, tautx=w.tautx, apodtx=w.apodtx, taurx=w.taurx, apodrx=w.apodrx,
                 t0=w.t0, dt=w.dt, nt=w.nt)
 
 
-def test_block_items_deterministic_and_frame_consistent(c1_small):
+def test_block_items_deterministic_and_frame_consistent(tabbed_small):
     """Single-frame staged launches split tiles into receive-block items whose
     sums the last block adds in order: repeated calls give the same bits, and
     so does the frame-per-tile path of a multi-frame call."""
-    bf = bf_for(c1_small, "cubic")
-    a, b = bf(c1_small["rf"]), bf(c1_small["rf"])
+    bf = bf_for(tabbed_small, "cubic")
+    a, b = bf(tabbed_small["rf"]), bf(tabbed_small["rf"])
     np.testing.assert_array_equal(a, b)
-    frames = np.stack([c1_small["rf"], c1_small["rf"][::-1].copy()])
+    frames = np.stack([tabbed_small["rf"], tabbed_small["rf"][::-1].copy()])
     np.testing.assert_array_equal(bf(frames)[0], a)
     assert bf.kernel_status() == 0
 
@@ -135,16 +135,16 @@ def test_tap_census_near_boundaries():
 
 
 @pytest.mark.parametrize("sumtype", ["tx_and_rx", "tx_only", "rx_only", "none"])
-def test_c1_geometry_small_grid(c1_small, sumtype):
-    case = c1_small
+def test_plane_wave_geometry_small_grid(tabbed_small, sumtype):
+    case = tabbed_small
     out = bf_for(case, "cubic", sumtype)(case["rf"])
     ref = oracle_for(case, "cubic", sumtype, threads=NCPU)
     r, m = assert_image_close(out, ref, what=sumtype)
-    report(f"tabbed_c1_64x128_cubic_{sumtype}", rel_l2=r, max_abs_peak=m)
+    report(f"tabbed_64x128_cubic_{sumtype}", rel_l2=r, max_abs_peak=m)
 
 
-def test_c1_small_fp64_error_and_census(c1_small):
-    case = c1_small
+def test_small_grid_fp64_error_and_census(tabbed_small):
+    case = tabbed_small
     out = bf_for(case, "cubic")(case["rf"])
     ref64 = oracle.das_tabbed_fp64(case["rf"], case["tautx"], case["apodtx"], case["taurx"],
                                    case["apodrx"], case["t0"], case["dt"], case["nt"])
@@ -155,7 +155,7 @@ def test_c1_small_fp64_error_and_census(c1_small):
     ref32 = oracle_for(case, "cubic", threads=NCPU)
     r32 = oracle.rel_l2(ref32, ref64)
     assert r64 <= 1e-3 and r64 <= 1.25 * r32, (r64, r32)
-    report("tabbed_c1_64x128_cubic_vs_fp64", rel_l2=r64,
+    report("tabbed_64x128_cubic_vs_fp64", rel_l2=r64,
            max_abs_peak=oracle.max_abs_rel_peak(out, ref64), oracle_f32_rel_l2_vs_fp64=r32)
     cnt, isum = bf_for(case, "cubic").tap_census()
     ok_cnt, ok_isum = oracle.tap_census(case["tautx"], case["apodtx"], case["taurx"], case["apodrx"],
@@ -165,60 +165,60 @@ def test_c1_small_fp64_error_and_census(c1_small):
 
 
 @pytest.mark.parametrize("kind", ["nearest", "linear"])
-def test_other_kinds_vs_oracle(c1_small, kind):
-    out = bf_for(c1_small, kind)(c1_small["rf"])
-    ref = oracle_for(c1_small, kind, threads=NCPU)
+def test_other_kinds_vs_oracle(tabbed_small, kind):
+    out = bf_for(tabbed_small, kind)(tabbed_small["rf"])
+    ref = oracle_for(tabbed_small, kind, threads=NCPU)
     assert_image_close(out, ref, what=kind)
 
 
-def test_linear_reference_floor_vs_oracle(c1_small):
-    out = bf_for(c1_small, dict(kind="linear", reference_floor=True))(c1_small["rf"])
-    ref = oracle_for(c1_small, "linear_floor", threads=NCPU)
+def test_linear_reference_floor_vs_oracle(tabbed_small):
+    out = bf_for(tabbed_small, dict(kind="linear", reference_floor=True))(tabbed_small["rf"])
+    ref = oracle_for(tabbed_small, "linear_floor", threads=NCPU)
     assert_image_close(out, ref, rel=1e-6, peak=1e-6, what="linear_floor")
 
 
-def test_pixel_order_does_not_change_results(c1_small):
-    a = bf_for(c1_small, "cubic", pixel_order="auto")(c1_small["rf"])
-    b = bf_for(c1_small, "cubic", pixel_order="natural")(c1_small["rf"])
+def test_pixel_order_does_not_change_results(tabbed_small):
+    a = bf_for(tabbed_small, "cubic", pixel_order="auto")(tabbed_small["rf"])
+    b = bf_for(tabbed_small, "cubic", pixel_order="natural")(tabbed_small["rf"])
     np.testing.assert_array_equal(a, b)
 
 
-def test_frames_batch_equals_single_frames(c1_small):
+def test_frames_batch_equals_single_frames(tabbed_small):
     rng = np.random.default_rng(1)
-    frames = np.stack([c1_small["rf"], rng.normal(size=c1_small["rf"].shape).astype(np.float32),
-                       -c1_small["rf"]])
+    frames = np.stack([tabbed_small["rf"], rng.normal(size=tabbed_small["rf"].shape).astype(np.float32),
+                       -tabbed_small["rf"]])
     for sumtype in ("tx_and_rx", "tx_only"):
-        bf = bf_for(c1_small, "cubic", sumtype)
+        bf = bf_for(tabbed_small, "cubic", sumtype)
         batch = bf(frames)
         for f in range(3):
             np.testing.assert_array_equal(batch[f], bf(frames[f]))
 
 
 @pytest.mark.parametrize("storage,tol", [("float16", 1e-3), ("bfloat16", 1e-2)])
-def test_reduced_precision_storage(c1_small, storage, tol):
-    case = c1_small
+def test_reduced_precision_storage(tabbed_small, storage, tol):
+    case = tabbed_small
     out = bf_for(case, "cubic", storage=storage)(case["rf"])
     ref64 = oracle.das_tabbed_fp64(case["rf"], case["tautx"], case["apodtx"], case["taurx"],
                                    case["apodrx"], case["t0"], case["dt"], case["nt"])
     r = oracle.rel_l2(out, ref64)
-    report(f"tabbed_c1_64x128_cubic_{storage}_vs_fp64", rel_l2=r)
+    report(f"tabbed_64x128_cubic_{storage}_vs_fp64", rel_l2=r)
     assert r < tol
 
 
-def test_torch_io_and_buffer(c1_small):
-    bf = bf_for(c1_small, "cubic")
-    rf = torch.as_tensor(c1_small["rf"], device="cuda")
+def test_torch_io_and_buffer(tabbed_small):
+    bf = bf_for(tabbed_small, "cubic")
+    rf = torch.as_tensor(tabbed_small["rf"], device="cuda")
     buf = torch.empty(bf.nop, device="cuda")
     out = bf(rf, out_as_numpy=False, buffer=buf)
     assert out.data_ptr() == buf.data_ptr() and out.is_cuda
-    np.testing.assert_array_equal(out.cpu().numpy(), bf(c1_small["rf"]))
+    np.testing.assert_array_equal(out.cpu().numpy(), bf(tabbed_small["rf"]))
     with pytest.raises(pg.BeamformerException):
         bf(rf, buffer=torch.empty(3, device="cuda"))
     with pytest.raises(pg.BeamformerException):
         bf(rf[:, :5])
 
 
-def test_full_c1_vs_threaded_oracle():
+def test_full_workload_vs_threaded_oracle():
     """The full 11 x 128 x 2048, 256 x 512 workload against the oracle."""
     w = phantom.linear_pw_tabbed(device="cuda")
     case = dict(rf=w.rf, tautx=w.tautx, apodtx=w.apodtx, taurx=w.taurx, apodrx=w.apodrx,
@@ -226,8 +226,8 @@ def test_full_c1_vs_threaded_oracle():
     bf = bf_for(case, "cubic")
     out = bf(case["rf"])
     ref = oracle_for(case, "cubic", threads=NCPU)
-    r, m = assert_image_close(out, ref, what="full c1")
-    report("tabbed_c1_full_cubic_vs_oracle", rel_l2=r, max_abs_peak=m)
+    r, m = assert_image_close(out, ref, what="full workload")
+    report("tabbed_11x128x2048_cubic_vs_oracle", rel_l2=r, max_abs_peak=m)
     cnt, isum = bf.tap_census()
     ok_cnt, ok_isum = oracle.tap_census(case["tautx"], case["apodtx"], case["taurx"], case["apodrx"],
                                         case["t0"], case["dt"], case["nt"])
@@ -258,22 +258,22 @@ def test_interp_known_answer_gpu():
 
 @pytest.mark.parametrize("kind", ["cubic", "nearest", "linear"])
 @pytest.mark.parametrize("sumtype", ["tx_and_rx", "tx_only"])
-def test_staged_kernel_matches_generic(c1_small, kind, sumtype):
+def test_staged_kernel_matches_generic(tabbed_small, kind, sumtype):
     """The TMA-staged kernel and the global-gather kernel give identical bits."""
-    staged = bf_for(c1_small, kind, sumtype)
-    plain = bf_for(c1_small, kind, sumtype, stage_channels=False)
+    staged = bf_for(tabbed_small, kind, sumtype)
+    plain = bf_for(tabbed_small, kind, sumtype, stage_channels=False)
     assert staged._plan is not None and plain._plan is None
-    a, b = staged(c1_small["rf"]), plain(c1_small["rf"])
+    a, b = staged(tabbed_small["rf"]), plain(tabbed_small["rf"])
     np.testing.assert_array_equal(a, b)
     assert staged.kernel_status() == 0
 
 
-def test_staged_frames_and_half_storage(c1_small):
+def test_staged_frames_and_half_storage(tabbed_small):
     rng = np.random.default_rng(2)
-    frames = np.stack([c1_small["rf"], rng.normal(size=c1_small["rf"].shape).astype(np.float32)])
+    frames = np.stack([tabbed_small["rf"], rng.normal(size=tabbed_small["rf"].shape).astype(np.float32)])
     for storage in ("float32", "float16"):
-        a = bf_for(c1_small, "cubic", storage=storage)(frames)
-        b = bf_for(c1_small, "cubic", storage=storage, stage_channels=False)(frames)
+        a = bf_for(tabbed_small, "cubic", storage=storage)(frames)
+        b = bf_for(tabbed_small, "cubic", storage=storage, stage_channels=False)(frames)
         np.testing.assert_array_equal(a, b)
 
 
@@ -315,10 +315,10 @@ def test_nearest_usf4_vs_reference_golden(golden, name):
 
 
 @pytest.mark.parametrize("usf", [2, 5])
-def test_nearest_upsampled_vs_oracle(c1_small, usf):
-    out = bf_for(c1_small, dict(kind="nearest", usf=usf))(c1_small["rf"])
-    ref = oracle.das_tabbed(c1_small["rf"], c1_small["tautx"], c1_small["apodtx"], c1_small["taurx"],
-                            c1_small["apodrx"], c1_small["t0"], c1_small["dt"], c1_small["nt"],
+def test_nearest_upsampled_vs_oracle(tabbed_small, usf):
+    out = bf_for(tabbed_small, dict(kind="nearest", usf=usf))(tabbed_small["rf"])
+    ref = oracle.das_tabbed(tabbed_small["rf"], tabbed_small["tautx"], tabbed_small["apodtx"], tabbed_small["taurx"],
+                            tabbed_small["apodrx"], tabbed_small["t0"], tabbed_small["dt"], tabbed_small["nt"],
                             interp="nearest", usf=usf, threads=NCPU)
     r, m = assert_image_close(out, ref, what=f"usf {usf}")
     report(f"tabbed_nearest_usf{usf}", rel_l2=r, max_abs_peak=m)
@@ -327,11 +327,11 @@ def test_nearest_upsampled_vs_oracle(c1_small, usf):
 @pytest.mark.parametrize("interp", [dict(kind="korder_cubic", k=8), dict(kind="korder_cubic", k=16),
                                     dict(kind="korder_cubic", k=8, zero_slopes=True),
                                     dict(kind="akima"), dict(kind="makima")])
-def test_gpu_only_interpolators_vs_oracle(c1_small, interp):
+def test_gpu_only_interpolators_vs_oracle(tabbed_small, interp):
     """korder / akima / makima (the reference's CUDA interpolators, restated in
     the oracle from __engines__.cu:58-355): tap set bit-exact, image within
     the float32 bar."""
-    c = c1_small
+    c = tabbed_small
     bf = bf_for(c, interp)
     out = bf(c["rf"])
     kind = interp["kind"]
@@ -361,13 +361,13 @@ def test_korder_large_k_and_edges(golden):
         assert_image_close(out, ref, what=f"{name} k={k}")
 
 
-def test_beamform_stream_equals_calls(c1_small):
+def test_beamform_stream_equals_calls(tabbed_small):
     """Frames streamed from host memory with overlapped copies give the images
     of one call per frame, bit for bit (float32 pinned and pageable, int16,
     4-D frames)."""
-    bf = bf_for(c1_small, "cubic")
+    bf = bf_for(tabbed_small, "cubic")
     rng = np.random.default_rng(7)
-    rf = c1_small["rf"]
+    rf = tabbed_small["rf"]
     frames = [rf, (rf * 0.5).astype(np.float32), torch.from_numpy(rf[::-1].copy()).pin_memory(),
               rng.normal(size=rf.shape).astype(np.float32)]
     got = list(bf.beamform_stream(frames))
@@ -380,9 +380,9 @@ def test_beamform_stream_equals_calls(c1_small):
     four = np.stack([rf, rf[::-1].copy()])
     (g,) = list(bf.beamform_stream([four]))
     np.testing.assert_array_equal(g, bf(four))
-    dm = pg.TabbedDMASBeamformer(tautx=c1_small["tautx"], taurx=c1_small["taurx"],
-                                 apodtx=c1_small["apodtx"], apodrx=c1_small["apodrx"],
-                                 t0=float(c1_small["t0"]), dt=float(c1_small["dt"]),
-                                 nt=int(c1_small["nt"]), lags=np.arange(1, 4))
+    dm = pg.TabbedDMASBeamformer(tautx=tabbed_small["tautx"], taurx=tabbed_small["taurx"],
+                                 apodtx=tabbed_small["apodtx"], apodrx=tabbed_small["apodrx"],
+                                 t0=float(tabbed_small["t0"]), dt=float(tabbed_small["dt"]),
+                                 nt=int(tabbed_small["nt"]), lags=np.arange(1, 4))
     with pytest.raises(pg.BeamformerException):
         list(dm.beamform_stream([rf]))

@@ -51,7 +51,7 @@ def _counts(rf, full=30000):
 
 
 @pytest.fixture(scope="module")
-def c1_small():
+def tabbed_small():
     from pycbf_gb300 import phantom
     w = phantom.linear_pw_tabbed(nx=48, nz=96, n_speckle=1000, device="cuda")
     return w
@@ -69,10 +69,10 @@ def _tabbed(w, **kw):
                                     {"kind": "nearest", "usf": 4},
                                     {"kind": "korder_cubic", "k": 8}, {"kind": "akima"}])
 @pytest.mark.parametrize("sumtype", ["tx_and_rx", "tx_only"])
-def test_tabbed_int16_equals_float_counts(c1_small, interp, sumtype):
+def test_tabbed_int16_equals_float_counts(tabbed_small, interp, sumtype):
     import torch
-    rfi = _counts(c1_small.rf)
-    bf = _tabbed(c1_small, interp=interp, sumtype=sumtype)
+    rfi = _counts(tabbed_small.rf)
+    bf = _tabbed(tabbed_small, interp=interp, sumtype=sumtype)
     a = bf(rfi, out_as_numpy=False)
     b = bf(rfi.astype(np.float32), out_as_numpy=False)
     assert torch.equal(a, b)
@@ -80,18 +80,18 @@ def test_tabbed_int16_equals_float_counts(c1_small, interp, sumtype):
 
 
 @pytest.mark.gpu
-def test_int16_frames_torch_and_storage(c1_small):
+def test_int16_frames_torch_and_storage(tabbed_small):
     import torch
-    rfi = _counts(c1_small.rf)
+    rfi = _counts(tabbed_small.rf)
     frames = np.stack([rfi, (rfi // 2).astype(np.int16), -rfi])
-    bf = _tabbed(c1_small, interp={"kind": "cubic"})
+    bf = _tabbed(tabbed_small, interp={"kind": "cubic"})
     want = bf(frames.astype(np.float32), out_as_numpy=False)
     assert torch.equal(bf(frames, out_as_numpy=False), want)
     pinned = torch.from_numpy(frames).pin_memory()
     assert torch.equal(bf(pinned, out_as_numpy=False), want)
     assert torch.equal(bf(pinned.cuda(), out_as_numpy=False), want)
     # float16 storage: the counts are converted to float32, then stored as float16
-    bfh = _tabbed(c1_small, interp={"kind": "cubic"}, storage="float16")
+    bfh = _tabbed(tabbed_small, interp={"kind": "cubic"}, storage="float16")
     assert torch.equal(bfh(rfi, out_as_numpy=False), bfh(rfi.astype(np.float32), out_as_numpy=False))
 
 
