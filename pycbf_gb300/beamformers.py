@@ -408,6 +408,15 @@ class _GPUBeamformer(Beamformer):
         return out
 
     def __call__(self, txrxt, out_as_numpy: bool = True, buffer=None):
+        """Beamform channel data (ntx, nrx, nt) or (nframes, ntx, nrx, nt).
+
+        The work is queued on the current CUDA stream.  With out_as_numpy=True
+        the call returns when the image is in host memory.  With False it
+        returns the CUDA tensor at once; a pinned host input may then still be
+        in flight and must not be overwritten before the stream reaches it.
+        The calls of one beamformer share its workspace and staging plan, so
+        they must not run on two streams at the same time.
+        """
         out = self._beamform(txrxt, buffer)
         return out.cpu().numpy() if out_as_numpy else out
 
