@@ -486,7 +486,7 @@ __device__ __forceinline__ void das_pixel(const DasArgs &a, long long i, int f, 
                     }
                     const int t = k0 + k;
                     if (!CENSUS && SUM == PYCBF_GB_SUM_NONE)
-                        a.out[((long long)(f * ntx + t) * nrx + r) * np + op] = c;
+                        a.out[(((long long)f * ntx + t) * nrx + r) * np + op] = c;
                     if (SUM == PYCBF_GB_SUM_RX_ONLY) {
                         if (in_regs) {
 #pragma unroll
