@@ -41,6 +41,17 @@ def test_korder_matrix_matches_the_oracle_restatement():
         np.testing.assert_array_equal(helpers.korder_matrix(k), oracle.korder_S(k))
 
 
+def test_korder_matrix_matches_reference_golden(golden):
+    """The reference's own __make_S_by_k__ (tests/golden/make_korder_golden.py),
+    rounded to float32 as its classes round it: equal bit for bit."""
+    from oracle import oracle
+    from pycbf_gb300 import helpers
+    g = golden("korder_S.npz")
+    for k in (4, 6, 8, 16, 32):
+        np.testing.assert_array_equal(helpers.korder_matrix(k), g[f"S{k}"])
+        np.testing.assert_array_equal(oracle.korder_S(k), g[f"S{k}"])
+
+
 def test_poly_kind_limits():
     with pytest.raises(pg.BeamformerException):
         pg.TabbedBeamformer(**tabs(), **T, interp={"kind": "korder_cubic", "k": 130})
