@@ -4,7 +4,7 @@ Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` import this module, and only as the checker (or as the timed CPU
 baseline).  The product package ``pycbf_gb300`` never imports it.
 
-Three layers:
+Four layers:
 
 * ``liboracle.so`` built from ``oracle/pycbf_oracle.c`` -- a float32
   restatement of the reference's C path (pycbf/cpu/pycbf.c) and of the
@@ -12,6 +12,12 @@ Three layers:
 * ``oracle/_ref/libpycbf_ref.so`` -- the reference's own ``pycbf.c`` compiled
   from its sources by ``oracle/Makefile`` (only where the reference checkout
   exists).  Used to pin the restatement and, when present, as the CPU baseline.
+* ``oracle/_ref/libpycbf_refgpu.so`` -- the reference's CUDA delay-and-sum
+  kernels (pycbf/gpu/__engines__.cu) compiled for the CPU where they lie,
+  with oracle/refgpu_shim.h for the CUDA built-ins and oracle/refgpu_driver.cpp
+  emulating their launches (only where the reference checkout exists).  Pins
+  the restatement of the interpolators and the synthetic geometry that the
+  reference has only on the GPU.
 * float64 NumPy/SciPy restatements (``*_fp64``) -- the accuracy yardstick.
 
 Pinning: tests/test_oracle.py checks the restatement against the golden
@@ -31,7 +37,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
 _REF = None
+_REFGPU: dict = {}
 _LOCK = threading.Lock()
+_POLY_LOCK = threading.Lock()  # guards the C library's fusion switch
 
 INTERP_CODES = {"cubic": 0, "nearest": 1, "linear": 2, "linear_floor": 3}
 SUMTYPE_CODES = {"none": 0, "tx_only": 1, "rx_only": 2, "tx_and_rx": 3}
@@ -88,6 +96,8 @@ def lib() -> ct.CDLL:
             L.orc_poly_index.restype = _i
             L.orc_das_poly.argtypes = [_i, _i, _p, _f, _f, _i, _p, _i, _i, _ll, _f, _p, _p, _p, _p,
                                        _i, _p]
+            L.orc_set_poly_fusion.argtypes = [_i]
+            L.orc_set_poly_fusion.restype = None
             _LIB = L
         return _LIB
 
@@ -111,6 +121,102 @@ def ref_lib() -> ct.CDLL | None:
             R.beamform_nearest.restype = None
             _REF = R
         return _REF
+
+
+def build_refgpu(ref_root: str = "/root/reference") -> str | None:
+    """Compile the reference's CUDA kernels for the CPU into oracle/_ref when its
+    checkout exists (oracle/refgpu_driver.cpp)."""
+    src = os.path.join(ref_root, "pycbf", "gpu", "__engines__.cu")
+    if not os.path.exists(src):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "refgpu", f"REF={ref_root}"], check=True)
+    return os.path.join(HERE, "_ref", "libpycbf_refgpu.so")
+
+
+def refgpu_lib(contracted: bool = False) -> ct.CDLL | None:
+    """The reference's CUDA delay-and-sum kernels compiled for the CPU, or None
+    where they were not built.  contracted=True: the build with multiply-adds
+    fused, as NVRTC's default does (make -C oracle refgpu-fused)."""
+    name = "libpycbf_refgpu_fused.so" if contracted else "libpycbf_refgpu.so"
+    with _LOCK:
+        if name not in _REFGPU:
+            path = os.path.join(HERE, "_ref", name)
+            if not os.path.exists(path):
+                return None
+            try:
+                R = ct.CDLL(path)
+            except OSError:  # e.g. a binary built for another machine
+                return None
+            R.rgd_tabbed.argtypes = [_i, _i, _p, _f, _f, _i, _p, _ll, _ll, _ll, _ll, _p, _p, _p,
+                                     _p, _i, _p]
+            R.rgd_tabbed.restype = _i
+            R.rgd_synthetic.argtypes = [_i, _i, _p, _f, _f, _i, _i, _p, _ll, _ll, _ll, _ll, _p, _p,
+                                        _p, _p, _p, _p, _p, _p, _f, _p, _i, _p]
+            R.rgd_synthetic.restype = _i
+            _REFGPU[name] = R
+        return _REFGPU[name]
+
+
+# the reference's interp flags (its jumpTable order) and -1 for its korder kernel
+REFGPU_INTERP = {"nearest": 0, "linear": 1, "akima": 2, "makima": 3, "korder_cubic": -1}
+
+
+def _refgpu_S(interp, k):
+    if interp == "korder_cubic" and k > 0:
+        return korder_S(k)
+    return np.zeros((1, 1), np.float32)
+
+
+def das_tabbed_refgpu(rf, tautx, apodtx, taurx, apodrx, t0, dt, nt, interp, k=4,
+                      sumtype="tx_and_rx", contracted=False):
+    """Tabbed image from the reference's own CUDA kernel
+    (das_bmode_tabbed_multi_interp / _korder_cubic, pycbf/gpu/__engines__.cu:
+    726-864) run on the CPU.  Its tap rule is |apodtx*apodrx| > 0.01."""
+    R = refgpu_lib(contracted)
+    if R is None:
+        raise RuntimeError("the reference's kernels are not built (make -C oracle refgpu)")
+    rf = _c32(rf)
+    tautx, apodtx, taurx, apodrx = map(_c32, (tautx, apodtx, taurx, apodrx))
+    nfr = rf.shape[0] if rf.ndim == 4 else 1
+    ntx, nrx, np_ = tautx.shape[0], taurx.shape[0], tautx.shape[1]
+    S = _refgpu_S(interp, k)
+    out = np.zeros(nfr * out_size(sumtype, ntx, nrx, np_), dtype=np.float32)
+    st = R.rgd_tabbed(REFGPU_INTERP[interp], int(k), _ptr(S), float(t0), float(dt), int(nt),
+                      _ptr(rf), ntx, nrx, np_, nfr, _ptr(tautx), _ptr(apodtx), _ptr(taurx),
+                      _ptr(apodrx), SUMTYPE_CODES[sumtype], _ptr(out))
+    if st:
+        raise ValueError("rgd_tabbed rejected its arguments")
+    return out
+
+
+def das_synthetic_refgpu(rf, geometry, t0, dt, nt, interp, k=4, sumtype="tx_and_rx",
+                         contracted=False):
+    """Synthetic-point image from the reference's own CUDA kernel
+    (das_bmode_synthetic_multi_interp / _korder_cubic, pycbf/gpu/__engines__.cu:
+    506-725, delays and masks of calc_tautx_apodtx / calc_taurx_apodrx :377-470)
+    run on the CPU.  geometry: the constructor arrays (ovectx, nvectx, doftx,
+    alatx, t0tx, ovecrx, nvecrx, alarx, c0, pnts).  korder receives k as the
+    reference's launch passes it: an int32 in a float parameter."""
+    R = refgpu_lib(contracted)
+    if R is None:
+        raise RuntimeError("the reference's kernels are not built (make -C oracle refgpu)")
+    g = {name: _c32(geometry[name]) for name in ("ovectx", "nvectx", "doftx", "alatx", "t0tx",
+                                                  "ovecrx", "nvecrx", "alarx", "pnts")}
+    rf = _c32(rf)
+    nfr = rf.shape[0] if rf.ndim == 4 else 1
+    ntx, nrx = g["ovectx"].shape[0], g["ovecrx"].shape[0]
+    np_, ndim = g["pnts"].shape
+    S = _refgpu_S(interp, k)
+    out = np.zeros(nfr * out_size(sumtype, ntx, nrx, np_), dtype=np.float32)
+    st = R.rgd_synthetic(REFGPU_INTERP[interp], int(k), _ptr(S), float(t0), float(dt), int(nt),
+                         int(ndim), _ptr(rf), ntx, nrx, np_, nfr, _ptr(g["ovectx"]),
+                         _ptr(g["nvectx"]), _ptr(g["t0tx"]), _ptr(g["alatx"]), _ptr(g["doftx"]),
+                         _ptr(g["ovecrx"]), _ptr(g["nvecrx"]), _ptr(g["alarx"]),
+                         float(np.float32(geometry["c0"])), _ptr(g["pnts"]),
+                         SUMTYPE_CODES[sumtype], _ptr(out))
+    if st:
+        raise ValueError("rgd_synthetic rejected its arguments")
+    return out
 
 
 def _c32(a) -> np.ndarray:
@@ -429,9 +535,11 @@ def korder_S(k):
 
 
 def das_poly(rf, tautx, apodtx, taurx, apodrx, t0, dt, nt, interp, k=8, S=None, thresh=1e-2,
-             sumtype="tx_and_rx"):
+             sumtype="tx_and_rx", fused=True):
     """Float32 Tabbed image with korder_cubic (k, S), akima or makima (restated
-    from pycbf/gpu/__engines__.cu:58-355)."""
+    from pycbf/gpu/__engines__.cu:58-355).  fused=False rounds the multiply-adds
+    that the device contracts in two steps, as a host build of the reference's
+    kernels does."""
     rf = _c32(rf)
     tautx, apodtx, taurx, apodrx = map(_c32, (tautx, apodtx, taurx, apodrx))
     ntx, nrx, np_ = tautx.shape[0], taurx.shape[0], tautx.shape[1]
@@ -441,7 +549,13 @@ def das_poly(rf, tautx, apodtx, taurx, apodrx, t0, dt, nt, interp, k=8, S=None, 
     else:  # akima / makima, or korder with k = 0 (zero derivative estimates)
         S, k = np.zeros((1, 1), np.float32), 0
     out = np.zeros(out_size(sumtype, ntx, nrx, np_), dtype=np.float32)
-    lib().orc_das_poly(code, int(k), _ptr(S), float(t0), float(dt), int(nt), _ptr(rf), ntx, nrx,
-                       np_, float(thresh), _ptr(tautx), _ptr(apodtx), _ptr(taurx), _ptr(apodrx),
-                       SUMTYPE_CODES[sumtype], _ptr(out))
+    L = lib()
+    with _POLY_LOCK:
+        L.orc_set_poly_fusion(int(bool(fused)))
+        try:
+            L.orc_das_poly(code, int(k), _ptr(S), float(t0), float(dt), int(nt), _ptr(rf), ntx,
+                           nrx, np_, float(thresh), _ptr(tautx), _ptr(apodtx), _ptr(taurx),
+                           _ptr(apodrx), SUMTYPE_CODES[sumtype], _ptr(out))
+        finally:
+            L.orc_set_poly_fusion(1)
     return out

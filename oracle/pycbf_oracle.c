@@ -247,17 +247,30 @@ ORC_EXPORT void orc_das_tabbed(int interp, int usf, float t0, float dt, int nt,
 /* The interpolators the reference has only in its CUDA file: korder cubic  */
 /* (__engines__.cu:292-355, S from gpu/__core_bf_classes__.py:366-395),     */
 /* akima (:188-269) and makima (:58-183).  The reference compiles them with */
-/* NVRTC, whose default contracts x0 + dx*n and x - x0 - dx*n into one     */
-/* fused multiply-add each; they are written as fmaf here, every other      */
-/* operation as in the source, one rounding each.  Out-of-range values are  */
+/* NVRTC, whose default contracts x0 + dx*n, x - x0 - dx*n and the korder  */
+/* derivative sums into fused multiply-adds; those are fused here          */
+/* (orc_madd), every other operation as in the source, one rounding each.   */
+/* Out-of-range values are                                                  */
 /* the fill 0.  Two reads past the channel in the reference are given       */
 /* defined values: an akima/makima index at or past nx-1 (x a hair below    */
 /* the last knot with the quotient rounded up) returns y[nx-1].             */
+/* orc_set_poly_fusion(0) rounds those multiply-adds in two steps instead,  */
+/* as a host build of the reference's kernels does (tests only).            */
 /* ------------------------------------------------------------------------ */
+static int orc_poly_fused = 1;
+
+ORC_EXPORT void orc_set_poly_fusion(int on) { orc_poly_fused = on != 0; }
+
+/* a * b + c: one rounding (the device contraction) or two */
+static inline float orc_madd(float a, float b, float c)
+{
+    return orc_poly_fused ? fmaf(a, b, c) : a * b + c;
+}
+
 ORC_EXPORT int orc_poly_index(int kind, float x, float x0, float dx, int nx)
 {
     /* knot index of a tap, or -1 when the fill applies */
-    float xn = fmaf(dx, (float)(nx - 1), x0);
+    float xn = orc_madd(dx, (float)(nx - 1), x0);
     if (kind == 4) {
         int ixin = (int)((x - x0) / dx);
         if ((x < x0) || (ixin > nx - 1) || (x > xn)) return -1;
@@ -288,10 +301,10 @@ static float orc_korder_point(float x, const float *y, int nx, float x0, float d
     }
     float y0 = y[ixin], y1 = y[ixin + 1], yp0 = 0.0f, yp1 = 0.0f;
     for (int i = 0; i < k; ++i) {
-        yp0 = fmaf(S[ik0 * k + i], y[iy0 + i], yp0);
-        yp1 = fmaf(S[ik0 * k + k + i], y[iy0 + i], yp1);
+        yp0 = orc_madd(S[ik0 * k + i], y[iy0 + i], yp0);
+        yp1 = orc_madd(S[ik0 * k + k + i], y[iy0 + i], yp1);
     }
-    float xnorm = fmaf(-dx, (float)ixin, x - x0) / dx;
+    float xnorm = orc_madd(-dx, (float)ixin, x - x0) / dx;
     float a0 = y0, a1 = yp0;
     float a2 = 3.0f * (y1 - y0) - 2.0f * yp0 - yp1;
     float a3 = 2.0f * (y0 - y1) + yp0 + yp1;
@@ -374,7 +387,7 @@ static float orc_akima_point(float x, const float *y, int nx, float x0, float dx
     float b = sp0;
     float c = (3 * mp0 - 2 * sp0 - sp1) / dx;
     float d = (sp0 + sp1 - 2 * mp0) / (dx * dx);
-    float delta = x - fmaf(dx, (float)ixo, x0);
+    float delta = x - orc_madd(dx, (float)ixo, x0);
     return a + b * delta + c * delta * delta + d * delta * delta * delta;
 }
 

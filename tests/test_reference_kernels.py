@@ -1,0 +1,99 @@
+"""The oracle against the reference's own CUDA kernels (pycbf/gpu/__engines__.cu)
+compiled for the CPU from where they lie (oracle/refgpu_driver.cpp; CPU only,
+skipped where the reference checkout was not built into oracle/_ref).
+
+The host build rounds every operation alone, so the oracle's interpolators
+run with fused=False here (the device contracts a few multiply-adds; the
+oracle's default mode fuses those).  The reference's tap rule is
+|apodtx*apodrx| > 0.01 against a double 0.01, which for float32 weights is
+>= the float after 0.01f.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+pytestmark = pytest.mark.skipif(oracle.refgpu_lib() is None,
+                                reason="the reference's kernels are not built here")
+
+GPU_RULE = float(np.nextafter(np.float32(0.01), np.float32(1)))
+POLY = [("korder_cubic", 4), ("korder_cubic", 8), ("korder_cubic", 16), ("akima", 0),
+        ("makima", 0)]
+
+
+def _tabbed_args(case):
+    return (case["rf"], case["tautx"], case["apodtx"], case["taurx"], case["apodrx"],
+            float(case["t0"]), float(case["dt"]), int(case["nt"]))
+
+
+@pytest.mark.parametrize("name", ["pw_small", "edge"])
+@pytest.mark.parametrize("interp,k", POLY)
+def test_tabbed_poly_kinds_equal_reference_kernels(golden, name, interp, k):
+    args = _tabbed_args(golden(f"tabbed_{name}.npz"))
+    for sumtype in ("tx_and_rx", "none"):
+        ref = oracle.das_tabbed_refgpu(*args, interp=interp, k=k, sumtype=sumtype)
+        orc = oracle.das_poly(*args, interp=interp, k=k, thresh=GPU_RULE, sumtype=sumtype,
+                              fused=False)
+        np.testing.assert_array_equal(orc, ref)
+
+
+@pytest.mark.parametrize("name", ["pw_small", "edge", "short2", "short3"])
+def test_tabbed_nearest_and_linear_equal_reference_kernels(golden, name):
+    """The reference's CUDA nearest (round half up) and linear (which returns
+    the floor sample: the oracle's linear_floor)."""
+    args = _tabbed_args(golden(f"tabbed_{name}.npz"))
+    for ref_kind, orc_kind in (("nearest", "nearest"), ("linear", "linear_floor")):
+        for sumtype in ("tx_and_rx", "none"):
+            ref = oracle.das_tabbed_refgpu(*args, interp=ref_kind, sumtype=sumtype)
+            orc = oracle.das_tabbed(*args, interp=orc_kind, thresh=GPU_RULE, sumtype=sumtype)
+            np.testing.assert_array_equal(orc, ref)
+
+
+def _focused_2d():
+    """Focused transmits with a depth of field (the reference's hourglass and
+    planar branches, __engines__.cu:409-423) and an F-number receive."""
+    rng = np.random.default_rng(5)
+    nele, ntx, nt = 32, 5, 512
+    xele = (np.arange(nele) - (nele - 1) / 2) * 0.3e-3
+    xf = np.linspace(-3e-3, 3e-3, ntx)
+    xs, zs = np.meshgrid(np.linspace(-5e-3, 5e-3, 40), np.linspace(5e-3, 25e-3, 60), indexing="ij")
+    f32 = lambda a: np.asarray(a, np.float32)
+    geo = dict(ovectx=f32(np.stack([xf, np.full(ntx, 15e-3)], 1)),
+               nvectx=f32(np.tile([0.0, 1.0], (ntx, 1))), doftx=f32(np.full(ntx, 6e-3)),
+               alatx=f32(np.full(ntx, 0.3)), t0tx=f32(np.full(ntx, 15e-3 / 1540.0)),
+               ovecrx=f32(np.stack([xele, np.zeros(nele)], 1)),
+               nvecrx=f32(np.tile([0.0, 1.0], (nele, 1))), alarx=f32(np.full(nele, 0.4)),
+               c0=np.float32(1540.0), pnts=f32(np.stack([xs.ravel(), zs.ravel()], 1)))
+    rf = rng.normal(size=(ntx, nele, nt)).astype(np.float32)
+    return geo, rf, np.float32(0.0), np.float32(1 / 20e6), nt
+
+
+def _diverging_3d():
+    from pycbf_gb300 import phantom
+    w = phantom.matrix_dw_synthetic(nside=8, nvs=2, nt=1024, nvox=(12, 12, 24), n_speckle=300,
+                                    lims=((-2e-3, 2e-3), (-2e-3, 2e-3), (5e-3, 15e-3)),
+                                    device="cpu")
+    return w.geometry, w.rf, w.t0, w.dt, w.nt
+
+
+def _oracle_synthetic(geo, rf, t0, dt, nt, interp, sumtype):
+    keys = ("ovectx", "nvectx", "doftx", "alatx", "t0tx", "ovecrx", "nvecrx", "alarx", "c0",
+            "pnts")
+    tabs = oracle.synth_tables(*(geo[k] for k in keys))
+    if interp in ("nearest", "linear"):
+        kind = "nearest" if interp == "nearest" else "linear_floor"
+        return oracle.das_tabbed(rf, *tabs, t0, dt, nt, interp=kind, thresh=0.01, sumtype=sumtype)
+    # the reference's Synthetic korder kernel receives k as 0 (an int32 in a float parameter)
+    return oracle.das_poly(rf, *tabs, t0, dt, nt, interp=interp, k=0, thresh=0.01,
+                           sumtype=sumtype, fused=False)
+
+
+@pytest.mark.parametrize("geometry", ["focused_2d", "diverging_3d"])
+@pytest.mark.parametrize("interp", ["nearest", "linear", "akima", "makima", "korder_cubic"])
+def test_synthetic_equals_reference_kernels(geometry, interp):
+    """Delays and masks computed per tap (calc_tautx_apodtx / calc_taurx_apodrx)
+    in geometries whose acceptance angles are far from the float resolution of
+    the cosine: every per-channel output equal."""
+    geo, rf, t0, dt, nt = _focused_2d() if geometry == "focused_2d" else _diverging_3d()
+    ref = oracle.das_synthetic_refgpu(rf, geo, t0, dt, nt, interp, k=8, sumtype="none")
+    np.testing.assert_array_equal(_oracle_synthetic(geo, rf, t0, dt, nt, interp, "none"), ref)
