@@ -153,6 +153,8 @@ def refgpu_lib(contracted: bool = False) -> ct.CDLL | None:
             R.rgd_synthetic.argtypes = [_i, _i, _p, _f, _f, _i, _i, _p, _ll, _ll, _ll, _ll, _p, _p,
                                         _p, _p, _p, _p, _p, _p, _f, _p, _i, _p]
             R.rgd_synthetic.restype = _i
+            R.rgd_dmas.argtypes = [_p, _ll, _ll, _p, _i, _i, _i, _p, _ll]
+            R.rgd_dmas.restype = _i
             _REFGPU[name] = R
         return _REFGPU[name]
 
@@ -216,6 +218,26 @@ def das_synthetic_refgpu(rf, geometry, t0, dt, nt, interp, k=4, sumtype="tx_and_
                          SUMTYPE_CODES[sumtype], _ptr(out))
     if st:
         raise ValueError("rgd_synthetic rejected its arguments")
+    return out
+
+
+def dmas_refgpu(im, nlag, power=False, sumlags=True, launched=None):
+    """DMAS from the reference's own kernel (calc_dmas,
+    pycbf/gpu/__advanced_engines__.cu:17-61) run on the CPU: im (nsep, np);
+    the lags are the positions 0..nlag-1 (the kernel does not read the lag
+    values).  launched: the number of threads the reference's class launches
+    (ceil(ntx*nrx*nop/nthread)*nthread); default every (lag, image, pixel)."""
+    R = refgpu_lib()
+    if R is None:
+        raise RuntimeError("the reference's kernels are not built (make -C oracle refgpu)")
+    im = _c32(im)
+    nsep, np_ = im.shape
+    lags = np.arange(nlag, dtype=np.int32)
+    out = np.zeros(np_ if sumlags else nlag * np_, dtype=np.float32)
+    n = nlag * nsep * np_ if launched is None else int(launched)
+    if R.rgd_dmas(_ptr(im), nsep, np_, _ptr(lags), int(nlag), int(bool(power)),
+                  int(bool(sumlags)), _ptr(out), n):
+        raise ValueError("rgd_dmas rejected its arguments")
     return out
 
 

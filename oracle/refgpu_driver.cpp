@@ -1,11 +1,12 @@
 /*
- * The reference's CUDA delay-and-sum kernels run on the CPU (test
- * infrastructure only).  pycbf/gpu/__engines__.cu is compiled from where it
- * lies (its path arrives as REF_ENGINES), with refgpu_shim.h standing in for
- * the CUDA built-ins; nothing of it is copied here.  Each entry point below
- * emulates the reference's launch of one kernel: one thread per
- * (frame, transmit, receive, pixel) tap, blocks of one thread, run in thread
- * order, each tap's atomicAdd a plain add.  The launch arguments are the ones
+ * The reference's CUDA delay-and-sum and DMAS kernels run on the CPU (test
+ * infrastructure only).  pycbf/gpu/__engines__.cu and __advanced_engines__.cu
+ * are compiled from where they lie (their paths arrive as REF_ENGINES and
+ * REF_ADVANCED), with refgpu_shim.h standing in for the CUDA built-ins;
+ * nothing of them is copied here.  Each entry point below emulates the
+ * reference's launch of one kernel: blocks of one thread, run in thread
+ * order (one per (frame, transmit, receive, pixel) tap for delay-and-sum),
+ * each atomicAdd a plain add.  The launch arguments are the ones
  * the reference's Python classes pass (pycbf/gpu/__core_bf_classes__.py:
  * 176-243 Synthetic, 291-354 Tabbed), including the int32 k that the
  * Synthetic korder kernel receives in a float parameter.
@@ -18,6 +19,7 @@
 
 #include "refgpu_shim.h"
 #include REF_ENGINES
+#include REF_ADVANCED
 
 namespace {
 
@@ -101,6 +103,21 @@ int rgd_synthetic(int interp, int k, const float *S, float t0, float dt, int nt,
                                              nvecrx, alarx, interp, c0, np, pnts, out, nfr, flag);
         });
     }
+    return 0;
+}
+
+/* DMAS (calc_dmas, pycbf/gpu/__advanced_engines__.cu:17-61) as the
+ * reference's classes launch it (gpu/__advanced_bf_classes__.py:51-63):
+ * nthreads emulated threads (their ceil(ntx*nrx*nop/nthread) blocks of
+ * nthread), each handling tid < nlag*nsep*np, lag = the lag's position.
+ * imout is accumulated into. */
+int rgd_dmas(const float *imsep, long long nsep, long long np, const int *lags, int nlag,
+             int sumtype, int sumlags, float *imout, long long nthreads)
+{
+    if (nthreads < 0 || nthreads >= (1LL << 32)) return 1;
+    launch_taps(nthreads, [&] {
+        calc_dmas(imsep, nsep, np, lags, nlag, sumtype, sumlags, imout);
+    });
     return 0;
 }
 

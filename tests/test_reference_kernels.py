@@ -1,5 +1,6 @@
-"""The oracle against the reference's own CUDA kernels (pycbf/gpu/__engines__.cu)
-compiled for the CPU from where they lie (oracle/refgpu_driver.cpp; CPU only,
+"""The oracle against the reference's own CUDA kernels (pycbf/gpu/__engines__.cu,
+__advanced_engines__.cu) compiled for the CPU from where they lie
+(oracle/refgpu_driver.cpp; CPU only,
 skipped where the reference checkout was not built into oracle/_ref).
 
 The host build rounds every operation alone, so the oracle's interpolators
@@ -97,3 +98,20 @@ def test_synthetic_equals_reference_kernels(geometry, interp):
     geo, rf, t0, dt, nt = _focused_2d() if geometry == "focused_2d" else _diverging_3d()
     ref = oracle.das_synthetic_refgpu(rf, geo, t0, dt, nt, interp, k=8, sumtype="none")
     np.testing.assert_array_equal(_oracle_synthetic(geo, rf, t0, dt, nt, interp, "none"), ref)
+
+
+@pytest.mark.parametrize("power", [False, True])
+@pytest.mark.parametrize("sumlags", [True, False])
+def test_dmas_equals_reference_kernel(golden, power, sumlags):
+    """calc_dmas (pycbf/gpu/__advanced_engines__.cu:17-61) over every (lag,
+    image, pixel): the oracle with the lags at the kernel's positions
+    0..nlag-1 agrees within float summation (the kernel adds in float in
+    thread order, the oracle in double)."""
+    g = golden("coherence_small.npz")
+    nrx, nx, nz = g["im"].shape
+    im = g["im"].reshape(nrx, nx * nz)
+    nlag = int(g["dmas_nlag"]) + 1
+    ref = oracle.dmas_refgpu(im, nlag, power=power, sumlags=sumlags).reshape(-1)
+    orc = oracle.dmas(im, np.arange(nlag), power=power, sumlags=sumlags).reshape(-1)
+    assert oracle.rel_l2(orc, ref) <= 1e-6
+    assert np.abs(orc - ref).max() <= 1e-6 * np.abs(ref).max()
