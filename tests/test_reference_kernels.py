@@ -115,3 +115,17 @@ def test_dmas_equals_reference_kernel(golden, power, sumlags):
     orc = oracle.dmas(im, np.arange(nlag), power=power, sumlags=sumlags).reshape(-1)
     assert oracle.rel_l2(orc, ref) <= 1e-6
     assert np.abs(orc - ref).max() <= 1e-6 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name", ["pw_small", "edge"])
+@pytest.mark.parametrize("interp,k", POLY)
+def test_device_contraction_stays_within_the_parity_bar(golden, name, interp, k):
+    """The kernels are checked against the oracle with the multiply-adds the
+    device contracts fused; the reference's host build rounds them alone.
+    The two oracle modes differ by cancellation in x - x0 - dx*n (korder) at
+    most ~3e-6, inside the 1e-5 image bar, and take the same taps."""
+    args = _tabbed_args(golden(f"tabbed_{name}.npz"))
+    fused = oracle.das_poly(*args, interp=interp, k=k, fused=True)
+    plain = oracle.das_poly(*args, interp=interp, k=k, fused=False)
+    assert oracle.rel_l2(fused, plain) <= 1e-5
+    np.testing.assert_array_equal(fused != 0, plain != 0)
