@@ -352,9 +352,10 @@ def tap_census(tautx, apodtx, taurx, apodrx, t0, dt, nt, interp="cubic", usf=1, 
     count = np.zeros(np_, dtype=np.int32)
     isum = np.zeros(np_, dtype=np.int64)
     code = {"nearest": 1, "korder_cubic": 4, "akima": 5, "makima": 6}.get(interp, 0)
-    lib().orc_tap_census(code, int(usf), float(t0), float(dt), int(nt), ntx, nrx, np_,
-                         float(thresh), _ptr(tautx), _ptr(apodtx), _ptr(taurx), _ptr(apodrx),
-                         _ptr(count), _ptr(isum))
+    with _POLY_LOCK:  # the poly kinds' range test reads the fusion switch
+        lib().orc_tap_census(code, int(usf), float(t0), float(dt), int(nt), ntx, nrx, np_,
+                             float(thresh), _ptr(tautx), _ptr(apodtx), _ptr(taurx),
+                             _ptr(apodrx), _ptr(count), _ptr(isum))
     return count, isum
 
 
