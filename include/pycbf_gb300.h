@@ -83,6 +83,14 @@ typedef struct pycbf_gb_rfinfo {
     int dtype;           /* PYCBF_GB_F32 / _F16 / _BF16 / _I16                     */
 } pycbf_gb_rfinfo;
 
+/* Size limits; beyond them a call returns PYCBF_GB_ERANGE before any CUDA
+ * call:
+ *   ntx, nrx <= 2^20; nt < 2^22; nframes <= 65535; np < 2^31;
+ *   cubic interpolation (the spline prefilter): nt <= 18000;
+ *   delay-and-sum: ntx <= 227 for Tabbed (151 with PYCBF_GB_SUM_RX_ONLY),
+ *   ntx <= 454 for Synthetic (227 with PYCBF_GB_SUM_RX_ONLY), the per-pixel
+ *   transmit delays and weights living in shared memory. */
+
 /* Synthetic-point geometry, all device pointers (float32).  The fields follow
  * the Synthetic dataclass (pycbf/__bf_base_classes__.py:166-178).  The acos
  * tests of __engines__.cu:412,427,468 are evaluated as cosine compares, so

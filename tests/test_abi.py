@@ -72,6 +72,32 @@ def test_tabbed_rejects_bad_rfinfo(bad, code):
     assert st == code
 
 
+def test_size_limits_return_erange():
+    """Each limit the header lists, one past it; every call is rejected before
+    any CUDA call (the pointers are never dereferenced)."""
+    L = _lib.load()
+    p = ct.c_void_p(16)
+
+    def tabbed(info, interp=0, sumtype=3, ws=None, wsb=0):
+        return L.pycbf_gb_das_tabbed(ct.byref(info), p, p, p, p, p, 10, None, interp, 0.01,
+                                     sumtype, None, p, ws, wsb, None)
+
+    assert tabbed(_info(ntx=(1 << 20) + 1)) == _lib.ERANGE
+    assert tabbed(_info(nrx=(1 << 20) + 1)) == _lib.ERANGE
+    assert tabbed(_info(ntx=228)) == _lib.ERANGE
+    assert tabbed(_info(ntx=152), sumtype=2) == _lib.ERANGE
+    cubic = _info(nt=18001)
+    need = L.pycbf_gb_workspace_bytes(ct.byref(cubic), _lib.INTERP["cubic"])
+    assert tabbed(cubic, interp=_lib.INTERP["cubic"], ws=p, wsb=need) == _lib.ERANGE
+
+    geo = _lib.SyntheticGeom(**{n: 16 for n, _ in _lib.SyntheticGeom._fields_
+                                if n not in ("np", "c0")}, np=10, c0=1540.0)
+    synth = lambda info, sumtype=3: L.pycbf_gb_das_synthetic(
+        ct.byref(info), p, ct.byref(geo), None, 0, sumtype, p, None, 0, None)
+    assert synth(_info(ndim=2, ntx=455)) == _lib.ERANGE
+    assert synth(_info(ndim=2, ntx=228), sumtype=2) == _lib.ERANGE
+
+
 def test_tabbed_rejects_null_and_codes():
     L = _lib.load()
     info = _info()
