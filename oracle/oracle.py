@@ -29,6 +29,7 @@ from __future__ import annotations
 import ctypes as ct
 import os
 import subprocess
+import sys
 import threading
 from concurrent.futures import ThreadPoolExecutor
 
@@ -129,7 +130,12 @@ def build_refgpu(ref_root: str = "/root/reference") -> str | None:
     src = os.path.join(ref_root, "pycbf", "gpu", "__engines__.cu")
     if not os.path.exists(src):
         return None
-    subprocess.run(["make", "-s", "-C", HERE, "refgpu", f"REF={ref_root}"], check=True)
+    r = subprocess.run(["make", "-s", "-C", HERE, "refgpu", f"REF={ref_root}"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:  # the checker only: its tests skip without it
+        print("oracle: the reference's kernels did not build:\n" + r.stderr[-2000:],
+              file=sys.stderr)
+        return None
     return os.path.join(HERE, "_ref", "libpycbf_refgpu.so")
 
 
