@@ -4,7 +4,9 @@
   sumtype, on seeded and edge cases (tests/golden/tabbed_*.npz) -- bit-exact.
 * The reference's own pycbf.c compiled here (oracle/_ref), where present --
   bit-exact on the same inputs.
-* The interpolation known answer of the reference notebook (35.48316740429086).
+* The interpolation known answer of the reference notebook (35.48316740429086),
+  and the notebook's RMSEs of the reference's GPU nearest / linear / akima /
+  makima, reproduced by its CUDA kernels compiled for the CPU.
 * SLSC and DMAS outputs of the reference notebook's own code.
 * The float64 yardstick agrees with the float32 oracle to float32 accuracy.
 """
@@ -143,20 +145,52 @@ def test_dmas_reference_kernel_lag_positions():
     np.testing.assert_allclose(out[0], np.abs(im).sum(0), rtol=1e-6)
 
 
-@pytest.mark.slow
-def test_interp_known_answer():
+@pytest.fixture(scope="module")
+def kat():
+    """The notebook's seeded data (tests/kat_interp.py), its argument tuple and
+    the CPU cubic image every RMSE is taken against."""
     import kat_interp
     d = kat_interp.make_data()
-    args = (d["rf"], d["tautxrx"], d["apod"], d["tautxrx"], d["apod"], d["t"][0], d["t"][1] - d["t"][0],
-            len(d["t"]))
-    cubic = oracle.das_tabbed(*args, interp="cubic")
+    args = (d["rf"], d["tautxrx"], d["apod"], d["tautxrx"], d["apod"], d["t"][0],
+            d["t"][1] - d["t"][0], len(d["t"]))
+    return d, args, oracle.das_tabbed(*args, interp="cubic")
+
+
+@pytest.mark.slow
+def test_interp_known_answer(kat):
+    import kat_interp
+    d, args, cubic = kat
     near = oracle.das_tabbed(*args, interp="nearest")
     rmse = kat_interp.rmse_roi(near, cubic, d)
     assert abs(rmse - kat_interp.NOTEBOOK_RMSE) <= 1e-9 * kat_interp.NOTEBOOK_RMSE
     with open(os.path.join(HERE, "golden", "kat_interp.json")) as fp:
-        kat = json.load(fp)
-    assert abs(float(np.sum(cubic.astype(np.float64))) - kat["checksum_cubic"]) < 1e-6 * abs(
-        kat["checksum_cubic"])
+        recorded = json.load(fp)
+    assert abs(float(np.sum(cubic.astype(np.float64))) - recorded["checksum_cubic"]) < 1e-6 * abs(
+        recorded["checksum_cubic"])
+
+
+# RMSEs against the CPU cubic image that the notebook printed for the
+# reference's GPU classes (compare_interpolation_methods.ipynb, cell 10 output)
+GPU_KAT = {"nearest": (35.48316740429086, 1e-6), "linear": (246.199658213788, 1e-7),
+           "akima": (246.1996543436526, 1e-7), "makima": (246.19965454650733, 1e-7)}
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("kind", list(GPU_KAT))
+def test_reference_gpu_known_answers(kat, kind):
+    """The reference's CUDA kernels compiled for the CPU (oracle/_ref) reproduce
+    the notebook's device-run RMSEs (float summation order aside: nearest
+    2e-7, the others 5e-9 relative); the oracle equals that build bit for bit
+    on the golden cases (tests/test_reference_kernels.py).  linear returns the
+    floor sample, and akima / makima multiply per-sample slopes by a delta in
+    seconds, so all three sit at ~246.2, about half the image RMS."""
+    import kat_interp
+    if oracle.refgpu_lib() is None:
+        pytest.skip("the reference's kernels are not built here")
+    d, args, cubic = kat
+    want, tol = GPU_KAT[kind]
+    got = kat_interp.rmse_roi(oracle.das_tabbed_refgpu(*args, interp=kind), cubic, d)
+    assert abs(got - want) <= tol * want
 
 
 def test_fp64_columns_agree_with_the_scipy_spline():
