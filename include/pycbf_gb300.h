@@ -11,6 +11,11 @@
  *   - is stream-ordered and does not synchronise;
  *   - keeps no mutable global state, so it is safe to call from several
  *     host threads on distinct outputs.
+ * The exception is pycbf_gb_das_tabbed_cubic_noalloc: it takes no
+ * workspace, because its scratch is a device array that the library itself
+ * holds (a fixed PYCBF_GB_NOALLOC_SCRATCH_BYTES on every GPU that loads the
+ * library), and that array is mutable global state shared by all its calls:
+ * calls that overlap on the GPU race on it.
  *
  * All arithmetic is float32.  Channel data may be stored as float32, float16,
  * bfloat16 or int16; delays, weights and sums stay float32.
@@ -351,8 +356,10 @@ int pycbf_gb_slsc(const float *im, const unsigned char *mask, long long nframes,
 /* inside this library, held by every GPU that loads it until the process */
 /* exits.  Channel data whose coefficients                                 */
 /* (pycbf_gb_workspace_bytes(rf, PYCBF_GB_INTERP_CUBIC)) exceed it are      */
-/* rejected with PYCBF_GB_ERANGE.  The first call on a device looks up the */
-/* array's address on that device; make it before any stream capture.     */
+/* rejected with PYCBF_GB_ERANGE; every check runs before any work is      */
+/* queued.  The first call on a device looks up the array's address on     */
+/* that device and keeps it (valid until a cudaDeviceReset); make it       */
+/* before any stream capture.                                              */
 /* All calls share the array: calls whose work overlaps on the GPU (other  */
 /* streams, other host threads) race on it.  Other arguments and results   */
 /* are those of pycbf_gb_das_tabbed with interp = cubic and no plan.       */

@@ -41,6 +41,7 @@ _REF = None
 _REFGPU: dict = {}
 _LOCK = threading.Lock()
 _POLY_LOCK = threading.Lock()  # guards the C library's fusion switch
+_NO_LOCK = __import__("contextlib").nullcontext()
 
 INTERP_CODES = {"cubic": 0, "nearest": 1, "linear": 2, "linear_floor": 3}
 SUMTYPE_CODES = {"none": 0, "tx_only": 1, "rx_only": 2, "tx_and_rx": 3}
@@ -60,12 +61,40 @@ def build(force: bool = False) -> str:
     return path
 
 
-def build_ref(ref_root: str = "/root/reference") -> str | None:
-    """Compile the reference's own pycbf.c into oracle/_ref when its checkout exists."""
-    src = os.path.join(ref_root, "pycbf", "cpu", "pycbf.c")
-    if not os.path.exists(src):
+def ref_root() -> str:
+    """The reference checkout: $PYCBF_REF, else the default that oracle/Makefile
+    names (its recipe is the one place that names this machine's checkout)."""
+    env = os.environ.get("PYCBF_REF")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+    return r.stdout.strip()
+
+
+def ref_src_copy() -> str:
+    """The private copy of the reference's pycbf.c (oracle/_ref/src, never committed)."""
+    return os.path.join(HERE, "_ref", "src", "pycbf.c")
+
+
+def build_ref(ref_root_dir: str | None = None) -> str | None:
+    """Compile the reference's own pycbf.c into oracle/_ref.
+
+    Where the checkout exists, from its sources where they lie (and a private
+    copy of the two C files is left in oracle/_ref/src, which is git-ignored);
+    elsewhere -- the GPU host, which has no checkout -- from that copy.  None
+    when neither exists."""
+    root = ref_root_dir or ref_root()
+    src = os.path.join(root, "pycbf", "cpu", "pycbf.c")
+    env = dict(os.environ, PYCBF_REF=root)
+    if os.path.exists(src):
+        subprocess.run(["make", "-s", "-C", HERE, "ref-src"], check=True, env=env)
+    elif not os.path.exists(ref_src_copy()):
         return None
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
+    r = subprocess.run(["make", "-s", "-C", HERE, "ref"], capture_output=True, text=True, env=env)
+    if r.returncode != 0:  # the baseline then falls back to the port
+        print("oracle: the reference's pycbf.c did not build:\n" + r.stderr[-2000:],
+              file=sys.stderr)
+        return None
     return os.path.join(HERE, "_ref", "libpycbf_ref.so")
 
 
@@ -124,19 +153,23 @@ def ref_lib() -> ct.CDLL | None:
         return _REF
 
 
-def build_refgpu(ref_root: str = "/root/reference") -> str | None:
+def build_refgpu(ref_root_dir: str | None = None, contracted: bool = False) -> str | None:
     """Compile the reference's CUDA kernels for the CPU into oracle/_ref when its
-    checkout exists (oracle/refgpu_driver.cpp)."""
-    src = os.path.join(ref_root, "pycbf", "gpu", "__engines__.cu")
+    checkout exists (oracle/refgpu_driver.cpp); contracted=True: the build with
+    multiply-adds fused, as NVRTC's default does."""
+    root = ref_root_dir or ref_root()
+    src = os.path.join(root, "pycbf", "gpu", "__engines__.cu")
     if not os.path.exists(src):
         return None
-    r = subprocess.run(["make", "-s", "-C", HERE, "refgpu", f"REF={ref_root}"],
-                       capture_output=True, text=True)
+    target = "refgpu-fused" if contracted else "refgpu"
+    r = subprocess.run(["make", "-s", "-C", HERE, target], capture_output=True, text=True,
+                       env=dict(os.environ, PYCBF_REF=root))
     if r.returncode != 0:  # the checker only: its tests skip without it
         print("oracle: the reference's kernels did not build:\n" + r.stderr[-2000:],
               file=sys.stderr)
         return None
-    return os.path.join(HERE, "_ref", "libpycbf_refgpu.so")
+    return os.path.join(HERE, "_ref", "libpycbf_refgpu_fused.so" if contracted
+                        else "libpycbf_refgpu.so")
 
 
 def refgpu_lib(contracted: bool = False) -> ct.CDLL | None:
@@ -358,11 +391,100 @@ def tap_census(tautx, apodtx, taurx, apodrx, t0, dt, nt, interp="cubic", usf=1, 
     count = np.zeros(np_, dtype=np.int32)
     isum = np.zeros(np_, dtype=np.int64)
     code = {"nearest": 1, "korder_cubic": 4, "akima": 5, "makima": 6}.get(interp, 0)
-    with _POLY_LOCK:  # the poly kinds' range test reads the fusion switch
+    # the poly kinds' range test reads the C library's fusion switch
+    lock = _POLY_LOCK if code >= 4 else _NO_LOCK
+    with lock:
         lib().orc_tap_census(code, int(usf), float(t0), float(dt), int(nt), ntx, nrx, np_,
                              float(thresh), _ptr(tautx), _ptr(apodtx), _ptr(taurx),
                              _ptr(apodrx), _ptr(count), _ptr(isum))
     return count, isum
+
+
+def _pixel_chunks(np_, threads, min_chunk=2048):
+    n = max(1, min(4 * max(1, threads), -(-np_ // min_chunk)))
+    edges = np.linspace(0, np_, n + 1).astype(np.int64)
+    return [(int(a), int(b)) for a, b in zip(edges[:-1], edges[1:]) if b > a]
+
+
+def das_tabbed_by_pixels(rf, tautx, apodtx, taurx, apodrx, t0, dt, nt, interp="cubic",
+                         thresh=1e-2, sumtype="tx_and_rx", threads=1, min_chunk=2048):
+    """das_tabbed over column ranges of the tables on a thread pool.
+
+    Pixels are independent, so each pixel's taps are still added in the
+    reference's own order (transmit-major, receive-minor, in place:
+    pycbf/cpu/__core_bf_classes__.py:240-245) whatever the split; only the
+    work is divided.  Sized for the large workloads (hundreds of millions of
+    table entries): no per-thread copy of a whole output.
+    """
+    rf = _c32(rf)
+    tautx, apodtx, taurx, apodrx = (np.asarray(a, np.float32) for a in (tautx, apodtx, taurx, apodrx))
+    ntx, nrx, np_ = tautx.shape[0], taurx.shape[0], tautx.shape[1]
+    rows = {"none": ntx * nrx, "tx_only": nrx, "rx_only": ntx, "tx_and_rx": 1}[sumtype]
+    out = np.zeros((rows, np_), np.float32)
+
+    def run(span):
+        p0, p1 = span
+        cols = [np.ascontiguousarray(a[:, p0:p1]) for a in (tautx, apodtx, taurx, apodrx)]
+        part = das_tabbed(rf, *cols, t0, dt, nt, interp=interp, thresh=thresh, sumtype=sumtype,
+                          threads=1)
+        out[:, p0:p1] = part.reshape(rows, p1 - p0)
+
+    with ThreadPoolExecutor(max(1, threads)) as ex:
+        list(ex.map(run, _pixel_chunks(np_, threads, min_chunk)))
+    return out.ravel()
+
+
+def tap_census_by_pixels(tautx, apodtx, taurx, apodrx, t0, dt, nt, interp="cubic", thresh=1e-2,
+                         threads=1, min_chunk=2048):
+    """tap_census over column ranges of the tables on a thread pool (cubic and
+    nearest; the per-pixel counts do not depend on the split)."""
+    if interp not in ("cubic", "nearest", "linear"):
+        raise ValueError("tap_census_by_pixels: cubic, linear or nearest")
+    np_ = tautx.shape[1]
+    count = np.zeros(np_, np.int32)
+    isum = np.zeros(np_, np.int64)
+
+    def run(span):
+        p0, p1 = span
+        cols = [np.ascontiguousarray(a[:, p0:p1]) for a in (tautx, apodtx, taurx, apodrx)]
+        c, s = tap_census(*cols, t0, dt, nt, interp=interp, thresh=thresh)
+        count[p0:p1] = c
+        isum[p0:p1] = s
+
+    with ThreadPoolExecutor(max(1, threads)) as ex:
+        list(ex.map(run, _pixel_chunks(np_, threads, min_chunk)))
+    return count, isum
+
+
+def dmas_by_pixels(im, lags, power=False, threads=1, min_chunk=2048):
+    """dmas (summed over lags) over column ranges of the per-element image."""
+    im = np.asarray(im, np.float32)
+    out = np.zeros(im.shape[1], np.float32)
+
+    def run(span):
+        p0, p1 = span
+        out[p0:p1] = dmas(np.ascontiguousarray(im[:, p0:p1]), lags, power=power)
+
+    with ThreadPoolExecutor(max(1, threads)) as ex:
+        list(ex.map(run, _pixel_chunks(im.shape[1], threads, min_chunk)))
+    return out
+
+
+def slsc_by_lines(im, mask, nlag, nkern, threads=1, min_chunk=4):
+    """slsc over ranges of lateral lines (the kernel is axial, so lines are
+    independent).  im, mask: (nrx, nx, nz)."""
+    im = np.asarray(im, np.float32)
+    nrx, nx, nz = im.shape
+    out = np.zeros((nx, nz), np.float64)
+
+    def run(span):
+        x0, x1 = span
+        out[x0:x1] = slsc(np.ascontiguousarray(im[:, x0:x1]), np.asarray(mask)[:, x0:x1], nlag,
+                          nkern)
+
+    with ThreadPoolExecutor(max(1, threads)) as ex:
+        list(ex.map(run, _pixel_chunks(nx, threads, min_chunk)))
+    return out
 
 
 def spline_y2(y, dt):

@@ -80,6 +80,27 @@ bool das_shape_ok(int geom, int sumtype, long long ntx) {
     return per * (size_t)ntx * 128 * sizeof(float) <= 227 * 1024;
 }
 
+}  // namespace
+
+// The argument checks of pycbf_gb_das_tabbed_prefiltered, in its order (also
+// run up front by the allocation-free entry point, before it queues any work).
+// coef may be a placeholder here: only its alignment is checked.
+int pgb::check_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef, const float *tautx,
+                                  const float *apodtx, const float *taurx, const float *apodrx,
+                                  long long np, float thresh, int sumtype, const float *out) {
+    int st = check_rf(rf, false, true);
+    if (st) return st;
+    if (!coef || !tautx || !apodtx || !taurx || !apodrx || !out) return PYCBF_GB_EINVAL;
+    if (reinterpret_cast<uintptr_t>(coef) % 16) return PYCBF_GB_EINVAL;
+    if (np < 0 || np >= (1LL << 31)) return PYCBF_GB_ERANGE;
+    if (np == 0) return PYCBF_GB_OK;
+    if (sumtype < 0 || sumtype > 5 || std::isnan(thresh)) return PYCBF_GB_EINVAL;
+    if (!das_shape_ok(GEOM_TABBED, sumtype, rf->ntx)) return PYCBF_GB_ERANGE;
+    return PYCBF_GB_OK;
+}
+
+namespace {
+
 // The TMA-staged kernel covers ntx <= 12 with the sums over transmits per
 // receive; its 16-byte bulk copies need channel strides and the data base
 // aligned to 16 bytes.
@@ -274,13 +295,10 @@ int pycbf_gb_das_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef,
                                     const float *apodrx, long long np, const int *pixel_index,
                                     float thresh, int sumtype, const void *plan, float *out,
                                     void *stream) {
-    int st = check_rf(rf, false, true);
+    int st = pgb::check_tabbed_prefiltered(rf, coef, tautx, apodtx, taurx, apodrx, np, thresh,
+                                           sumtype, out);
     if (st) return st;
-    if (!coef || !tautx || !apodtx || !taurx || !apodrx || !out) return PYCBF_GB_EINVAL;
-    if (reinterpret_cast<uintptr_t>(coef) % 16) return PYCBF_GB_EINVAL;
-    if (np <= 0 || np >= (1LL << 31)) return np == 0 ? PYCBF_GB_OK : PYCBF_GB_ERANGE;
-    if (sumtype < 0 || sumtype > 5 || std::isnan(thresh)) return PYCBF_GB_EINVAL;
-    if (!das_shape_ok(GEOM_TABBED, sumtype, rf->ntx)) return PYCBF_GB_ERANGE;
+    if (np == 0) return PYCBF_GB_OK;
     DasArgs a = {};
     fill_time_axis(a, rf);
     a.data = coef;

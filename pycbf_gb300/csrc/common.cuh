@@ -261,6 +261,11 @@ cudaError_t launch_dmas(const float *im, long long nframes, long long nsep, long
 cudaError_t launch_slsc(const float *im, const unsigned char *mask, long long nframes, int nrx,
                         int nx, int nz, int nlag, int nkern, float *out, cudaStream_t s);
 
+// argument checks of the cubic Tabbed delay-and-sum on prefiltered records (abi.cu)
+int check_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef, const float *tautx,
+                             const float *apodtx, const float *taurx, const float *apodrx,
+                             long long np, float thresh, int sumtype, const float *out);
+
 // int16 channel data -> float32 (spline.cu)
 cudaError_t launch_convert_i16(const short *src, long long n, float *dst, cudaStream_t s);
 

@@ -12,13 +12,18 @@
 //     every GPU that loads this library holds it until the process exits;
 //   - the first call on a device looks up the array's device address for that
 //     device (cudaGetSymbolAddress, with the device current) and remembers it,
-//     so that first call should come before any stream capture;
+//     so that first call should come before any stream capture; the
+//     remembered address assumes the device is not reset
+//     (cudaDeviceReset) while the library stays loaded;
 //   - every call shares the array and leaves the last call's coefficients in
 //     it; nothing in it needs to start at zero (the prefilter overwrites every
 //     coefficient it later reads), but calls whose work overlaps on the GPU --
 //     on two streams, or from two host threads -- race on it;
-//   - channel data whose coefficients exceed the array are rejected with
-//     PYCBF_GB_ERANGE before any work is queued.
+//   - every argument is checked before any work is queued: channel data whose
+//     coefficients exceed the array are rejected with PYCBF_GB_ERANGE, and the
+//     delay-and-sum's own checks (pointers, sizes, sum type, threshold) run
+//     first too, so a rejected call leaves the array untouched; np == 0 is a
+//     successful call that queues nothing.
 //
 // The work itself is the existing prefilter and cubic delay-and-sum entry
 // points, pointed at the array; nothing here calls cudaMalloc, cudaFree or an
@@ -35,6 +40,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 constexpr int kMaxDevices = 256;
 std::mutex g_scratch_mutex;
 void *g_scratch_ptr[kMaxDevices] = {};
+
+// A non-null, 16-byte aligned placeholder for the argument checks (never
+// dereferenced: the host-side name of a device array is not its address).
+const void *placeholder_coef() { return reinterpret_cast<const void *>(256); }
 
 // Device address of the array on the current device (looked up once per device).
 int scratch_address(void **out) {
@@ -62,10 +71,17 @@ extern "C" int pycbf_gb_das_tabbed_cubic_noalloc(const pycbf_gb_rfinfo *rf, cons
                                                  float thresh, int sumtype, float *out,
                                                  void *stream) {
     if (!rf) return PYCBF_GB_EINVAL;
+    if (!rfdata) return PYCBF_GB_EINVAL;
+    // the delay-and-sum's checks, with the (16-byte aligned) array standing in for
+    // the coefficients it will read
+    int st = pgb::check_tabbed_prefiltered(rf, placeholder_coef(), tautx, apodtx, taurx,
+                                           apodrx, np, thresh, sumtype, out);
+    if (st) return st;
     const size_t need = pycbf_gb_workspace_bytes(rf, PYCBF_GB_INTERP_CUBIC);
     if (need > kScratchBytes) return PYCBF_GB_ERANGE;
+    if (np == 0) return PYCBF_GB_OK;
     void *scratch = nullptr;
-    int st = scratch_address(&scratch);
+    st = scratch_address(&scratch);
     if (st) return st;
     st = pycbf_gb_spline_coefficients(rf, rfdata, scratch, kScratchBytes, stream);
     if (st) return st;

@@ -1,6 +1,7 @@
 """Generate the golden fixtures of tests/golden/ by running the reference itself.
 
-Runs only where the reference checkout exists (default /root/reference):
+Runs only where the reference checkout exists ($PYCBF_REF, else the default of
+oracle/Makefile):
 
 * the reference's own ``pycbf.cpu.TabbedBeamformer`` (pycbf/cpu/__core_bf_classes__.py)
   calling its own ``pycbf.c`` -- compiled by oracle/Makefile into a temporary
@@ -15,7 +16,7 @@ Runs only where the reference checkout exists (default /root/reference):
   vs CPU cubic RMSE, printed at :571 as 35.48316740429086) is recomputed from
   data regenerated by tests/kat_interp.py, through the reference's classes.
 
-Usage:  python tests/golden/make_golden.py [--ref /root/reference]
+Usage:  python tests/golden/make_golden.py [--ref CHECKOUT]
 """
 from __future__ import annotations
 
@@ -123,10 +124,11 @@ def run_reference(refcpu, case, kind, usf=1, sumtype="tx_and_rx"):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None)
     ap.add_argument("--skip-kat", action="store_true")
     args = ap.parse_args()
-    refcpu, tmp = import_reference(args.ref)
+    from oracle.oracle import ref_root
+    refcpu, tmp = import_reference(args.ref or ref_root())
 
     # ---- Tabbed cases through the reference's own CPU class ----------------
     cases = {"pw_small": small_pw_case(), "edge": edge_case(), "short2": short_case(2),

@@ -38,5 +38,12 @@ def main(ref):
     print("wrote korder_S.npz:", sorted(out))
 
 
+def oracle_ref_root() -> str:
+    """The reference checkout: $PYCBF_REF, else the default of oracle/Makefile."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))))
+    from oracle.oracle import ref_root
+    return ref_root()
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else oracle_ref_root())

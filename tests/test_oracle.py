@@ -205,3 +205,27 @@ def test_fp64_columns_agree_with_the_scipy_spline():
     c = oracle.das_fp64_columns(w.rf, w.tautx[:, sub], w.apodtx[:, sub], w.taurx[:, sub],
                                 w.apodrx[:, sub], w.t0, w.dt)
     assert oracle.rel_l2(c, a[sub]) <= 1e-5
+
+
+def test_pixel_split_oracle_equals_whole(golden):
+    """The pixel-range thread split keeps every pixel's summation order: the
+    image, the per-element image, the census, DMAS and SLSC equal the whole-range
+    calls bit for bit."""
+    case = golden("tabbed_pw_small.npz")
+    args = (case["rf"], case["tautx"], case["apodtx"], case["taurx"], case["apodrx"],
+            float(case["t0"]), float(case["dt"]), int(case["nt"]))
+    for sumtype in ("tx_and_rx", "tx_only", "none"):
+        whole = oracle.das_tabbed(*args, sumtype=sumtype, threads=1)
+        split = oracle.das_tabbed_by_pixels(*args, sumtype=sumtype, threads=3, min_chunk=50)
+        np.testing.assert_array_equal(whole, split)
+    np.testing.assert_array_equal(np.stack(oracle.tap_census(*args[1:])),
+                                  np.stack(oracle.tap_census_by_pixels(*args[1:], threads=3, min_chunk=50)))
+    nrx = case["taurx"].shape[0]
+    sep = oracle.das_tabbed(*args, sumtype="tx_only").reshape(nrx, -1)
+    lags = np.arange(1, nrx)
+    np.testing.assert_array_equal(oracle.dmas(sep, lags), oracle.dmas_by_pixels(sep, lags, threads=3, min_chunk=50))
+    nx, nz = 24, 32
+    mask = np.abs(case["apodrx"]).reshape(nrx, nx, nz) >= np.float32(0.01)
+    a = oracle.slsc(sep.reshape(nrx, nx, nz), mask, 4, 2)
+    b = oracle.slsc_by_lines(sep.reshape(nrx, nx, nz), mask, 4, 2, threads=3, min_chunk=2)
+    np.testing.assert_array_equal(a, b)

@@ -129,3 +129,48 @@ def test_device_contraction_stays_within_the_parity_bar(golden, name, interp, k)
     plain = oracle.das_poly(*args, interp=interp, k=k, fused=False)
     assert oracle.rel_l2(fused, plain) <= 1e-5
     np.testing.assert_array_equal(fused != 0, plain != 0)
+
+
+SYNTH_KEYS = ("ovectx", "nvectx", "doftx", "alatx", "t0tx", "ovecrx", "nvecrx", "alarx", "c0",
+              "pnts")
+
+
+def _mask_flips(w):
+    """Taps whose inclusion differs between the reference's kernels built with and
+    without contracted multiply-adds, and between the oracle's cosine compare and
+    the uncontracted build; the image differences beside them."""
+    g = w.geometry
+    run = lambda contracted: oracle.das_synthetic_refgpu(w.rf, g, w.t0, w.dt, w.nt, "linear",
+                                                         sumtype="none", contracted=contracted)
+    plain, fused = run(False), run(True)
+    tabs = oracle.synth_tables(*(g[k] for k in SYNTH_KEYS))
+    orc = oracle.das_tabbed(w.rf, *tabs, w.t0, w.dt, w.nt, interp="linear_floor", thresh=0.01,
+                            sumtype="none")
+    ntx, nrx = np.shape(g["ovectx"])[0], np.shape(g["ovecrx"])[0]
+    img = lambda a: a.reshape(ntx, nrx, -1).sum((0, 1))
+    flips = lambda a, b: int(((a != 0) != (b != 0)).sum())
+    return (flips(plain, fused), oracle.rel_l2(img(fused), img(plain)), flips(plain, orc),
+            oracle.rel_l2(img(orc), img(plain)), plain.size)
+
+
+@pytest.mark.skipif(oracle.build_refgpu(contracted=True) is None,
+                    reason="the contracted build of the reference's kernels is not available")
+def test_far_virtual_source_masks_depend_on_rounding():
+    """Plane waves modelled as virtual sources 10 m behind the array (the
+    192-element Synthetic workload's geometry, here 48 elements and 9 transmits)
+    have acceptance angles of ~4.5e-4 rad: |proj/mag| sits within a few float
+    steps of 1, and the reference's own decision acos(|proj/mag|) > ala
+    (pycbf/gpu/__engines__.cu:412,427) flips with how multiply-adds are
+    contracted.  In 3-D diverging waves nothing flips."""
+    from pycbf_gb300 import phantom
+    w = phantom.linear_pw_synthetic(nele=48, nsteer=9, nt=1536, nx=48, nz=96, n_speckle=2000,
+                                    xlim=(-4.8e-3, 4.8e-3), zlim=(5e-3, 20e-3), device="cpu")
+    f_ref, r_ref, f_orc, r_orc, n = _mask_flips(w)
+    print(f"far virtual sources: reference contracted vs not {f_ref}/{n} taps, rel-L2 {r_ref:.3g}; "
+          f"oracle vs reference {f_orc} taps, rel-L2 {r_orc:.3g}")
+    assert f_ref > 0.05 * n and r_ref > 0.1  # the reference disagrees with itself
+    w = phantom.matrix_dw_synthetic(nside=8, nvs=2, nt=1024, nvox=(12, 12, 24), n_speckle=300,
+                                    lims=((-2e-3, 2e-3), (-2e-3, 2e-3), (5e-3, 15e-3)),
+                                    device="cpu")
+    f_ref, r_ref, f_orc, r_orc, n = _mask_flips(w)
+    assert f_ref == 0 and f_orc == 0
