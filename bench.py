@@ -100,6 +100,82 @@ def algorithmic_bytes(w):
     return 4 * (2 * (ntx + nrx) * np_ + ntx * nrx * w.nt + np_)
 
 
+def fp64_columns(w, cols, dev):
+    """Float64 'tx_and_rx' image of the Tabbed workload at the pixel columns
+    `cols`: the natural cubic spline of every channel solved in float64, each
+    tap decided as the float32 C path decides it (|fl(apodtx apodrx)| >=
+    0.01, t0 <= fl(tautx + taurx) <= fl(t0 + fl(dt (nt-1)))) and evaluated at
+    the float64 delay sum.  The accuracy yardstick of the FP64 errors below
+    (pycbf/cpu/pycbf.c:68-166 and 179-207 carried out in double)."""
+    import numpy as np
+    import torch
+    f64 = torch.float64
+    rf = torch.as_tensor(w.rf, device=dev, dtype=f64)
+    ntx, nrx, nt = rf.shape
+    y = rf.reshape(-1, nt).T                                        # (nt, nch)
+    # natural spline: 0.5 z_i-1 + 2 z_i + 0.5 z_i+1 = (y_i+1 - 2 y_i + y_i-1) / 2, z = y'' dt^2 / 6
+    n = nt - 2
+    A = (torch.diag(torch.full((n,), 2.0, dtype=f64, device=dev))
+         + torch.diag(torch.full((n - 1,), 0.5, dtype=f64, device=dev), 1)
+         + torch.diag(torch.full((n - 1,), 0.5, dtype=f64, device=dev), -1))
+    z = torch.zeros_like(y)
+    z[1:-1] = torch.linalg.solve(A, 0.5 * (y[2:] - 2.0 * y[1:-1] + y[:-2]))
+    yz = torch.stack([y.T.reshape(ntx, nrx, nt), z.T.reshape(ntx, nrx, nt)])
+    t32 = lambda a: torch.as_tensor(np.ascontiguousarray(a[:, cols]), device=dev)
+    ttx, atx, trx, arx = t32(w.tautx), t32(w.apodtx), t32(w.taurx), t32(w.apodrx)
+    t0 = np.float32(w.t0)
+    xmax = np.float32(t0 + np.float32(np.float32(w.dt) * np.float32(nt - 1)))
+    x32 = ttx[:, None, :] + trx[None, :, :]                          # float32 sums, as the C path
+    ok = ((atx[:, None, :] * arx[None, :, :]).abs() >= np.float32(0.01)) & (x32 >= float(t0)) \
+        & (x32 <= float(xmax))
+    q = ((ttx.to(f64)[:, None, :] + trx.to(f64)[None, :, :]) - float(t0)) / float(np.float32(w.dt))
+    j = torch.clamp(torch.floor(q), 0, nt - 2).long()
+    a, b = (j + 1) - q, q - j
+    ti = torch.arange(ntx, device=dev)[:, None, None]
+    ri = torch.arange(nrx, device=dev)[None, :, None]
+    g = lambda k, jj: yz[k][ti, ri, jj]
+    s = a * g(0, j) + b * g(0, j + 1) + (a ** 3 - a) * g(1, j) + (b ** 3 - b) * g(1, j + 1)
+    apod = atx.to(f64)[:, None, :] * arx.to(f64)[None, :, :]
+    return torch.where(ok, apod * s, torch.zeros_like(s)).sum((0, 1))
+
+
+# Algorithmic work per unit (fixed here, used by every roofline entry):
+#   bytes: the compulsory traffic of one call -- delay/apodization tables (Tabbed,
+#          float32, read once), channel data in its storage type (read once per
+#          frame), pixel coordinates (Synthetic, float32), images (float32, written
+#          once); intermediates are not counted
+#   FLOPs: 20 per contributing cubic tap + 2 per tap (weight product and threshold),
+#          + 13 per (transmit, pixel) and (receive, pixel) delay of the Synthetic
+#          geometry (distance, projection, square root, division), + 3 per (pixel,
+#          receive) for DMAS (signed root, two multiply-adds), + for SLSC per pixel
+#          2 K sum_m (nrx - m) for the lag products and 4 K nrx for the per-element
+#          means and norms over the K = 2 nkern + 1 sample kernel; the adjoint adds
+#          26 per contributing tap (interpolation transpose and delay derivative) +
+#          2 per tap.
+def roofline_of(seconds, alg_bytes, flops, hbm_peak, fp32_peak, kernel, note=""):
+    t_hbm, t_fp32 = alg_bytes / (hbm_peak * 1e9), flops / (fp32_peak * 1e12)
+    out = {"bound": "hbm" if t_hbm >= t_fp32 else "fp32",
+           "hbm": {"achieved_gbs": alg_bytes / seconds / 1e9,
+                   "frac": alg_bytes / seconds / 1e9 / hbm_peak},
+           "fp32": {"achieved_tflops": flops / seconds / 1e12,
+                    "frac": flops / seconds / 1e12 / fp32_peak},
+           "algorithmic_bytes": int(alg_bytes), "flops": int(flops), "kernel": kernel}
+    out["frac"] = out["hbm"]["frac"] if out["bound"] == "hbm" else out["fp32"]["frac"]
+    if note:
+        out["note"] = note
+    return out
+
+
+def das_flops(contrib, taps, delays=0, extra=0):
+    return 20 * contrib + 2 * taps + 13 * delays + extra
+
+
+def rel_l2_t(a, b) -> float:
+    import torch
+    a, b = torch.as_tensor(a).double().ravel(), torch.as_tensor(b).double().ravel().to(a.device)
+    return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+
+
 # ---------------------------------------------------------------------------
 # CPU side
 # ---------------------------------------------------------------------------
@@ -364,9 +440,18 @@ def main_ours(a):
             "frac": flops / das_s / 1e12 / fp32_peak, "flops_per_launch": flops,
             "contributing_taps": n_contrib, "peak_source": "measured (FMA probe)"}
 
+    # float64 yardstick on 512 seeded pixels of the workload
+    import numpy as np
+    cols = np.sort(np.random.default_rng(2).choice(bf.nop, 512, replace=False))
+    f64 = fp64_columns(w, cols, dev)
+    fp64_plain = rel_l2_t(torch.as_tensor(np.asarray(img, np.float64)[cols], device=dev), f64)
+    roofline["fp64_rel_l2"] = fp64_plain
+
+    ctx = {"hbm_peak": hbm_peak, "fp32_peak": fp32_peak, "cols": cols, "f64": f64,
+           "contrib": n_contrib}
     variants = {}
     if not a.no_variants:
-        variants = run_variants(a, w, dev, taps)
+        variants = run_variants(a, w, dev, taps, ctx)
         for k in ("demod_256x512", "demod_512x1024"):
             if k in variants:
                 variants[k]["iq_fp32_frac"] = variants[k]["iq_tflops"] / fp32_peak
@@ -386,13 +471,24 @@ def main_ours(a):
     }
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, a.cpu_seconds)
+    # the target numbers in one compact key, last on the line: the plain FP32
+    # forward, the batched FP16-storage forward and the forward + adjoint in
+    # samples/s, their ratios to the plain forward and their FP64 errors
+    tg = {"plain_fp32": {"value": value, "fp64_rel_l2": fp64_plain,
+                         "hbm_frac": roofline["frac"], "fp32_frac": fp32["frac"]}}
+    for key in ("fp16_batch8", "fwd_adj_tabbed"):
+        v = variants.get(key)
+        if v:
+            tg[key] = {"value": v["value"], "vs_plain": v["value"] / value,
+                       "fp64_rel_l2": v.get("fp64_rel_l2")}
+    line["north_star_targets"] = tg
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
 
 
-def run_variants(a, w, dev, taps):
+def run_variants(a, w, dev, taps, ctx):
     """Secondary lines: batched frames with FP16/BF16 storage, and nearest."""
     import numpy as np
     import torch
@@ -402,7 +498,12 @@ def run_variants(a, w, dev, taps):
     want = (lambda g: True) if a.variants == "all" else (lambda g: g in a.variants.split(","))
     nfr = 8
     rng = np.random.default_rng(0)
-    frames = np.stack([w.rf] + [w.rf * np.float32(rng.uniform(0.5, 1.5)) for _ in range(nfr - 1)])
+    scales = [1.0] + [float(np.float32(rng.uniform(0.5, 1.5))) for _ in range(nfr - 1)]
+    frames = np.stack([w.rf] + [w.rf * np.float32(sc) for sc in scales[1:]])
+    hbm, fp32p, cols, f64 = ctx["hbm_peak"], ctx["fp32_peak"], ctx["cols"], ctx["f64"]
+    ntx, nrx, nt = w.rf.shape
+    np_ = w.tautx.shape[1]
+    table_bytes = 4 * 2 * (ntx + nrx) * np_
     stream = torch.cuda.current_stream()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
     batch8 = (("fp32_batch8", "float32", "cubic", nfr), ("fp16_batch8", "float16", "cubic", nfr),
@@ -424,12 +525,22 @@ def run_variants(a, w, dev, taps):
             e1.record(stream)
             torch.cuda.synchronize()
             times.append(e0.elapsed_time(e1) * 1e-3)
-        res[name] = {"value": taps * nf / statistics.mean(times), "unit": UNIT,
-                     "ms_per_call": 1e3 * statistics.mean(times), "frames_per_call": nf,
-                     "storage": storage, "interp": kind}
-    for group, fn in (("adjoint", lambda: run_adjoint_variants(a, w, dev, taps)),
-                      ("batch64", lambda: run_batch_variants(a, dev)),
-                      ("synthetic", lambda: run_synthetic_variants(a, dev)),
+        t = statistics.mean(times)
+        res[name] = {"value": taps * nf / t, "unit": UNIT,
+                     "ms_per_call": 1e3 * t, "frames_per_call": nf,
+                     "storage": storage, "interp": kind, "launches_per_call": 2}
+        if kind == "cubic":
+            nbytes = table_bytes + nf * (ntx * nrx * nt * x.element_size() + 4 * np_)
+            res[name]["roofline"] = roofline_of(
+                t, nbytes, nf * das_flops(ctx["contrib"], taps), hbm, fp32p,
+                "das_staged_kernel (frame, tile) items + spline_coef_kernel")
+            o = out.reshape(nf, -1)[:, torch.as_tensor(cols, device=dev)]
+            errs = [rel_l2_t(o[k], scales[k] * f64) for k in range(nf)]
+            res[name]["fp64_rel_l2"] = max(errs)
+            res[name]["fp64_rel_l2_note"] = "max over the frames, 512 seeded pixels"
+    for group, fn in (("adjoint", lambda: run_adjoint_variants(a, w, dev, taps, ctx)),
+                      ("batch64", lambda: run_batch_variants(a, dev, ctx)),
+                      ("synthetic", lambda: run_synthetic_variants(a, dev, ctx)),
                       ("tables", lambda: run_table_variant(a, dev)),
                       ("demod", lambda: run_demod_variant(a, dev)),
                       ("ingest", lambda: run_ingest_variant(a, w, dev, taps))):
@@ -577,7 +688,7 @@ def _synthetic(cls, w, **kw):
     return cls(**{k: g[k] for k in keys}, t0=w.t0, dt=w.dt, nt=w.nt, **kw)
 
 
-def run_synthetic_variants(a, dev):
+def run_synthetic_variants(a, dev, ctx):
     """Synthetic-point workloads with delays computed on the fly.
 
     synthetic_*: 192 elements at 0.2 mm, 75 plane waves over -18..18 deg (far
@@ -607,13 +718,31 @@ def run_synthetic_variants(a, dev):
         "synthetic_slsc": _synthetic(pg.SyntheticSLSCBeamformer, w, interp=cub, grid_shape=(nx, nz),
                               nlag=16, nkern=3),
     }
+    hbm, fp32p = ctx["hbm_peak"], ctx["fp32_peak"]
+    contrib = int(cases["synthetic_das"].tap_census()[0].sum().item())
+    ntx, nrx, np_ = 75, nrx, nx * nz
+    io_bytes = rf.numel() * 4 + 4 * 2 * np_ + 4 * np_       # channel data, pixels, image
+    base_flops = das_flops(contrib, ntx * nrx * np_, delays=(ntx + nrx) * np_)
+    K = 2 * 3 + 1
+    slsc_flops = np_ * (2 * K * sum(nrx - m for m in range(1, 17)) + 4 * K * nrx)
+    extra = {"synthetic_das": (0, "das_kernel<synthetic, cubic, tx_and_rx, f32> + spline_coef_kernel"),
+             "synthetic_dmas": (3 * np_ * nrx, "das_kernel<synthetic, cubic, dmas_ssr, f32> + "
+                                               "spline_coef_kernel (all-pairs sum fused)"),
+             "synthetic_slsc": (slsc_flops, "das_kernel<synthetic, cubic, tx_only, f32> + "
+                                            "slsc_kernel + spline_coef_kernel")}
+    launches = {"synthetic_das": 2, "synthetic_dmas": 2, "synthetic_slsc": 3}
     for name, bf in cases.items():
         call = lambda: bf(rf, out_as_numpy=False)
         call()
         t = _event_time(call, 3, flush, stream)
         taps = bf.ntx * bf.nrx * bf.nop
+        add, kern = extra[name]
         res[name] = {"value": taps / t, "unit": UNIT, "ms_per_call": 1e3 * t, "taps": taps,
-                     "workload": "synthetic 192el 75pw 4096s 512x1024", "interp": "cubic"}
+                     "contributing_taps": contrib, "launches_per_call": launches[name],
+                     "workload": "synthetic 192el 75pw 4096s 512x1024", "interp": "cubic",
+                     "roofline": roofline_of(t, io_bytes, base_flops + add, hbm, fp32p, kern),
+                     "tap_set": "far-virtual-source masks by the cosine compare of the oracle "
+                                "(the reference's own acos decision is rounding-dependent there)"}
         del bf
     del rf, w, cases
     torch.cuda.empty_cache()
@@ -625,13 +754,21 @@ def run_synthetic_variants(a, dev):
     call()
     t = _event_time(call, 2, flush, stream)
     taps = 8 * bf.ntx * bf.nrx * bf.nop
+    contrib = 8 * int(bf.tap_census()[0].sum().item())
+    np_ = bf.nop
+    io_bytes = frames.numel() * 2 + 4 * 3 * np_ + 4 * 8 * np_
+    flops = das_flops(contrib, taps, delays=8 * (bf.ntx + bf.nrx) * np_)
     res["matrix_3d_fp16"] = {"value": taps / t, "unit": UNIT, "ms_per_call": 1e3 * t,
-                         "frames_per_call": 8, "taps": taps, "storage": "float16",
-                         "workload": "synthetic 3-D 32x32 matrix 25dw 2048s 128x128x256"}
+                             "frames_per_call": 8, "taps": taps, "contributing_taps": contrib,
+                             "storage": "float16", "launches_per_call": 2,
+                             "workload": "synthetic 3-D 32x32 matrix 25dw 2048s 128x128x256",
+                             "roofline": roofline_of(t, io_bytes, flops, hbm, fp32p,
+                                                     "das_kernel<synthetic, cubic, tx_and_rx, f16> "
+                                                     "+ spline_coef_kernel")}
     return res
 
 
-def run_batch_variants(a, dev):
+def run_batch_variants(a, dev, ctx):
     """64 seeded uneven frames (ntx 1..75, nrx 64..192, nt 1024..4096, grids
     128x128..512x1024, Tabbed and Synthetic) in one persistent launch replayed
     as a CUDA graph, launch shape autotuned, for float32 / float16 / bfloat16
@@ -639,6 +776,7 @@ def run_batch_variants(a, dev):
     import numpy as np
     import torch
 
+    import pycbf_gb300 as pg
     from pycbf_gb300 import phantom
     from pycbf_gb300.batch import BatchBeamformer, beamformers_for
     frames = phantom.batch_frames(n=64, device=dev)
@@ -646,16 +784,34 @@ def run_batch_variants(a, dev):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
     reps = max(3, a.steps // 2)
     res, images32 = {}, None
+    contrib = None
     for storage in ("float32", "float16", "bfloat16"):
         t0 = time.perf_counter()
         bb = BatchBeamformer(beamformers_for(frames, storage))
         tune_s = time.perf_counter() - t0
         outs = bb([f["rf"] for f in frames])
         t = _event_time(bb.replay, reps, flush, stream)
+        if contrib is None:
+            contrib = [int(b.tap_census()[0].sum().item()) for b in bb.beamformers]
+        esize = {"float32": 4, "float16": 2, "bfloat16": 2}[storage]
+        nbytes, flops = 0, 0
+        for b, c in zip(bb.beamformers, contrib):
+            ntap = b.ntx * b.nrx * b.nop
+            nbytes += b.ntx * b.nrx * b.nt * esize + 4 * b.nop
+            if isinstance(b, pg.TabbedBeamformer):
+                nbytes += 4 * 2 * (b.ntx + b.nrx) * b.nop
+                flops += das_flops(c, ntap)
+            else:
+                nbytes += 4 * b.ndimp * b.nop
+                flops += das_flops(c, ntap, delays=(b.ntx + b.nrx) * b.nop)
         entry = {"value": bb.taps / t, "unit": UNIT, "ms_per_call": 1e3 * t, "frames_per_call": 64,
-                 "storage": storage, "taps_per_call": bb.taps, "launches_per_call": 2,
+                 "storage": storage, "taps_per_call": bb.taps,
+                 "launches_per_call": bb.launches_per_replay(),
                  "config": bb.config.__dict__, "configs_timed": len(bb.timings),
                  "setup_and_autotune_s": tune_s,
+                 "roofline": roofline_of(t, nbytes, flops, ctx["hbm_peak"], ctx["fp32_peak"],
+                                         "batch_spline_kernel + batch_das_kernel (queue form) or "
+                                         "every frame's spline + delay-and-sum (branch form)"),
                  "kinds": {k: sum(f["kind"] == k for f in frames) for k in ("tabbed", "synthetic")}}
         if storage == "float32":
             images32 = [o.clone() for o in outs]
@@ -684,7 +840,7 @@ def _event_time(fn, reps, flush, stream):
     return statistics.mean(times)
 
 
-def run_adjoint_variants(a, w, dev, taps):
+def run_adjoint_variants(a, w, dev, taps, ctx):
     """Forward + adjoint against the plain forward.
 
     fwd_adj_tabbed: the workload above through the differentiable path,
@@ -724,10 +880,25 @@ def run_adjoint_variants(a, w, dev, taps):
         fwd_tab(), fwd_adj_tab()
     t_f = _event_time(fwd_tab, reps, flush, stream)
     t_fa = _event_time(fwd_adj_tab, reps, flush, stream)
+    ntx, nrx, nt = w.rf.shape
+    np_ = bf.nop
+    nbytes = (4 * 2 * (ntx + nrx) * np_ + 4 * ntx * nrx * nt + 4 * np_      # forward
+              + 4 * np_ + 4 * ntx * nrx * nt + 4 * (ntx + nrx) * np_)      # gout, gradients
+    flops = das_flops(ctx["contrib"], taps) + 26 * ctx["contrib"] + 2 * taps
+    with torch.no_grad():
+        img = bf.differentiable(rf)
+    fwd_err = rel_l2_t(img.reshape(-1)[torch.as_tensor(ctx["cols"], device=dev)], ctx["f64"])
     res["fwd_adj_tabbed"] = {"value": taps / t_fa, "unit": UNIT, "ms_per_call": 1e3 * t_fa,
                              "forward_ms": 1e3 * t_f, "forward_value": taps / t_f,
                              "grads": ["rf", "tautx", "taurx"], "interp": "cubic",
-                             "sumtype": "tx_and_rx"}
+                             "sumtype": "tx_and_rx", "fp64_rel_l2": fwd_err,
+                             "fp64_rel_l2_note": "the forward image of the differentiable path, "
+                                                 "512 seeded pixels; gradients are checked "
+                                                 "against float64 autograd in the tests",
+                             "roofline": roofline_of(t_fa, nbytes, flops, ctx["hbm_peak"],
+                                                     ctx["fp32_peak"],
+                                                     "spline + das_staged_kernel + adj_delay_kernel "
+                                                     "+ adj_scatter_kernel + adj_finalize_kernel")}
 
     sw = phantom.two_layer_pw_synthetic(device=dev)
     g = sw.geometry
@@ -765,12 +936,23 @@ def run_adjoint_variants(a, w, dev, taps):
     t_f = _event_time(fwd_s, reps, flush, stream)
     t_fa = _event_time(fwd_adj_s, reps, flush, stream)
     t_tr = _event_time(train_step, reps, flush, stream)
+    scontrib = int(sbf.tap_census()[0].sum().item())
+    sntx, snrx, snt = sw.rf.shape
+    snp = sbf.nop
+    s_bytes = (4 * sntx * snrx * snt + 4 * 2 * snp + 4 * snp + 4 * snrx * snp     # forward
+               + 4 * snrx * snp + 4 * sntx * snrx * snt + 4 * snp)              # gout, gradients
+    s_flops = (das_flops(scontrib, staps, delays=(sntx + snrx) * snp) + 26 * scontrib
+               + 2 * staps)
     res["fwd_adj_sos"] = {"value": staps / t_fa, "unit": UNIT, "ms_per_call": 1e3 * t_fa,
                           "forward_ms": 1e3 * t_f, "forward_value": staps / t_f,
                           "train_step_ms": 1e3 * t_tr, "grads": ["rf", "slowness"],
                           "workload": "synthetic two-layer 128el 11pw 2048s 256x512, per-element "
                                       "images, 32x64 slowness map + global c",
-                          "interp": "cubic", "sumtype": "tx_only"}
+                          "interp": "cubic", "sumtype": "tx_only",
+                          "roofline": roofline_of(t_fa, s_bytes, s_flops, ctx["hbm_peak"],
+                                                  ctx["fp32_peak"],
+                                                  "spline + das_kernel<slowness> + adj_delay_kernel "
+                                                  "+ adj_scatter_kernel + adj_finalize_kernel")}
     return res
 
 

@@ -136,9 +136,14 @@ size_t pycbf_gb_workspace_bytes(const pycbf_gb_rfinfo *rf, int interp);
 /* Natural cubic spline coefficients of every channel.                     */
 /* Replaces tie_knots1D_fixed (pycbf/cpu/pycbf.c:114-166), which the      */
 /* reference runs per channel inside beamform_cubic (pycbf.c:194).        */
-/* coef receives, per channel and sample j, (y_j, y_j+1, z_j, z_j+1) with  */
-/* z = y'' dt^2 / 6 and y_nt = z_nt = 0; float32 x4 for F32 and I16       */
-/* channel data, the storage type x4 otherwise.  coef must hold            */
+/* coef receives, per channel and sample j, one record of the interval    */
+/* [t_j, t_j+1] with z = y'' dt^2 / 6 and y_nt = z_nt = 0.  F32 and I16    */
+/* channel data: float32 x4, the interval's cubic as a polynomial in the   */
+/* fraction b = (x - xlo_j) / dt, (p0, p1, p2, p3) with c_j = (xhi_j -     */
+/* xlo_j) / dt for the knots as the reference rounds them:                 */
+/*   p0 = c y_j + (c^3 - c) z_j,  p1 = y_j+1 - y_j + (1 - 3c^2) z_j - z_j+1, */
+/*   p2 = 3c z_j,  p3 = z_j+1 - z_j;                                       */
+/* F16/BF16: (y_j, y_j+1, z_j, z_j+1) in the storage type.  coef must hold */
 /* pycbf_gb_workspace_bytes(rf, PYCBF_GB_INTERP_CUBIC) bytes.              */
 /* ---------------------------------------------------------------------- */
 int pycbf_gb_spline_coefficients(const pycbf_gb_rfinfo *rf, const void *rfdata, void *coef,

@@ -245,6 +245,12 @@ class BatchBeamformer:
         self.timings = timings
         return best
 
+    def launches_per_replay(self) -> int:
+        """Kernel launches in one replay of the graph: the batched prefilter and
+        the persistent delay-and-sum (queue form), or every frame's own spline
+        prefilter and delay-and-sum (branch form)."""
+        return 2 if self.config.branches == 0 else 2 * len(self.beamformers)
+
     # -- use -----------------------------------------------------------------
     def replay(self):
         """Beamform what the input buffers hold (no copies)."""

@@ -70,6 +70,11 @@ void fill_time_axis(DasArgs &a, const pycbf_gb_rfinfo *rf) {
     volatile float span2 = rf->dt * (float)rf->nt;
     a.xend = rf->t0 + span2;
     a.eps = boundary_eps(rf->nt);
+    {
+        int k = 0;
+        while ((1LL << k) < (long long)rf->nt) ++k;
+        a.eps_fast = std::ldexp(1.25f * 1.5f, k - 23);
+    }
     // the last knot as NVRTC compiles x0 + dx*(nx-1) in the reference's CUDA kernels
     a.xfma = std::fmaf(rf->dt, (float)(rf->nt - 1), rf->t0);
 }
@@ -161,6 +166,7 @@ int prepare_data(const pycbf_gb_rfinfo *rf, const void *rfdata, int interp, void
     sa.coef = workspace;
     sa.nch = rf->nframes * rf->ntx * rf->nrx;
     sa.nt = rf->nt;
+    sa.t0 = rf->t0;
     sa.dt = rf->dt;
     int st = cuda_status(launch_spline(sa, rf->dtype, s));
     if (st) return st;

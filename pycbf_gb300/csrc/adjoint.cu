@@ -3,8 +3,8 @@
 // Forward (per frame f, pixel p, summed over the taps that contribute):
 //   img[p] += w * S_ch(x),  x = tau_tx(p) + tau_rx(p),  ch = (f, tx, rx)
 //   S(x) = a y_j + b y_j+1 + (a^3 - a) z_j + (b^3 - b) z_j+1
-// with the knot j, fractions a, b and the records (y, z) of the spline
-// prefilter, z = 1/2 T^-1 D y (T = tridiag(0.5, 2, 0.5) on the interior
+// with the knot j, fractions a, b and (y, z) of the spline prefilter (whose
+// float32 records hold the same cubic as a polynomial in b), z = 1/2 T^-1 D y (T = tridiag(0.5, 2, 0.5) on the interior
 // samples, D the second difference; natural ends z_0 = z_nt-1 = 0).
 //
 // Three kernels, all deterministic (no atomics; every sum has a fixed order):
@@ -49,13 +49,6 @@ __device__ __forceinline__ bool cubic_tap(float x, const DasArgs &a, int &j, flo
     am = b = 0.f;
     if (inr) knot_fractions(x, (float)idx, a, am, b);
     return inr;
-}
-
-// dS/dx: d(a)/dx = -1/dt, d(b)/dx = 1/dt
-__device__ __forceinline__ float cubic_slope(const float4 &c, float am, float b, float inv_dt) {
-    const float da = fmaf(3.f * am, am, -1.f);
-    const float db = fmaf(3.f * b, b, -1.f);
-    return (c.y - c.x + fmaf(db, c.w, -da * c.z)) * inv_dt;
 }
 
 // the upstream gradient of (frame f, receive r) at kernel-order pixel i (g.gk
@@ -135,17 +128,18 @@ __global__ void __launch_bounds__(kBlock) adj_delay_kernel(const __grid_constant
         for (int t0 = 0; t0 < ntx; t0 += G) {
             bool hit[G];
             int jj[G];
-            float am[G], bb[G], ap[G], sum[G];
+            float am[G], bb[G], ap[G], sum[G], xs[G];
             bool any = false;
 #pragma unroll
             for (int k = 0; k < G; ++k) {
                 const int t = t0 + k;
                 hit[k] = false;
                 jj[k] = 0;
-                am[k] = bb[k] = sum[k] = 0.f;
+                am[k] = bb[k] = sum[k] = xs[k] = 0.f;
                 ap[k] = 1.f;
                 if (t < ntx) {
                     const float x = __fadd_rn(stau[(size_t)t * kBlock], trx);
+                    xs[k] = x;
                     bool ok = true;
                     if (GEOM == GEOM_TABBED) {
                         ap[k] = __fmul_rn(sw[(size_t)t * kBlock], arx);
@@ -166,7 +160,9 @@ __global__ void __launch_bounds__(kBlock) adj_delay_kernel(const __grid_constant
                                                 jj[k]);
 #pragma unroll
                 for (int k = 0; k < G; ++k)
-                    if (hit[k]) sum[k] = fmaf(gp, cubic_slope(c[k], am[k], bb[k], a.inv_dt), sum[k]);
+                    if (hit[k])
+                        sum[k] = fmaf(gp, Kind<PYCBF_GB_INTERP_CUBIC, T>::slope(c[k], xs[k], (float)jj[k], a),
+                                      sum[k]);
             }
 #pragma unroll
             for (int k = 0; k < G; ++k) {

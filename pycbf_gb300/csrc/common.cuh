@@ -28,21 +28,46 @@ __device__ __forceinline__ float load_sample_reg(__nv_bfloat16 v) { return __bfl
 __device__ __forceinline__ float load_sample(const short *p) { return (float)__ldg(p); }
 __device__ __forceinline__ float load_sample_reg(short v) { return (float)v; }
 
-// A spline coefficient record (y_j, y_j+1, z_j, z_j+1): float4 for float32
-// channel data, four 16-bit values packed in a uint2 otherwise.
+// A spline coefficient record of interval j of a channel.
+//
+// float32 (and int16) channel data: the interval's cubic as a polynomial in
+// the fraction b = (x - xlo_j) / dt, v(b) = p0 + p1 b + p2 b^2 + p3 b^3, one
+// float4.  It equals the reference's evaluation (pycbf.c:93-98)
+//   a y_j + b y_j+1 + (a^3 - a) z_j + (b^3 - b) z_j+1,  a = (xhi_j - x) / dt
+// rewritten with a = c_j - b, c_j = (xhi_j - xlo_j) / dt, where xlo_j =
+// fl(t0 + fl(dt j)) and xhi_j = fl(t0 + fl(dt (j+1))) are the knots as the
+// reference rounds them (c_j differs from 1 by up to ~ulp(x)/dt):
+//   p0 = c y_j + (c^3 - c) z_j        p1 = y_j+1 - y_j + (1 - 3c^2) z_j - z_j+1
+//   p2 = 3c z_j                       p3 = z_j+1 - z_j
+// so a tap needs only b (from x and xlo_j) and three multiply-adds.
+// 16-bit channel data: (y_j, y_j+1, z_j, z_j+1) packed in a uint2 (the
+// polynomial's coefficients would lose more to 16-bit rounding).
 template <typename T> struct CoefRec;
 template <> struct CoefRec<float> {
     using raw = float4;
+    static constexpr bool kPoly = true;
     static __device__ __forceinline__ float4 load(const raw *p) { return __ldg(p); }
     static __device__ __forceinline__ float4 unpack(const raw &r) { return r; }
-    static __device__ __forceinline__ raw pack(float a, float b, float c, float d) {
-        return make_float4(a, b, c, d);
+    // the record of interval j from the samples and second-derivative terms
+    static __device__ __forceinline__ raw make(float y0, float y1, float z0, float z1, int j,
+                                               float t0, float dt) {
+        const float xlo = __fadd_rn(t0, __fmul_rn(dt, (float)j));
+        const float xhi = __fadd_rn(t0, __fmul_rn(dt, (float)(j + 1)));
+        const float c = __fdiv_rn(__fsub_rn(xhi, xlo), dt);
+        const float c2 = c * c;
+        return make_float4(fmaf(c2 * c - c, z0, c * y0), fmaf(1.f - 3.f * c2, z0, y1 - y0) - z1,
+                           3.f * c * z0, z1 - z0);
     }
 };
 // int16 channels are prefiltered into float32 records
 template <> struct CoefRec<short> : CoefRec<float> {};
 template <> struct CoefRec<__half> {
     using raw = uint2;
+    static constexpr bool kPoly = false;
+    static __device__ __forceinline__ raw make(float y0, float y1, float z0, float z1, int, float,
+                                               float) {
+        return pack(y0, y1, z0, z1);
+    }
     static __device__ __forceinline__ float4 load(const raw *p) { return unpack(__ldg(p)); }
     static __device__ __forceinline__ float4 unpack(raw r) {
         __half2 h0 = *reinterpret_cast<__half2 *>(&r.x);
@@ -60,6 +85,11 @@ template <> struct CoefRec<__half> {
 };
 template <> struct CoefRec<__nv_bfloat16> {
     using raw = uint2;
+    static constexpr bool kPoly = false;
+    static __device__ __forceinline__ raw make(float y0, float y1, float z0, float z1, int, float,
+                                               float) {
+        return pack(y0, y1, z0, z1);
+    }
     static __device__ __forceinline__ float4 load(const raw *p) { return unpack(__ldg(p)); }
     static __device__ __forceinline__ float4 unpack(raw r) {
         __nv_bfloat162 h0 = *reinterpret_cast<__nv_bfloat162 *>(&r.x);
@@ -104,6 +134,11 @@ __device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
     asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
     return unpack2(r);
 }
+__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+    return unpack2(r);
+}
 __device__ __forceinline__ float2 fma2_rn(float2 a, float2 b, float2 c) {
     unsigned long long r;
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)), "l"(pack2(c)));
@@ -130,7 +165,7 @@ struct SplineArgs {
     void *coef;              // (nch, nt) coefficient records
     long long nch;
     int nt;
-    float dt;
+    float t0, dt;            // the time axis (the float32 records depend on the knots)
 };
 cudaError_t launch_spline(const SplineArgs &a, int dtype, cudaStream_t s);
 
@@ -158,6 +193,9 @@ struct DasArgs {
     long long np;
     int ntx, nrx, nt, ndim, nframes;
     float t0, dt, inv_dt, xmax, xend, thresh, eps;
+    // the staged cubic taps' floor test: 1.25 x the largest gap 1.5 |q| 2^-23
+    // between the reciprocal quotient and the IEEE quotient for |q| < nt
+    float eps_fast;
     const float *slow;  // GEOM_SYNTH_SLOW: slowness per pixel (s/m), kernel pixel order
     float xfma;         // fma(dt, nt-1, t0): the last knot as the reference's CUDA kernels round it
     // staged kernel: SM cycles after which an mbarrier wait gives up (0: 2^31,

@@ -83,16 +83,39 @@ template <typename T> struct Kind<PYCBF_GB_INTERP_CUBIC, T> {
         using rec = typename CoefRec<T>::raw;
         return CoefRec<T>::load(static_cast<const rec *>(data) + ch + idx);
     }
-    // fj: the knot index as a float (exact: j < 2^23)
-    // knot positions (xhi, xlo), fractions (a, b) and cubic weights in packed
-    // float32 pairs, each lane rounded as knot_fractions rounds it; b comes
-    // from (xlo - x) * -1/dt, the same bits as (x - xlo) * 1/dt
+    // fj: the knot index as a float (exact: j < 2^23).
+    // float32 records: b = (x - xlo) / dt with xlo = fl(t0 + fl(dt j)) as the
+    // reference rounds it (x - xlo is exact), then the interval's polynomial.
+    // 16-bit records (y, z): knot positions (xhi, xlo), fractions (a, b) and
+    // cubic weights in packed float32 pairs, each lane rounded as
+    // knot_fractions rounds it; b comes from (xlo - x) * -1/dt, the same bits
+    // as (x - xlo) * 1/dt.
     static __device__ __forceinline__ float value(const P &c, float x, float fj, const DasArgs &a) {
-        const float2 K = add2_rn(make_float2(a.t0, a.t0),
-                                 make_float2(__fmul_rn(a.dt, __fadd_rn(fj, 1.0f)), __fmul_rn(a.dt, fj)));
-        const float2 AB = mul2_rn(add2_rn(K, make_float2(-x, -x)), make_float2(a.inv_dt, -a.inv_dt));
-        const float2 W = fma2_rn(mul2_rn(AB, AB), AB, make_float2(-AB.x, -AB.y));
-        return fmaf(AB.x, c.x, fmaf(AB.y, c.y, fmaf(W.x, c.z, W.y * c.w)));
+        if constexpr (CoefRec<T>::kPoly) {
+            const float xlo = __fadd_rn(a.t0, __fmul_rn(a.dt, fj));
+            const float b = __fmul_rn(__fsub_rn(x, xlo), a.inv_dt);
+            return fmaf(fmaf(fmaf(c.w, b, c.z), b, c.y), b, c.x);
+        } else {
+            const float2 K = add2_rn(make_float2(a.t0, a.t0),
+                                     make_float2(__fmul_rn(a.dt, __fadd_rn(fj, 1.0f)), __fmul_rn(a.dt, fj)));
+            const float2 AB = mul2_rn(add2_rn(K, make_float2(-x, -x)), make_float2(a.inv_dt, -a.inv_dt));
+            const float2 W = fma2_rn(mul2_rn(AB, AB), AB, make_float2(-AB.x, -AB.y));
+            return fmaf(AB.x, c.x, fmaf(AB.y, c.y, fmaf(W.x, c.z, W.y * c.w)));
+        }
+    }
+    // dS/dx at x (the delay derivative of the adjoint): d(b)/dx = 1/dt, d(a)/dx = -1/dt
+    static __device__ __forceinline__ float slope(const P &c, float x, float fj, const DasArgs &a) {
+        if constexpr (CoefRec<T>::kPoly) {
+            const float xlo = __fadd_rn(a.t0, __fmul_rn(a.dt, fj));
+            const float b = __fmul_rn(__fsub_rn(x, xlo), a.inv_dt);
+            return fmaf(fmaf(3.f * c.w, b, 2.f * c.z), b, c.y) * a.inv_dt;
+        } else {
+            float am, b;
+            knot_fractions(x, fj, a, am, b);
+            const float da = fmaf(3.f * am, am, -1.f);
+            const float db = fmaf(3.f * b, b, -1.f);
+            return (c.y - c.x + fmaf(db, c.w, -da * c.z)) * a.inv_dt;
+        }
     }
 };
 

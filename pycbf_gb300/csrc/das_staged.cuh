@@ -3,14 +3,15 @@
 // The pixels of a CTA (a "tile": 128 consecutive table columns, which the
 // host stores in Morton order of their delays) need, for each (tx, rx)
 // channel, only the samples between the smallest and largest delay of the
-// tile.  A plan, built once per table set (tabbed_plan_kernel), records per
-// tile the receives that can contribute at all (the exact reject
-// fl(max|apodtx| * |apodrx|) >= thresh of at least one pixel), and per tile
-// the delay bounds of every transmit and of every live receive.  In the main
-// kernel warp 0 turns those bounds into sample windows (the same exact index
-// rule as the taps, and indices are monotonic in the delay, so every
-// contributing tap falls inside) and issues one cp.async.bulk per transmit
-// into a 4-stage ring, completing on an mbarrier; all warps then gather from
+// tile's pixels that the receive can reach.  A plan, built once per table set
+// (tabbed_plan_kernel), records per tile the receives that can contribute at
+// all (the exact reject fl(max|apodtx| * |apodrx|) >= thresh of at least one
+// pixel) and, per live receive and transmit, that window: the exact index rule
+// of the taps applied to the smallest and largest delay sum fl(tautx + taurx)
+// over the pixels the receive reaches (indices are monotonic in the delay, so
+// every contributing tap falls inside), aligned to 16 bytes.  In the main
+// kernel one warp per live receive issues one cp.async.bulk per transmit into
+// a 4-stage ring, completing on an mbarrier; all warps then gather from
 // shared memory.  A receive whose windows exceed a stage is not staged and its
 // taps gather from global memory instead.
 //
@@ -31,9 +32,11 @@ constexpr unsigned kWaitLimit = 1u << 30;  // polls; the ~1 s clock bound ends a
 
 // plan layout (int32 words): [0] status, [1] work-queue head of the staged
 // kernel, [2] number of block items, [3] pad, then per tile a record of
-// plan_tile_words(ntx, nrx) words:
-//   nlive | rx index per live receive (nrx) | rx lo,hi per live receive (2*nrx floats)
-//   | tx lo,hi per transmit (2*ntx floats)
+// plan_tile_words(nrx) words:
+//   [0] nlive, [1..3] pad, then per live receive k (in receive order) 16 words
+//   at 4 + 16 k: [0] code (receive index, | kUnstaged when its windows exceed
+//   a stage), [1] total staged elements, [2..3] pad, [4 + t] the window of
+//   transmit t: first element e0 | (element offset in the stage << 19)
 // then the tile order (one int per tile, most live receives first), a
 // per-tile counter, the block items (int4 each: tile, first and one-past-last
 // position in the tile's live list, block ordinal << 16 | blocks of the
@@ -48,17 +51,22 @@ constexpr unsigned kWaitLimit = 1u << 30;  // polls; the ~1 s clock bound ends a
 // the average CTA's share -- and the last item of a tile to finish adds the
 // tile's block sums in block order.
 constexpr int kRxBlock = kRxBlockSum;
-__host__ __device__ inline long long plan_tile_words(int ntx, int nrx) {
-    return 1 + (long long)nrx + 2LL * nrx + 2LL * ntx;
+constexpr int kRxWords = 16;           // plan words per live receive
+constexpr int kUnstaged = 0x40000000;  // receive code flag: gathered from global memory
+constexpr int kWinBits = 19;           // window start bits (the staged path needs nt <= 2^19)
+constexpr int kStagedMaxNt = 1 << kWinBits;
+__host__ __device__ inline long long plan_tile_words(int nrx) {
+    return 4 + (long long)kRxWords * nrx;
 }
 constexpr int kPlanHeaderWords = 4;
 struct PlanLayout {
     long long tiles, tile_words, max_blocks, order, counters, items, partials, total;
 };
 __host__ __device__ inline PlanLayout plan_layout(long long np, int ntx, int nrx) {
+    (void)ntx;
     PlanLayout L;
     L.tiles = (np + kBlock - 1) / kBlock;
-    L.tile_words = plan_tile_words(ntx, nrx);
+    L.tile_words = plan_tile_words(nrx);
     L.max_blocks = (nrx + kRxBlock - 1) / kRxBlock;
     L.order = kPlanHeaderWords + L.tiles * L.tile_words;
     L.counters = L.order + L.tiles;
@@ -177,97 +185,122 @@ __device__ __forceinline__ typename Kind<KIND, T>::P staged_load(
 }
 
 // ---------------------------------------------------------------------------
-// plan: one CTA per tile
+// plan: one CTA per tile.  Pass 1 marks the live receives (a warp per
+// receive, each lane four of the tile's pixels); thread 0 numbers them in
+// receive order; pass 2 computes each live receive's windows: per transmit
+// the smallest and largest delay sum over the pixels the receive reaches,
+// reduced over the warp, through the exact window rule.  The windows of a
+// receive are packed one after another (each 16-byte aligned) into one stage;
+// a receive whose windows exceed a stage is marked unstaged.
 // ---------------------------------------------------------------------------
 template <int KIND, typename T>
 __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_constant__ DasArgs a,
                                                              int *plan) {
     using E = typename StagedElem<KIND, T>::E;
-    __shared__ float red[3][kBlock / 32];
-    __shared__ int s_any;
+    constexpr unsigned kFull = 0xffffffffu;
+    extern __shared__ int s_pos[];  // nrx: position of each receive in the live list, or -1
+    __shared__ float s_tt[kTxReg][kBlock];
+    __shared__ float s_amax[kBlock];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    constexpr int kWarps = kBlock / 32;
     const long long tile = blockIdx.x;
-    const long long i = tile * kBlock + tid;
-    const bool valid = i < a.np;
+    const long long np = a.np;
     const int ntx = a.ntx, nrx = a.nrx;
-    int *rec = plan + kPlanHeaderWords + tile * plan_tile_words(ntx, nrx);
-    int *rxidx = rec + 1;
-    float *rxlh = reinterpret_cast<float *>(rec + 1 + nrx);
-    float *txlh = rxlh + 2 * nrx;
-    const float inf = __int_as_float(0x7f800000);
-
-    auto block_minmax = [&](float lo, float hi, int any, float &blo, float &bhi, int &bany) {
-        for (int o = 16; o; o >>= 1) {
-            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-            any |= __shfl_xor_sync(0xffffffffu, any, o);
+    int *rec = plan + kPlanHeaderWords + tile * plan_tile_words(nrx);
+    const float nan = __int_as_float(0x7fc00000);
+    {
+        const long long i = tile * kBlock + tid;
+        const bool valid = i < np;
+        float amax = 0.f;
+        for (int t = 0; t < ntx; ++t) {
+            s_tt[t][tid] = valid ? __ldg(a.tautx + (long long)t * np + i) : nan;
+            if (valid) amax = fmaxf(amax, fabsf(__ldg(a.apodtx + (long long)t * np + i)));
         }
-        __syncthreads();
-        if (lane == 0) {
-            red[0][w] = lo;
-            red[1][w] = hi;
-            red[2][w] = __int_as_float(any);
-        }
-        __syncthreads();
-        blo = red[0][0];
-        bhi = red[1][0];
-        bany = __float_as_int(red[2][0]);
-        for (int k = 1; k < kBlock / 32; ++k) {
-            blo = fminf(blo, red[0][k]);
-            bhi = fmaxf(bhi, red[1][k]);
-            bany |= __float_as_int(red[2][k]);
-        }
-    };
-
-    float amax = 0.f;
-    for (int t = 0; t < ntx; ++t) {
-        float tau = inf, taun = -inf;
-        if (valid) {
-            tau = taun = __ldg(a.tautx + (long long)t * a.np + i);
-            amax = fmaxf(amax, fabsf(__ldg(a.apodtx + (long long)t * a.np + i)));
-        }
-        float lo, hi;
-        int any;
-        block_minmax(tau == tau ? tau : inf, taun == taun ? taun : -inf, 0, lo, hi, any);
-        if (tid == 0) {
-            txlh[2 * t] = lo;
-            txlh[2 * t + 1] = hi;
-        }
+        s_amax[tid] = amax;  // 0 for pixels past the end: never live
     }
     __syncthreads();
-    int nlive = 0;
-    for (int r = 0; r < nrx; ++r) {
-        float trx = 0.f, arx = 0.f;
-        if (valid) {
-            trx = __ldg(a.taurx + (long long)r * a.np + i);
-            arx = __ldg(a.apodrx + (long long)r * a.np + i);
+    // the receive's delay at pixel lane + 32 m and whether the receive reaches it
+    auto rx_pixels = [&](int r, float (&tr)[kBlock / 32], bool (&lv)[kBlock / 32]) {
+#pragma unroll
+        for (int m = 0; m < kBlock / 32; ++m) {
+            const int p = lane + 32 * m;
+            const long long i = tile * kBlock + p;
+            tr[m] = 0.f;
+            lv[m] = false;
+            if (i < np) {
+                tr[m] = __ldg(a.taurx + (long long)r * np + i);
+                const float ar = __ldg(a.apodrx + (long long)r * np + i);
+                lv[m] = (__fmul_rn(s_amax[p], fabsf(ar)) >= a.thresh) && (tr[m] == tr[m]);
+            }
         }
-        const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh) && (trx == trx);
-        float lo, hi;
-        int any;
-        block_minmax(live ? trx : inf, live ? trx : -inf, live ? 1 : 0, lo, hi, any);
-        if (!any) continue;
-        // staged only if all windows of this receive fit one stage
-        int bytes = 0;
-        if (tid < ntx) {
-            const float xlo = __fadd_rn(txlh[2 * tid], lo), xhi = __fadd_rn(txlh[2 * tid + 1], hi);
-            int e0, e1;
-            staged_window<KIND, T>(xlo, xhi, a, e0, e1);
-            bytes = (e1 - e0) * (int)sizeof(E);
-        }
-        for (int o = 16; o; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
-        if (w == 0 && lane == 0) s_any = bytes;
-        __syncthreads();
-        const bool staged = s_any <= kStageBytes;
-        if (tid == 0) {
-            rxidx[nlive] = staged ? r : (r | 0x40000000);
-            rxlh[2 * nlive] = lo;
-            rxlh[2 * nlive + 1] = hi;
-        }
-        ++nlive;
-        __syncthreads();
+    };
+    for (int r = w; r < nrx; r += kWarps) {
+        float tr[kBlock / 32];
+        bool lv[kBlock / 32];
+        rx_pixels(r, tr, lv);
+        bool any = false;
+#pragma unroll
+        for (int m = 0; m < kBlock / 32; ++m) any |= lv[m];
+        any = __any_sync(kFull, any);
+        if (lane == 0) s_pos[r] = any ? 1 : 0;
     }
-    if (tid == 0) rec[0] = nlive;
+    __syncthreads();
+    if (tid == 0) {
+        int run = 0;
+        for (int r = 0; r < nrx; ++r) s_pos[r] = s_pos[r] ? run++ : -1;
+        rec[0] = run;
+        rec[1] = rec[2] = rec[3] = 0;
+    }
+    __syncthreads();
+    for (int r = w; r < nrx; r += kWarps) {
+        const int k = s_pos[r];
+        if (k < 0) continue;
+        float tr[kBlock / 32];
+        bool lv[kBlock / 32];
+        rx_pixels(r, tr, lv);
+        int my_e0 = 0, my_cnt = 0;
+        for (int t = 0; t < ntx; ++t) {
+            float lo = __int_as_float(0x7f800000), hi = -lo;
+#pragma unroll
+            for (int m = 0; m < kBlock / 32; ++m) {
+                const float x = __fadd_rn(s_tt[t][lane + 32 * m], tr[m]);
+                if (lv[m] && x == x) {
+                    lo = fminf(lo, x);
+                    hi = fmaxf(hi, x);
+                }
+            }
+            for (int o = 16; o; o >>= 1) {
+                lo = fminf(lo, __shfl_xor_sync(kFull, lo, o));
+                hi = fmaxf(hi, __shfl_xor_sync(kFull, hi, o));
+            }
+            int e0, e1;
+            staged_window<KIND, T>(lo, hi, a, e0, e1);
+            if (lane == t) {
+                my_e0 = e0;
+                my_cnt = e1 - e0;
+            }
+        }
+        // stage offsets: exclusive prefix of the window lengths over the transmits
+        int off = my_cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(kFull, off, o);
+            if (lane >= o) off += v;
+        }
+        const int total = __shfl_sync(kFull, off, 31);
+        off -= my_cnt;
+        const bool staged = (long long)total * (long long)sizeof(E) <= kStageBytes &&
+                            a.nt <= kStagedMaxNt;
+        int *rr = rec + 4 + (long long)kRxWords * k;
+        if (lane == 0) {
+            rr[0] = staged ? r : (r | kUnstaged);
+            rr[1] = staged ? total : 0;
+            rr[2] = rr[3] = 0;
+        }
+        if (lane < kTxReg)
+            rr[4 + lane] = (staged && lane < ntx)
+                               ? (int)((unsigned)my_e0 | ((unsigned)off << kWinBits))
+                               : 0;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -292,8 +325,12 @@ constexpr int kTapGroup = 4;
 // indices, otherwise from global memory.  A tap whose quotient lies within
 // a few ulp of a rounding boundary has its index redone with the IEEE
 // division; the group branches only when some tap needs it.
+__device__ __forceinline__ float pair_lane(const float2 *v, int k) {
+    return (k & 1) ? v[k >> 1].y : v[k >> 1].x;
+}
+
 template <int KIND, typename T, bool STAGED, int N>
-__device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt, const float *at,
+__device__ __forceinline__ float staged_group(const DasArgs &a, const float2 *tt2, const float2 *at2,
                                               float trx, float arx, const int *bk,
                                               const typename StagedElem<KIND, T>::E *stage,
                                               long long ch_first, long long chs, int g, int ntx,
@@ -309,8 +346,10 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt,
 #pragma unroll
     for (int k = 0; k < N; k += 2) {
         if (k + 1 < N) {
-            const float2 x2 = add2_rn(make_float2(tt[k], tt[k + 1]), make_float2(trx, trx));
-            const float2 a2 = mul2_rn(make_float2(at[k], at[k + 1]), make_float2(arx, arx));
+            const float2 x2 = add2_rn(make_float2(pair_lane(tt2, k), pair_lane(tt2, k + 1)),
+                                      make_float2(trx, trx));
+            const float2 a2 = mul2_rn(make_float2(pair_lane(at2, k), pair_lane(at2, k + 1)),
+                                      make_float2(arx, arx));
             const float2 q2 = mul2_rn(add2_rn(x2, make_float2(-a.t0, -a.t0)),
                                          make_float2(a.inv_dt, a.inv_dt));
             px[k] = x2.x;
@@ -320,8 +359,8 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt,
             pq[k] = q2.x;
             pq[k + 1] = q2.y;
         } else {
-            px[k] = __fadd_rn(tt[k], trx);
-            pa[k] = __fmul_rn(at[k], arx);
+            px[k] = __fadd_rn(pair_lane(tt2, k), trx);
+            pa[k] = __fmul_rn(pair_lane(at2, k), arx);
             pq[k] = __fmul_rn(__fsub_rn(px[k], a.t0), a.inv_dt);
         }
     }
@@ -387,31 +426,116 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float *tt,
     return accr;
 }
 
-// Persistent: a grid sized to the GPU takes (frame, tile) items from the
-// plan's queue head (plan[1], zeroed before the launch) in the plan's order,
-// the tiles with most live receives first, so the slowest tiles start first
-// and the last wave is short.  The ring's barriers live across tiles: item
-// number g (counted over all tiles this CTA has run) uses slot g % kStages and
-// phase parity (g / kStages) & 1.  Each tile is computed entirely by one CTA,
-// so the results do not depend on the scheduling.
+// Cubic taps from float32 polynomial records in a stage: N <= kTapGroup
+// transmits of receive (trx, arx), their delays and weights as float32 pairs
+// tt2/at2 (the pair's second lane past N is padding).  The delay sums, weights
+// and quotients are formed two taps per instruction (each lane rounded as the
+// scalar operation).  The knot is floor(q) for the fast quotient q = fl(fl(x -
+// t0) * fl(1/dt)): q - 1/2 is exact for 0 <= q < 2^22, and adding 1.5 * 2^23
+// rounds it to an integer held in the low bits of the sum -- floor(q)
+// wherever q is not an integer -- so the sum's bit pattern minus that of 1.5 *
+// 2^23 is the index itself.  The fraction g = q - floor flags every tap whose
+// q lies within eps_fast of an integer: only there can q and the correctly
+// rounded quotient fl(fl(x - t0) / dt) have different floors, and the group
+// redoes those taps with the IEEE division.  Gathers are issued before that
+// rare branch and redone in it.
+template <int N>
+__device__ __forceinline__ float staged_cubic_group(const DasArgs &a, const float2 *tt2,
+                                                    const float2 *at2, float trx, float arx,
+                                                    const int *sb, const float4 *stage,
+                                                    float accr) {
+    constexpr unsigned cap = kStageBytes / sizeof(float4);
+    constexpr int NP = (N + 1) / 2;
+    const float2 trx2 = make_float2(trx, trx), arx2 = make_float2(arx, arx);
+    const float2 t02 = make_float2(a.t0, a.t0), inv2 = make_float2(a.inv_dt, a.inv_dt);
+    const float2 half2 = make_float2(0.5f, 0.5f), mag2 = make_float2(12582912.f, 12582912.f);
+    float2 x2[NP], ap2[NP], fj2[NP];
+    int e[2 * NP];
+    bool nearb = false;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        x2[p] = add2_rn(tt2[p], trx2);
+        ap2[p] = mul2_rn(at2[p], arx2);
+        const float2 q2 = mul2_rn(sub2_rn(x2[p], t02), inv2);
+        const float2 r2 = add2_rn(sub2_rn(q2, half2), mag2);
+        fj2[p] = sub2_rn(r2, mag2);
+        const float2 g2 = sub2_rn(q2, fj2[p]);
+        e[2 * p] = sb[2 * p] + (__float_as_int(r2.x) - 0x4B400000);
+        e[2 * p + 1] = sb[2 * p + 1] + (__float_as_int(r2.y) - 0x4B400000);
+        nearb |= !(g2.x >= a.eps_fast && g2.x <= 1.f - a.eps_fast);
+        if (2 * p + 1 < N) nearb |= !(g2.y >= a.eps_fast && g2.y <= 1.f - a.eps_fast);
+    }
+    float4 pv[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) pv[k] = stage[min((unsigned)e[k], cap - 1u)];
+    if (nearb) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const float x = (k & 1) ? x2[k >> 1].y : x2[k >> 1].x;
+            const float fl = floorf(__fdiv_rn(__fsub_rn(x, a.t0), a.dt));
+            const int j = (int)fminf(fmaxf(fl, -1.f), (float)a.nt);  // NaN: 0
+            if (k & 1) fj2[k >> 1].y = fl;
+            else fj2[k >> 1].x = fl;
+            pv[k] = stage[min((unsigned)(sb[k] + j), cap - 1u)];
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        // b = (x - xlo) / dt, xlo = fl(t0 + fl(dt j)) as the reference rounds the
+        // knot (two scalar roundings: no product feeds a packed add)
+        const float2 xlo2 = make_float2(__fadd_rn(a.t0, __fmul_rn(a.dt, fj2[p].x)),
+                                        __fadd_rn(a.t0, __fmul_rn(a.dt, fj2[p].y)));
+        const float2 b2 = mul2_rn(sub2_rn(x2[p], xlo2), inv2);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int k = 2 * p + h;
+            if (k < N) {
+                const float b = h ? b2.y : b2.x;
+                const float x = h ? x2[p].y : x2[p].x;
+                const float apod = h ? ap2[p].y : ap2[p].x;
+                const float v = fmaf(fmaf(fmaf(pv[k].w, b, pv[k].z), b, pv[k].y), b, pv[k].x);
+                const bool ok = (x >= a.t0) && (x <= a.xmax) && (fabsf(apod) >= a.thresh);
+                const float c = fmaf(apod, v, accr);
+                accr = ok ? c : accr;
+            }
+        }
+    }
+    return accr;
+}
+
+// Persistent: a grid sized to the GPU takes work items from the plan's queue
+// head (plan[1], zeroed before the launch) in the plan's order, largest first,
+// so the slowest items start first and the last wave is short: (tile, block
+// of receives) items for one frame summed over receives, (frame, tile) items
+// otherwise.  The ring's barriers live across items: ring entry number g
+// (counted over all items this CTA has run) uses slot g % kStages and phase
+// parity (g / kStages) & 1.  Each item is computed entirely by one CTA (and a
+// tile's blocks are added in block order), so the results do not depend on
+// the scheduling.
+//
+// Producers: warp 0 stages an item's first kStages receives; after that the
+// warp whose turn it is (receive it, warp it % 4) refills the slot of receive
+// it - 1 with receive it + 3 once every warp has left that slot.  Each warp
+// keeps the plan words of the next receive it will stage in registers,
+// loaded one turn ahead.
 template <int KIND, int SUM, typename T>
 __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_constant__ DasArgs a,
                                                               int *__restrict__ plan) {
     using E = typename StagedElem<KIND, T>::E;
+    constexpr bool kPolyCubic = KIND == PYCBF_GB_INTERP_CUBIC && CoefRec<T>::kPoly;
     constexpr int kWarps = kBlock / 32;
+    constexpr unsigned kFull = 0xffffffffu;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long full[kStages];
     __shared__ __align__(8) unsigned long long empty[kStages];
     __shared__ __align__(16) int sbase[kStages][kTxReg];  // element base of each window - its e0
     __shared__ int sstaged[kStages];
-    __shared__ float s_txlh[2 * kTxReg];
+    __shared__ int s_copies[kStages];  // the slot's latest phase has bulk copies in flight
     __shared__ int s_failed;
-    __shared__ long long s_produced;  // items (over all tiles) whose copies have been issued
+    __shared__ int s_produced;  // ring entries (over all items) whose copies have been issued
     __shared__ long long s_item;
     __shared__ int s_last;
-    // the tile's plan: live receive indices and their delay bounds
-    int *s_rx = reinterpret_cast<int *>(smem_raw + kStages * kStageBytes);
-    float *s_rxlh = reinterpret_cast<float *>(s_rx + a.nrx);
+    int *s_rx = reinterpret_cast<int *>(smem_raw + kStages * kStageBytes);  // the item's receive codes
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int ntx = a.ntx, nrx = a.nrx;
@@ -419,7 +543,6 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     const PlanLayout L = plan_layout(np, ntx, nrx);
     const long long tiles = L.tiles;
     const long long tile_words = L.tile_words;
-    // one frame summed over receives: (tile, receive block) items; otherwise (frame, tile)
     constexpr bool kBlockSum = SUM == PYCBF_GB_SUM_TX_AND_RX || SUM == PYCBF_GB_SUM_TX_ONLY;
     const bool by_block = kBlockSum && a.nframes == 1;
     const long long nitems = by_block ? (long long)__ldg(plan + 2) : tiles * a.nframes;
@@ -428,12 +551,12 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     int *counters = plan + L.counters;
     float *partials = reinterpret_cast<float *>(plan + L.partials);
     unsigned *queue = reinterpret_cast<unsigned *>(plan + 1);
-    const long long chs = (long long)nrx * a.nt;
     const long long wait_lim = a.wait_cycles > 0 ? a.wait_cycles : (1LL << 31);
 
     if (tid < kStages) {
         mbar_init(&full[tid], 1);
         mbar_init(&empty[tid], kWarps);
+        s_copies[tid] = 0;
     }
     if (tid == 0) {
         s_failed = 0;
@@ -441,15 +564,16 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     }
     mbar_fence_init();
 
-    long long g0 = 0;  // ring items this CTA has run before the current tile
+    int g0 = 0;  // ring entries this CTA has run before the current item
     for (;;) {
         if (tid == 0) s_item = (long long)atomicAdd(queue, 1u);
-        __syncthreads();  // also: every warp is done with the previous tile's ring and plan data
+        __syncthreads();  // also: every warp is done with the previous item's ring and codes
         const long long item = s_item;
         if (item >= nitems || s_failed) break;
         int f = 0, first = 0, bord = 0, nblocks = 1;
         long long tile;
         int nlive;
+        const int *rec;
         if (by_block) {
             const int4 it4 = __ldg(bitems + item);
             tile = it4.x;
@@ -457,85 +581,92 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             nlive = it4.z - it4.y;
             bord = it4.w >> 16;
             nblocks = it4.w & 0xffff;
+            rec = plan + kPlanHeaderWords + tile * tile_words;
         } else {
             f = (int)(item / tiles);
             tile = __ldg(order + (item - (long long)f * tiles));
+            rec = plan + kPlanHeaderWords + tile * tile_words;
+            nlive = __ldg(rec);
         }
         const long long i = tile * kBlock + tid;
         const bool valid = i < np;
-        const int *rec = plan + kPlanHeaderWords + tile * tile_words;
-        if (!by_block) nlive = __ldg(rec);
+        // this item's live receives: plan words of receive k at rx0 + kRxWords k
+        const int *rx0 = rec + 4 + (long long)kRxWords * first;
         const long long frame_ch = (long long)f * ntx * nrx;
         const long long op = valid ? (a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i) : 0;
-        {
-            // this item's live receives: the whole list, or one block of it
-            const float *txlh = reinterpret_cast<const float *>(rec + 1 + 3 * nrx);
-            if (tid < 2 * ntx) s_txlh[tid] = __ldg(txlh + tid);
-            for (int k = tid; k < nlive; k += kBlock) s_rx[k] = __ldg(rec + 1 + first + k);
-            const float *rxlh = reinterpret_cast<const float *>(rec + 1 + nrx) + 2 * first;
-            for (int k = tid; k < 2 * nlive; k += kBlock) s_rxlh[k] = __ldg(rxlh + k);
-        }
+        for (int k = tid; k < nlive; k += kBlock) s_rx[k] = __ldg(rx0 + (long long)kRxWords * k);
         __syncthreads();
 
-        // producer: windows of live receive `it` of this tile into its ring slot
-        auto produce = [&](int it) {
-            const long long gi = g0 + it;
-            const int slot = (int)(gi % kStages);
+        // stage receive `it` of this item into its ring slot with the plan words
+        // wv (this lane's transmit window) and tot (the receive's total elements)
+        auto produce = [&](int it, int wv, int tot) {
+            const int gi = g0 + it;
+            const int slot = gi & (kStages - 1);
             const int code = s_rx[it];
-            bool staged = !(code & 0x40000000);
-            const int r = code & 0x3fffffff;
-            int e0 = 0, e1 = 0;
-            if (staged && lane < ntx) {
-                const float xlo = __fadd_rn(s_txlh[2 * lane], s_rxlh[2 * it]);
-                const float xhi = __fadd_rn(s_txlh[2 * lane + 1], s_rxlh[2 * it + 1]);
-                staged_window<KIND, T>(xlo, xhi, a, e0, e1);
-            }
-            const int cnt = e1 - e0;
-            int off = cnt;
-            for (int o = 1; o < 32; o <<= 1) {
-                const int v = __shfl_up_sync(0xffffffffu, off, o);
-                if (lane >= o) off += v;
-            }
-            const int total = __shfl_sync(0xffffffffu, off, 31);
-            off -= cnt;
-            // the plan sized these windows to fit; a plan from other tables could
-            // not, and then this receive is gathered from global memory instead
-            if ((long long)total * (long long)sizeof(E) > kStageBytes) staged = false;
+            const bool staged = !(code & kUnstaged);
+            const int r = code & (kUnstaged - 1);
+            const int e0 = wv & ((1 << kWinBits) - 1);
+            const int off = (int)((unsigned)wv >> kWinBits);
+            int nxt = __shfl_down_sync(kFull, off, 1);
+            if (lane == ntx - 1) nxt = tot;
+            const int cnt = (staged && lane < ntx) ? nxt - off : 0;
             if (lane < kTxReg) sbase[slot][lane] = (staged && lane < ntx) ? off - e0 : 0;
-            if (lane == 0) sstaged[slot] = staged ? 1 : 0;
-            __syncwarp();
-            // stall test: the tile's first receive announces its bytes (at least 16)
+            // stall test: the item's first receive announces its bytes (at least 16)
             // and issues no copy, so its phase never completes and nothing is in flight
             const bool stall = a.stall_test && it == 0;
-            const unsigned bytes = staged ? (unsigned)(total * sizeof(E)) : 0u;
-            if (lane == 0) mbar_arrive_expect_tx(&full[slot], stall ? max(bytes, 16u) : bytes);
-            __syncwarp();
-            if (staged && lane < ntx && cnt > 0 && !stall) {
-                const E *src = static_cast<const E *>(a.data) + (frame_ch + (long long)lane * nrx + r) * a.nt + e0;
-                E *dst = reinterpret_cast<E *>(smem_raw + (size_t)slot * kStageBytes) + off;
-                tma_bulk_load(dst, src, (unsigned)(cnt * sizeof(E)), &full[slot]);
+            const unsigned bytes = staged ? (unsigned)(tot * (int)sizeof(E)) : 0u;
+            if (lane == 0) {
+                sstaged[slot] = staged ? 1 : 0;
+                s_copies[slot] = (staged && bytes > 0 && !stall) ? 1 : 0;
+                mbar_arrive_expect_tx(&full[slot], stall ? max(bytes, 16u) : bytes);
             }
+            __syncwarp();
+            if (cnt > 0 && !stall) {
+                const E *src = static_cast<const E *>(a.data) +
+                               (frame_ch + (long long)lane * nrx + r) * a.nt + e0;
+                E *dst = reinterpret_cast<E *>(smem_raw + (size_t)slot * kStageBytes) + off;
+                tma_bulk_load(dst, src, (unsigned)(cnt * (int)sizeof(E)), &full[slot]);
+            }
+            if (lane == 0) atomicMax(&s_produced, gi + 1);
         };
-        // warp 0 stages the tile's first kStages receives (their slots were freed
-        // by every warp before the barrier above); after that the producer role
-        // rotates over the warps (a bulk copy costs ~100 cycles to issue, and one
-        // warp issuing every receive's copies starved the others)
+        auto plan_words = [&](int it, int &wv, int &tot) {
+            const int *p = rx0 + (long long)kRxWords * it;
+            wv = (lane < ntx) ? __ldg(p + 4 + lane) : 0;
+            tot = __ldg(p + 1);
+        };
+        // warp 0 stages the item's first kStages receives (their slots were freed
+        // by every warp before the barrier above)
         if (w == 0) {
-            for (int it = 0; it < kStages && it < nlive; ++it) produce(it);
-            if (lane == 0 && nlive > 0) atomicMax(&s_produced, g0 + min(kStages, nlive));
+            int wv[kStages], tot[kStages];
+#pragma unroll
+            for (int it = 0; it < kStages; ++it)
+                if (it < nlive) plan_words(it, wv[it], tot[it]);
+#pragma unroll
+            for (int it = 0; it < kStages; ++it)
+                if (it < nlive) produce(it, wv[it], tot[it]);
         }
+        // this warp's next turn: receive it_w (it_w % 4 == w, it_w >= 1) stages it_w + 3
+        int next_it = (w == 0 ? kWarps : w) + kStages - 1;
+        int nwv = 0, ntot = 0;
+        if (next_it < nlive) plan_words(next_it, nwv, ntot);
 
-        // transmit side of this pixel; slots past ntx carry zero weights
-        float rtau[kTxReg], rapod[kTxReg];
+        // transmit side of this pixel as float32 pairs; slots past ntx carry zero weights
+        float2 tt2[kTxReg / 2], at2[kTxReg / 2];
         float amax = 0.f;
 #pragma unroll
         for (int k = 0; k < kTxReg; ++k) {
-            rtau[k] = a.t0;
-            rapod[k] = 0.f;
+            float tv = a.t0, av = 0.f;
             if (k < ntx && valid) {
-                rtau[k] = __ldg(a.tautx + (long long)k * np + i);
-                rapod[k] = __ldg(a.apodtx + (long long)k * np + i);
-                amax = fmaxf(amax, fabsf(rapod[k]));
+                tv = __ldg(a.tautx + (long long)k * np + i);
+                av = __ldg(a.apodtx + (long long)k * np + i);
+                amax = fmaxf(amax, fabsf(av));
+            }
+            if (k & 1) {
+                tt2[k >> 1].y = tv;
+                at2[k >> 1].y = av;
+            } else {
+                tt2[k >> 1].x = tv;
+                at2[k >> 1].x = av;
             }
         }
 
@@ -544,28 +675,31 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         int cur_block = -1;
         bool failed = false;
         // receive-side values, fetched two receives ahead
+        const float *trp = a.taurx + i, *arp = a.apodrx + i;
         auto rx_load = [&](int it, float &trx, float &arx) {
-            const int r = s_rx[it] & 0x3fffffff;
-            trx = valid ? __ldg(a.taurx + (long long)r * np + i) : 0.f;
-            arx = valid ? __ldg(a.apodrx + (long long)r * np + i) : 0.f;
+            const long long ro = (long long)(s_rx[it] & (kUnstaged - 1)) * np;
+            trx = valid ? __ldg(trp + ro) : 0.f;
+            arx = valid ? __ldg(arp + ro) : 0.f;
         };
         float trx1 = 0.f, arx1 = 0.f, trx2 = 0.f, arx2 = 0.f;
         if (nlive > 0) rx_load(0, trx1, arx1);
         if (nlive > 1) rx_load(1, trx2, arx2);
 
         for (int it = 0; it < nlive; ++it) {
-            const long long gi = g0 + it;
-            const int slot = (int)(gi % kStages);
-            const int r = s_rx[it] & 0x3fffffff;
+            const int gi = g0 + it;
+            const int slot = gi & (kStages - 1);
+            const int r = s_rx[it] & (kUnstaged - 1);
             const float trx = trx1, arx = arx1;
             trx1 = trx2;
             arx1 = arx2;
             if (it + 2 < nlive) rx_load(it + 2, trx2, arx2);
-            if (!mbar_wait_bounded(&full[slot], (unsigned)(gi / kStages) & 1u, wait_lim)) failed = true;
-            if (failed || *(volatile int *)&s_failed) {
-                failed = true;
-                s_failed = 1;
-                break;
+            if (!mbar_try_wait(&full[slot], (unsigned)(gi >> 2) & 1u)) {
+                if (*(volatile int *)&s_failed ||
+                    !mbar_wait_bounded(&full[slot], (unsigned)(gi >> 2) & 1u, wait_lim)) {
+                    failed = true;
+                    s_failed = 1;
+                    break;
+                }
             }
 
             if (SUM == PYCBF_GB_SUM_TX_AND_RX && r / kRxBlock != cur_block) {
@@ -576,33 +710,52 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh);
             float accr = 0.f;
             if (live) {
-                const long long ch_first = (frame_ch + r) * a.nt;
                 if (sstaged[slot]) {
                     const E *stage = reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes);
+                    int sb[kTxReg];
+#pragma unroll
+                    for (int g = 0; g < kTxReg; g += 4) {
+                        const int4 b = *reinterpret_cast<const int4 *>(&sbase[slot][g]);
+                        sb[g] = b.x;
+                        sb[g + 1] = b.y;
+                        sb[g + 2] = b.z;
+                        sb[g + 3] = b.w;
+                    }
 #pragma unroll
                     for (int g = 0; g < kTxReg; g += kTapGroup) {
                         if (g < ntx) {
-                            const int4 b = *reinterpret_cast<const int4 *>(&sbase[slot][g]);
-                            const int bk[kTapGroup] = {b.x, b.y, b.z, b.w};
                             // the last group holds only the transmits left (no padded tap)
                             const int rem = ntx - g;
-#define PGB_GROUP(n)                                                                            \
-    staged_group<KIND, T, true, n>(a, rtau + g, rapod + g, trx, arx, bk, stage, ch_first, chs, g, \
-                                   ntx, accr)
-                            if (rem >= 4) accr = PGB_GROUP(4);
-                            else if (rem == 3) accr = PGB_GROUP(3);
-                            else if (rem == 2) accr = PGB_GROUP(2);
-                            else accr = PGB_GROUP(1);
+                            if constexpr (kPolyCubic) {
+                                const float4 *st4 = reinterpret_cast<const float4 *>(stage);
+#define PGB_CGROUP(n) staged_cubic_group<n>(a, tt2 + g / 2, at2 + g / 2, trx, arx, sb + g, st4, accr)
+                                if (rem >= 4) accr = PGB_CGROUP(4);
+                                else if (rem == 3) accr = PGB_CGROUP(3);
+                                else if (rem == 2) accr = PGB_CGROUP(2);
+                                else accr = PGB_CGROUP(1);
+#undef PGB_CGROUP
+                            } else {
+#define PGB_GROUP(n)                                                                              \
+    staged_group<KIND, T, true, n>(a, tt2 + g / 2, at2 + g / 2, trx, arx, sb + g, stage, 0, 0, g, ntx, \
+                                   accr)
+                                if (rem >= 4) accr = PGB_GROUP(4);
+                                else if (rem == 3) accr = PGB_GROUP(3);
+                                else if (rem == 2) accr = PGB_GROUP(2);
+                                else accr = PGB_GROUP(1);
 #undef PGB_GROUP
+                            }
                         }
                     }
                 } else {
+                    const long long ch_first = (frame_ch + r) * a.nt;
+                    const long long chs = (long long)nrx * a.nt;
 #pragma unroll
                     for (int g = 0; g < kTxReg; g += kTapGroup) {
                         if (g < ntx) {
                             const int bk[kTapGroup] = {0, 0, 0, 0};
-                            accr = staged_group<KIND, T, false, kTapGroup>(a, rtau + g, rapod + g, trx, arx, bk,
-                                                                nullptr, ch_first, chs, g, ntx, accr);
+                            accr = staged_group<KIND, T, false, kTapGroup>(a, tt2 + g / 2, at2 + g / 2, trx,
+                                                                arx, bk, nullptr, ch_first, chs, g,
+                                                                ntx, accr);
                         }
                     }
                 }
@@ -617,17 +770,17 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             // this warp is done with the slot
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[slot]);
-            // warp it % kWarps refills the slot of the previous receive once every
-            // warp left it
-            if (w == it % kWarps && it >= 1 && it - 1 + kStages < nlive) {
-                const long long pg = gi - 1;
-                if (!mbar_wait_bounded(&empty[pg % kStages], (unsigned)(pg / kStages) & 1u, wait_lim)) {
+            // this warp's turn: refill the slot of the previous receive once every warp left it
+            if (it + kStages - 1 == next_it && next_it < nlive) {
+                const int pg = gi - 1;
+                if (!mbar_wait_bounded(&empty[pg & (kStages - 1)], (unsigned)(pg >> 2) & 1u, wait_lim)) {
                     failed = true;
                     s_failed = 1;
                     break;
                 }
-                produce(it - 1 + kStages);
-                if (lane == 0) atomicMax(&s_produced, pg + kStages + 1);
+                produce(next_it, nwv, ntot);
+                next_it += kWarps;
+                if (next_it < nlive) plan_words(next_it, nwv, ntot);
             }
         }
         __syncthreads();
@@ -667,17 +820,21 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     }
     __syncthreads();
     if (s_failed && tid == 0) {
-        // drain the copies still in flight before the CTA's shared memory goes
-        // away: the latest phase of each slot is one of the last kStages issued
+        // drain the bulk copies still in flight before the CTA's shared memory
+        // goes away: the latest phase of each slot is one of the last kStages
+        // entries issued; a phase with copies lands in microseconds, so it gets
+        // the full (~1 s) bound, and a phase without copies (the stall test's) is
+        // not waited for
         atomicExch(plan, 1);
-        const long long produced = *(volatile long long *)&s_produced;
-        for (long long j = max(0LL, produced - kStages); j < produced; ++j)
-            (void)mbar_wait_bounded(&full[j % kStages], (unsigned)(j / kStages) & 1u, wait_lim);
+        const int produced = *(volatile int *)&s_produced;
+        for (int j = max(0, produced - kStages); j < produced; ++j)
+            if (s_copies[j & (kStages - 1)])
+                (void)mbar_wait_bounded(&full[j & (kStages - 1)], (unsigned)(j >> 2) & 1u);
     }
 }
 
 inline size_t staged_smem_bytes(int nrx) {
-    return (size_t)kStages * kStageBytes + sizeof(int) * 3 * (size_t)nrx;
+    return (size_t)kStages * kStageBytes + sizeof(int) * (size_t)nrx;
 }
 
 // The order the persistent kernel takes the tiles in: most live receives
@@ -686,7 +843,7 @@ inline size_t staged_smem_bytes(int nrx) {
 static __global__ void __launch_bounds__(1024) plan_order_kernel(int *plan, long long tiles, int ntx,
                                                           int nrx) {
     extern __shared__ int bins[];  // nrx + 1 bins, nlive = nrx first
-    const long long tw = plan_tile_words(ntx, nrx);
+    const long long tw = plan_tile_words(nrx);
     const PlanLayout L = plan_layout(tiles * kBlock, ntx, nrx);
     int *order = plan + L.order;
     for (int b = threadIdx.x; b <= nrx; b += blockDim.x) bins[b] = 0;
@@ -723,12 +880,14 @@ static __global__ void __launch_bounds__(1024) plan_order_kernel(int *plan, long
             f(0, 0, 0, 1);
             return;
         }
+        // the block of live receive k
+        auto blk = [&](int k) { return (rec[4 + kRxWords * k] & (kUnstaged - 1)) / kRxBlock; };
         int nb = 0;
         for (int k = 0; k < nlive; ++k)
-            if (k == 0 || ((rec[1 + k] & 0x3fffffff) / kRxBlock) != ((rec[k] & 0x3fffffff) / kRxBlock)) ++nb;
+            if (k == 0 || blk(k) != blk(k - 1)) ++nb;
         int first = 0, ord = 0;
         for (int k = 1; k <= nlive; ++k) {
-            if (k == nlive || ((rec[1 + k] & 0x3fffffff) / kRxBlock) != ((rec[k] & 0x3fffffff) / kRxBlock)) {
+            if (k == nlive || blk(k) != blk(k - 1)) {
                 f(first, k, ord++, nb);
                 first = k;
             }
@@ -757,7 +916,13 @@ static __global__ void __launch_bounds__(1024) plan_order_kernel(int *plan, long
 template <int KIND, typename T>
 cudaError_t launch_plan_one(const DasArgs &a, int *plan, cudaStream_t s) {
     const long long tiles = (a.np + kBlock - 1) / kBlock;
-    tabbed_plan_kernel<KIND, T><<<(unsigned)tiles, kBlock, 0, s>>>(a, plan);
+    const size_t psmem = sizeof(int) * (size_t)a.nrx;
+    if (psmem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(tabbed_plan_kernel<KIND, T>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem);
+        if (e != cudaSuccess) return e;
+    }
+    tabbed_plan_kernel<KIND, T><<<(unsigned)tiles, kBlock, psmem, s>>>(a, plan);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     const size_t smem = sizeof(int) * ((size_t)max(a.nrx, kRxBlock) + 1);

@@ -11,9 +11,10 @@
 // owns a contiguous chunk of the channel (of odd length, so that the lanes'
 // sequential sweeps fall in distinct shared-memory banks; 33 samples at nt =
 // 2048, so each lane's serial chain is 49 steps); the channel, u and y2 sit in
-// shared memory.  Output per sample j: (y_j, y_j+1, z_j, z_j+1), z = y2 dx^2 / 6,
-// with y_nt = z_nt = 0, so the forward kernel does one 16-byte (or 8-byte)
-// load per tap.
+// shared memory.  Output per sample j: one record of interval j (CoefRec: the
+// interval's cubic as a polynomial in the fraction for float32 records,
+// (y_j, y_j+1, z_j, z_j+1) for 16-bit ones), z = y2 dx^2 / 6, with y_nt =
+// z_nt = 0, so the forward kernel does one 16-byte (or 8-byte) load per tap.
 #include <algorithm>
 
 #include "common.cuh"
@@ -51,8 +52,8 @@ __device__ __forceinline__ void lanes_sync(int bar) {
 template <typename T, int LANES = 32>
 __device__ __forceinline__ void spline_channel(const T *__restrict__ src,
                                                typename CoefRec<T>::raw *__restrict__ dst, int nt,
-                                               float dt, const SplineTable &tab, float *smem,
-                                               int bar = 0) {
+                                               float t0, float dt, const SplineTable &tab,
+                                               float *smem, int bar = 0) {
     const int lane = threadIdx.x & (LANES - 1);
     const int stride = (nt + 4) & ~3;  // >= nt+1, keeps every array 16-byte aligned
     float *y = smem;
@@ -119,21 +120,23 @@ __device__ __forceinline__ void spline_channel(const T *__restrict__ src,
             yn = y2k;
         }
     lanes_sync<LANES>(bar);
-    for (int k = lane; k < nt; k += LANES) dst[k] = CoefRec<T>::pack(y[k], y[k + 1], uz[k], uz[k + 1]);
+    for (int k = lane; k < nt; k += LANES)
+        dst[k] = CoefRec<T>::make(y[k], y[k + 1], uz[k], uz[k + 1], k, t0, dt);
 }
 
 // one channel per pair of warps (named barrier 1 + pair index)
 template <typename T>
 __global__ void __launch_bounds__(256)
 spline_coef_kernel(const T *__restrict__ rf, typename CoefRec<T>::raw *__restrict__ coef,
-                   long long nch, int nt, float dt, const __grid_constant__ SplineTable tab) {
+                   long long nch, int nt, float t0, float dt,
+                   const __grid_constant__ SplineTable tab) {
     extern __shared__ float smem[];
     const int pr = threadIdx.x >> 6;
     const int ppb = blockDim.x >> 6;
     const long long ch = (long long)blockIdx.x * ppb + pr;
     if (ch >= nch) return;  // both warps of a pair leave together
     const int stride = (nt + 4) & ~3;
-    spline_channel<T, 64>(rf + ch * (long long)nt, coef + ch * (long long)nt, nt, dt, tab,
+    spline_channel<T, 64>(rf + ch * (long long)nt, coef + ch * (long long)nt, nt, t0, dt, tab,
                           smem + (size_t)pr * 2 * stride, 1 + pr);
 }
 
@@ -147,7 +150,7 @@ __device__ __forceinline__ void batch_spline_one(const BatchJob &j, long long ch
     const int nt = j.a.nt;
     spline_channel<T, 64>(static_cast<const T *>(j.rf) + ch * (long long)nt,
                           static_cast<raw *>(const_cast<void *>(j.a.data)) + ch * (long long)nt, nt,
-                          j.a.dt, tab, sm, bar);
+                          j.a.t0, j.a.dt, tab, sm, bar);
 }
 
 __global__ void __launch_bounds__(256)
@@ -193,7 +196,7 @@ static cudaError_t launch_spline_t(const SplineArgs &a, cudaStream_t s) {
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
     spline_coef_kernel<T><<<(unsigned)blocks, 64 * ppb, smem, s>>>(
         static_cast<const T *>(a.rf), static_cast<typename CoefRec<T>::raw *>(a.coef), a.nch, a.nt,
-        a.dt, tab);
+        a.t0, a.dt, tab);
     return cudaGetLastError();
 }
 

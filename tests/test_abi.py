@@ -122,9 +122,10 @@ def test_plan_validation():
     L = _lib.load()
     info = _info()
     p = ct.c_void_p(16)
-    # header, 8 tile records, tile order, block counters, (pad to 16 bytes), 8 x 2 block
-    # items (int4; receive blocks of 64), 8 x 2 x 128 partial sums
-    head = 4 + 8 * (1 + 128 * 3 + 22) + 8 + 8
+    # header, 8 tile records (4 words + 16 per receive), tile order, block counters,
+    # (pad to 16 bytes), 8 x 2 block items (int4; receive blocks of 64), 8 x 2 x 128
+    # partial sums
+    head = 4 + 8 * (4 + 128 * 16) + 8 + 8
     head = (head + 3) // 4 * 4
     assert L.pycbf_gb_tabbed_plan_bytes(1000, 11, 128) == 4 * (head + 4 * 8 * 2 + 8 * 2 * 128)
     assert L.pycbf_gb_tabbed_plan_bytes(0, 11, 128) == 0
