@@ -411,6 +411,19 @@ int pycbf_gb_das_tabbed_adjoint(const pycbf_gb_rfinfo *rf, const void *coef,
                                 float thresh, int sumtype, const float *grad_out,
                                 float *grad_rf, float *grad_tautx, float *grad_taurx,
                                 void *workspace, size_t workspace_bytes, void *stream);
+/* The same with the forward's staging plan (pycbf_gb_tabbed_plan of these   */
+/* tables, or NULL): where the plan's staged path applies (cubic, float32   */
+/* channel data, one frame, ntx <= 12), the delay gradients gather the      */
+/* records from its staged windows.  The plan's queue head is reused, so it */
+/* must not be in use by another call at the same time.  No counterpart in  */
+/* the reference, whose beamformers are forward-only.                       */
+int pycbf_gb_das_tabbed_adjoint_planned(const pycbf_gb_rfinfo *rf, const void *coef,
+                                        const float *tautx, const float *apodtx,
+                                        const float *taurx, const float *apodrx, long long np,
+                                        const int *pixel_index, float thresh, int sumtype,
+                                        const void *plan, const float *grad_out, float *grad_rf,
+                                        float *grad_tautx, float *grad_taurx, void *workspace,
+                                        size_t workspace_bytes, void *stream);
 int pycbf_gb_das_synthetic_adjoint(const pycbf_gb_rfinfo *rf, const void *coef,
                                    const pycbf_gb_synthetic *geo, const float *slowness,
                                    const int *pixel_index, int sumtype, const float *grad_out,

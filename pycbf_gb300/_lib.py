@@ -30,6 +30,7 @@ EXPORTS = (
     "pycbf_gb_synthetic_rx_mask", "pycbf_gb_dmas", "pycbf_gb_slsc", "pycbf_gb_fp32_probe",
     "pycbf_gb_das_tabbed_cubic_noalloc", "pycbf_gb_das_synthetic_slowness",
     "pycbf_gb_adjoint_workspace_bytes", "pycbf_gb_das_tabbed_adjoint",
+    "pycbf_gb_das_tabbed_adjoint_planned",
     "pycbf_gb_das_synthetic_adjoint", "pycbf_gb_batch_plan_bytes", "pycbf_gb_batch_plan",
     "pycbf_gb_batch_run", "pycbf_gb_upsampled_bytes", "pycbf_gb_upsample",
     "pycbf_gb_poly_workspace_bytes", "pycbf_gb_poly_coefficients", "pycbf_gb_das_tabbed_poly",
@@ -119,6 +120,8 @@ def load() -> ct.CDLL:
         L.pycbf_gb_adjoint_workspace_bytes.restype = sz
         L.pycbf_gb_das_tabbed_adjoint.argtypes = [P(RFInfo), vp, vp, vp, vp, vp, ll, vp, f, i, vp,
                                                   vp, vp, vp, vp, sz, vp]
+        L.pycbf_gb_das_tabbed_adjoint_planned.argtypes = [P(RFInfo), vp, vp, vp, vp, vp, ll, vp, f,
+                                                          i, vp, vp, vp, vp, vp, vp, sz, vp]
         L.pycbf_gb_das_synthetic_adjoint.argtypes = [P(RFInfo), vp, P(SyntheticGeom), vp, vp, i,
                                                      vp, vp, vp, vp, sz, vp]
         L.pycbf_gb_batch_plan_bytes.argtypes = [P(BatchJob), i, i]

@@ -101,6 +101,7 @@ class _TabbedDAS(torch.autograd.Function):
             _stream())
         _lib.check(st, "pycbf_gb_das_tabbed_prefiltered")
         ctx.save_for_backward(coef, tautx, taurx, apodtx, apodrx)
+        ctx.plan = plan
         ctx.pixel_index = pixel_index
         ctx.spec = spec
         ctx.rf_meta = (tuple(rf4.shape), rf4.dtype)
@@ -126,11 +127,12 @@ class _TabbedDAS(torch.autograd.Function):
             nws = L.pycbf_gb_adjoint_workspace_bytes(ct.byref(info), np_)
             ws = torch.empty(nws, dtype=torch.uint8, device=dev)
         if need_rf or need_ttx or need_trx:
-            st = L.pycbf_gb_das_tabbed_adjoint(
+            st = L.pycbf_gb_das_tabbed_adjoint_planned(
                 ct.byref(info), _ptr(coef), _ptr(tautx), _ptr(apodtx), _ptr(taurx), _ptr(apodrx),
                 np_, _ptr(ctx.pixel_index), float(np.float32(spec.thresh)), spec.sumtype,
-                _ptr(gout), _ptr(g_rf), _ptr(g_ttx), _ptr(g_trx), _ptr(ws), nws, _stream())
-            _lib.check(st, "pycbf_gb_das_tabbed_adjoint")
+                _ptr(ctx.plan), _ptr(gout), _ptr(g_rf), _ptr(g_ttx), _ptr(g_trx), _ptr(ws), nws,
+                _stream())
+            _lib.check(st, "pycbf_gb_das_tabbed_adjoint_planned")
         if g_rf is not None and dtype != torch.float32:
             g_rf = g_rf.to(dtype)
         return g_rf, g_ttx, g_trx, None, None, None, None, None
@@ -206,7 +208,8 @@ def das_tabbed(rf: torch.Tensor, tautx: torch.Tensor, taurx: torch.Tensor, apodt
     (np,) / (nframes, np) for 'tx_and_rx', (nrx, np) / (nframes, nrx, np) for
     'tx_only'.  Values equal TabbedBeamformer(interp cubic) on the same inputs.
     plan: a staging plan built for exactly these tables and thresh
-    (pycbf_gb_tabbed_plan): the forward then runs the staged kernel.
+    (pycbf_gb_tabbed_plan): the forward then runs the staged kernel, and so
+    do the delay gradients for one frame of float32 channel data.
     """
     _check_rf(rf)
     rf4, squeeze = _as4(rf)

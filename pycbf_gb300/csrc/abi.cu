@@ -557,6 +557,44 @@ int pycbf_gb_das_tabbed_adjoint(const pycbf_gb_rfinfo *rf, const void *coef,
     return run_adjoint(rf, g, workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
 }
 
+int pycbf_gb_das_tabbed_adjoint_planned(const pycbf_gb_rfinfo *rf, const void *coef,
+                                        const float *tautx, const float *apodtx,
+                                        const float *taurx, const float *apodrx, long long np,
+                                        const int *pixel_index, float thresh, int sumtype,
+                                        const void *plan, const float *grad_out, float *grad_rf,
+                                        float *grad_tautx, float *grad_taurx, void *workspace,
+                                        size_t workspace_bytes, void *stream) {
+    int st = check_adjoint_common(rf, coef, sumtype, false);
+    if (st) return st;
+    if (!tautx || !apodtx || !taurx || !apodrx || !grad_out || std::isnan(thresh))
+        return PYCBF_GB_EINVAL;
+    if (plan && reinterpret_cast<uintptr_t>(plan) % 16) return PYCBF_GB_EINVAL;
+    if (np <= 0 || np >= (1LL << 31)) return np == 0 ? PYCBF_GB_OK : PYCBF_GB_ERANGE;
+    AdjArgs g = {};
+    fill_time_axis(g.d, rf);
+    g.d.data = coef;
+    g.d.tautx = tautx;
+    g.d.apodtx = apodtx;
+    g.d.taurx = taurx;
+    g.d.apodrx = apodrx;
+    g.d.pixel_index = pixel_index;
+    g.d.np = np;
+    g.d.thresh = thresh;
+    g.geom = GEOM_TABBED;
+    g.sumtype = sumtype;
+    g.gout = grad_out;
+    g.grad_rf = grad_rf;
+    g.grad_tautx = grad_tautx;
+    g.grad_taurx = grad_taurx;
+    // the staged delay gradients need the plan's staged path for cubic
+    // float32 records and one frame; otherwise the plan is not used
+    if (plan && rf->nframes == 1 && rf->dtype == PYCBF_GB_F32 &&
+        staged_ok(rf, PYCBF_GB_INTERP_CUBIC, sumtype, coef))
+        g.plan = static_cast<const int *>(plan);
+    return run_adjoint(rf, g, workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
+}
+
+
 int pycbf_gb_das_synthetic_adjoint(const pycbf_gb_rfinfo *rf, const void *coef,
                                    const pycbf_gb_synthetic *geo, const float *slowness,
                                    const int *pixel_index, int sumtype, const float *grad_out,

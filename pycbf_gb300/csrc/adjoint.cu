@@ -13,13 +13,14 @@
 //                       Tabbed tables, or into dL/ds (np) for the Synthetic
 //                       slowness form (x = (D_tx + D_rx) s + t0).
 //   adj_scatter_kernel  one CTA per (channel, part of the pixel range): the
-//                       transpose of the interpolation.  Each warp owns two
-//                       shared-memory rows (dL/dy, dL/dz) of the channel; the
-//                       taps of one warp step are grouped by knot with
+//                       transpose of the interpolation into two shared-memory
+//                       rows (dL/dy, dL/dz) of the channel, one pair per CTA.
+//                       The taps of one warp step are grouped by knot with
 //                       match.any and each group's weights are summed in lane
 //                       order by its lowest lane, which alone updates the rows
-//                       (so no two lanes ever touch one word together).  The
-//                       warp rows are added in warp order into the part's row.
+//                       (so no two lanes ever touch one word together); the
+//                       warps take turns, in warp order between CTA barriers,
+//                       so no two warps do either.
 //   adj_finalize_kernel one warp per channel: adds the parts in order, then
 //                       the adjoint of the prefilter, dL/drf = dL/dy +
 //                       1/2 D^T T^-1 dL/dz (T is symmetric: the same chunked
@@ -228,7 +229,7 @@ template <int GEOM, int SUM>
 __global__ void __launch_bounds__(128) adj_scatter_kernel(const __grid_constant__ AdjArgs g,
                                                           long long part_len, int Lp) {
     const DasArgs &a = g.d;
-    extern __shared__ float rows[];  // [warp][2][Lp]: dL/dy, dL/dz
+    extern __shared__ float rows[];  // [2][Lp]: dL/dy, dL/dz
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const long long np = a.np;
     const int ntx = a.ntx, nrx = a.nrx;
@@ -238,10 +239,10 @@ __global__ void __launch_bounds__(128) adj_scatter_kernel(const __grid_constant_
     const int r = (int)(c % nrx);
     const int t = (int)((c / nrx) % ntx);
     const int f = (int)(c / ((long long)nrx * ntx));
-    float *ry = rows + (size_t)w * 2 * Lp;
+    float *ry = rows;
     float *rz = ry + Lp;
-    for (int n = lane; n < 2 * Lp; n += 32) ry[n] = 0.f;
-    __syncwarp();
+    for (int n = threadIdx.x; n < 2 * Lp; n += blockDim.x) ry[n] = 0.f;
+    __syncthreads();
 
     const long long i0 = (long long)q * part_len;
     const long long i1 = min(np, i0 + part_len);
@@ -338,9 +339,9 @@ __global__ void __launch_bounds__(128) adj_scatter_kernel(const __grid_constant_
         }
         __syncwarp();
     };
-    // live steps two at a time (their taps computed together, their rows
-    // updated in step order: the sums of one step at a time), the next two
-    // fetched meanwhile
+    // live steps two at a time (their taps computed together; each warp adds
+    // its two steps' taps in its turn, warps in order), the next two fetched
+    // meanwhile
     In c0 = {{0.f, 0.f, 0.f, 0.f}, 0.f}, c1 = c0, n0 = c0, n1 = c0;
     long long b0 = next_live(i0);
     long long b1 = b0 < i1 ? next_live(b0 + blockDim.x) : i1;
@@ -353,8 +354,13 @@ __global__ void __launch_bounds__(128) adj_scatter_kernel(const __grid_constant_
         if (nb1 < i1) fetch(nb1 + threadIdx.x, n1);
         const Tap t0 = tap_of(b0, c0);
         const Tap t1 = tap_of(b1, c1);
-        scatter(t0);
-        scatter(t1);
+        for (int turn = 0; turn < nw; ++turn) {  // b0 is the same in every thread
+            if (w == turn) {
+                scatter(t0);
+                scatter(t1);
+            }
+            __syncthreads();
+        }
         b0 = nb0;
         b1 = nb1;
         c0 = n0;
@@ -362,33 +368,13 @@ __global__ void __launch_bounds__(128) adj_scatter_kernel(const __grid_constant_
     }
     __syncthreads();
     float *dst = g.partial + ((size_t)q * nch + c) * 2 * Lp;
-    for (int m = threadIdx.x; m < 2 * Lp; m += blockDim.x) {
-        float s = rows[m];
-        for (int k = 1; k < nw; ++k) s += rows[(size_t)k * 2 * Lp + m];
-        dst[m] = s;
-    }
+    for (int m = threadIdx.x; m < 2 * Lp; m += blockDim.x) dst[m] = rows[m];
 }
 
-// ---------------------------------------------------------------------------
-// adjoint of the prefilter, one warp per channel
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256)
-adj_finalize_kernel(const float *__restrict__ partial, int nparts, long long nch, int nt, int Lp,
-                    float *__restrict__ grad_rf, const __grid_constant__ SplineTable tab) {
-    extern __shared__ float smem[];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-    const long long ch = (long long)blockIdx.x * wpb + w;
-    if (ch >= nch) return;
-    const int stride = (nt + 4) & ~3;
-    float *zv = smem + (size_t)w * 2 * stride;  // dL/dz, then v = T^-1 dL/dz in place
-    float *u = zv + stride;
-    const float *p0 = partial + (size_t)ch * 2 * Lp;
-    const size_t pstride = (size_t)nch * 2 * Lp;  // between parts
-    for (int n = lane; n < nt; n += 32) {
-        float sz = 0.f;
-        for (int q = 0; q < nparts; ++q) sz += p0[q * pstride + Lp + n];
-        zv[n] = sz;
-    }
+// v = T^-1 dL/dz in place of zv (one warp; u: scratch of nt floats), with v_0 =
+// v_nt-1 = 0: the chunked recurrences of the forward prefilter (T symmetric)
+__device__ __forceinline__ void prefilter_adjoint_warp(float *zv, float *u, int nt,
+                                                       const SplineTable &tab, int lane) {
     if (lane == 0) u[0] = 0.f;
     __syncwarp();
     // T v = dL/dz on the interior samples 1..nt-2 (v_0 = v_nt-1 = 0)
@@ -424,6 +410,29 @@ adj_finalize_kernel(const float *__restrict__ partial, int nparts, long long nch
         zv[nt - 1] = 0.f;
     }
     __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// adjoint of the prefilter, one warp per channel
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+adj_finalize_kernel(const float *__restrict__ partial, int nparts, long long nch, int nt, int Lp,
+                    float *__restrict__ grad_rf, const __grid_constant__ SplineTable tab) {
+    extern __shared__ float smem[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const long long ch = (long long)blockIdx.x * wpb + w;
+    if (ch >= nch) return;
+    const int stride = (nt + 4) & ~3;
+    float *zv = smem + (size_t)w * 2 * stride;  // dL/dz, then v = T^-1 dL/dz in place
+    float *u = zv + stride;
+    const float *p0 = partial + (size_t)ch * 2 * Lp;
+    const size_t pstride = (size_t)nch * 2 * Lp;  // between parts
+    for (int n = lane; n < nt; n += 32) {
+        float sz = 0.f;
+        for (int q = 0; q < nparts; ++q) sz += p0[q * pstride + Lp + n];
+        zv[n] = sz;
+    }
+    prefilter_adjoint_warp(zv, u, nt, tab, lane);
     float *dst = grad_rf + ch * (long long)nt;
     for (int n = lane; n < nt; n += 32) {
         float sy = 0.f;
@@ -433,6 +442,7 @@ adj_finalize_kernel(const float *__restrict__ partial, int nparts, long long nch
         dst[n] = fmaf(0.5f, vm - 2.f * zv[n] + vp, sy);
     }
 }
+
 
 size_t delay_smem_bytes(int ntx) { return 3 * (size_t)ntx * kBlock * sizeof(float); }
 
@@ -464,7 +474,7 @@ cudaError_t launch_scatter_one(const AdjArgs &g, cudaStream_t s) {
     adj_live_kernel<GEOM><<<(unsigned)tiles, kBlock, 0, s>>>(g);
     cudaError_t lerr = cudaGetLastError();
     if (lerr != cudaSuccess) return lerr;
-    const size_t smem = (size_t)nw * 2 * Lp * sizeof(float);
+    const size_t smem = (size_t)2 * Lp * sizeof(float);
     auto kern = adj_scatter_kernel<GEOM, SUM>;
     cudaError_t err =
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -493,7 +503,17 @@ cudaError_t launch_scatter_one(const AdjArgs &g, cudaStream_t s) {
 template <int GEOM, int SUM, typename T>
 cudaError_t launch_adjoint_gs(const AdjArgs &g, cudaStream_t s) {
     if (g.grad_tautx || g.grad_taurx || g.grad_slow) {
-        cudaError_t err = launch_delay_one<GEOM, SUM, T>(g, s);
+        cudaError_t err;
+        if (GEOM == GEOM_TABBED && g.plan && CoefRec<T>::kPoly) {
+            // the forward's staging plan: the delay gradients gather from staged windows
+            DasArgs d = g.d;
+            d.gk = g.gk;
+            d.gtx = g.grad_tautx;
+            d.grx = g.grad_taurx;
+            err = launch_das_staged_adj(d, SUM, PYCBF_GB_F32, g.plan, s);
+        } else {
+            err = launch_delay_one<GEOM, SUM, T>(g, s);
+        }
         if (err != cudaSuccess) return err;
     }
     if (g.grad_rf) return launch_scatter_one<GEOM, SUM>(g, s);
@@ -532,9 +552,7 @@ int adjoint_parts(long long nch, long long np) {
 
 int adjoint_rows_warps(int nt) {
     const size_t row = 2 * (size_t)((nt + 1 + 3) & ~3) * sizeof(float);
-    for (int nw = 4; nw >= 1; nw >>= 1)
-        if (nw * row <= kRowSmemMax) return nw;
-    return 0;
+    return row <= kRowSmemMax ? 4 : 0;
 }
 
 size_t adjoint_grad_bytes(long long nframes, long long nrx, long long np) {

@@ -135,8 +135,160 @@ __global__ void slsc_kernel(const float *__restrict__ im, const unsigned char *_
     out[f * npix + pix] = res;
 }
 
+// ---------------------------------------------------------------------------
+// SLSC with register-blocked lag accumulators (nlag <= 16, nkern <= 3, nrx <=
+// 256): one thread per pixel (ix, iz), consecutive threads consecutive iz.
+// The thread first marks, in a bit set, the elements whose receive mask is on
+// over its whole axial kernel (the kept elements, in element order).  It then
+// walks the kept elements in chunks of 16 with the loop unrolled, so that the
+// normalised kernels of the previous 16 kept elements sit in a register ring
+// with static slots: each kept element's kernel (mean-subtracted, divided by
+// its population deviation; a zero vector when that deviation is below 1e-10)
+// is correlated with the 16 ring entries, 7 multiply-adds each, into one sum
+// per lag, and the valid pairs are counted per lag from a bit history of the
+// valid kernels (four 8-bit counts per register).  The result is the mean over
+// lags of sum / (pairs * kernel length), NaN for a lag without pairs, and 0
+// where the pixel keeps at most nlag elements -- the definition of slsc_kernel.
+// ---------------------------------------------------------------------------
+constexpr int kSlscLags = 16;
+constexpr int kSlscKern = 3;
+constexpr int kSlscWin = 2 * kSlscKern + 1;
+constexpr int kSlscWords = 8;  // kept-element bits: nrx <= 256
+
+__global__ void __launch_bounds__(128, 2)
+slsc_reg_kernel(const float *__restrict__ im, const unsigned char *__restrict__ mask, int nrx,
+                int nx, int nz, int nlag, int nkern, float *__restrict__ out) {
+    const long long pix = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long npix = (long long)nx * nz;
+    if (pix >= npix) return;
+    const int ix = (int)(pix / nz), iz = (int)(pix % nz);
+    const long long f = blockIdx.y;
+    const int z0 = max(0, iz - nkern), z1 = min(nz, iz + nkern + 1);
+    const int L = z1 - z0;
+    const float invL = 1.0f / (float)L;
+
+    // kept elements: receive mask on over the whole kernel
+    unsigned kept[kSlscWords];
+#pragma unroll
+    for (int q = 0; q < kSlscWords; ++q) kept[q] = 0u;
+    // the mask bytes of the kernel, all loads of an element in flight at once
+    // (out-of-kernel positions read as on)
+    for (int e = 0; e < nrx; ++e) {
+        const unsigned char *m = mask + ((long long)e * nx + ix) * nz;
+        unsigned on = 1u;
+#pragma unroll
+        for (int w = 0; w < kSlscWin; ++w) {
+            const int z = z0 + w;
+            on &= (z < z1) ? (unsigned)(__ldg(m + min(z, nz - 1)) != 0) : 1u;
+        }
+#pragma unroll
+        for (int q = 0; q < kSlscWords; ++q)
+            if (q == (e >> 5)) kept[q] |= on << (e & 31);
+    }
+    int nsel = 0;
+#pragma unroll
+    for (int q = 0; q < kSlscWords; ++q) nsel += __popc(kept[q]);
+
+    const float *base = im + (f * nrx) * (long long)nx * nz + (long long)ix * nz + z0;
+    const long long estride = (long long)nx * nz;
+    float ring[kSlscLags][kSlscWin];
+#pragma unroll
+    for (int u = 0; u < kSlscLags; ++u)
+#pragma unroll
+        for (int w = 0; w < kSlscWin; ++w) ring[u][w] = 0.f;
+    float lag[kSlscLags];
+#pragma unroll
+    for (int m = 0; m < kSlscLags; ++m) lag[m] = 0.f;
+    // bit k of vbits: the kept element k had a valid kernel (deviation >= 1e-10)
+    unsigned vbits[kSlscWords];
+#pragma unroll
+    for (int q = 0; q < kSlscWords; ++q) vbits[q] = 0u;
+
+    int q = 0;
+    unsigned cur = kept[0];
+    // the next kept element (element order), or -1
+    auto next_elem = [&]() -> int {
+        while (cur == 0u) {
+            if (++q >= kSlscWords) return -1;
+#pragma unroll
+            for (int r = 0; r < kSlscWords; ++r)
+                if (r == q) cur = kept[r];
+        }
+        const int b = __ffs(cur) - 1;
+        cur &= cur - 1u;
+        return 32 * q + b;
+    };
+    for (int k0 = 0; k0 < nsel; k0 += kSlscLags) {
+#pragma unroll
+        for (int u = 0; u < kSlscLags; ++u) {
+            if (k0 + u < nsel) {
+                const int e = next_elem();
+                const float *x = base + (long long)e * estride;
+                float v[kSlscWin];
+                float mu = 0.f;
+#pragma unroll
+                for (int w = 0; w < kSlscWin; ++w) {
+                    v[w] = (w < L) ? __ldg(x + w) : 0.f;
+                    mu += v[w];
+                }
+                mu *= invL;
+                float var = 0.f;
+#pragma unroll
+                for (int w = 0; w < kSlscWin; ++w) {
+                    v[w] = (w < L) ? v[w] - mu : 0.f;
+                    var = fmaf(v[w], v[w], var);
+                }
+                const float sd = sqrtf(var * invL);
+                const bool ok = !(sd < kSigmaMin);
+                const float inv_sd = ok ? 1.0f / sd : 0.f;
+#pragma unroll
+                for (int w = 0; w < kSlscWin; ++w) v[w] *= inv_sd;
+#pragma unroll
+                for (int m = 1; m <= kSlscLags; ++m) {
+                    const float *pr = ring[(u - m + kSlscLags) % kSlscLags];
+                    float d = lag[m - 1];
+#pragma unroll
+                    for (int w = 0; w < kSlscWin; ++w) d = fmaf(v[w], pr[w], d);
+                    lag[m - 1] = d;
+                }
+#pragma unroll
+                for (int w = 0; w < kSlscWin; ++w) ring[u][w] = v[w];
+                const int k = k0 + u;
+#pragma unroll
+                for (int qq = 0; qq < kSlscWords; ++qq)
+                    if (qq == (k >> 5)) vbits[qq] |= (ok ? 1u : 0u) << (k & 31);
+            }
+        }
+    }
+    float res = 0.f;
+    if (nsel >= nlag + 1) {
+        for (int m = 0; m < kSlscLags; ++m) {
+            if (m < nlag) {
+                // pairs of lag m + 1 with both kernels valid: popc(vbits & vbits >> (m + 1))
+                int c = 0;
+#pragma unroll
+                for (int qq = 0; qq < kSlscWords; ++qq) {
+                    const unsigned hi = qq + 1 < kSlscWords ? vbits[qq + 1] : 0u;
+                    const unsigned sh = __funnelshift_r(vbits[qq], hi, m + 1);
+                    c += __popc(vbits[qq] & sh);
+                }
+                const float r = c ? lag[m] * invL / (float)c : __int_as_float(0x7fc00000);
+                res += r / (float)nlag;
+            }
+        }
+    }
+    out[f * npix + pix] = res;
+}
+
 cudaError_t launch_slsc(const float *im, const unsigned char *mask, long long nframes, int nrx,
                         int nx, int nz, int nlag, int nkern, float *out, cudaStream_t s) {
+    if (nlag <= kSlscLags && nkern <= kSlscKern && nrx <= 32 * kSlscWords) {
+        const long long npix = (long long)nx * nz;
+        const long long bx = (npix + 127) / 128;
+        slsc_reg_kernel<<<dim3((unsigned)bx, (unsigned)nframes), 128, 0, s>>>(im, mask, nrx, nx, nz,
+                                                                              nlag, nkern, out);
+        return cudaGetLastError();
+    }
     const int kmax = 2 * nkern + 1;
     const size_t per_thread = sizeof(float) * ((size_t)nlag * kmax + 2 * (size_t)nlag);
     int bs = (int)std::min<size_t>(128, (200 * 1024) / per_thread);

@@ -204,6 +204,10 @@ struct DasArgs {
     // exercised without a fault)
     long long wait_cycles;
     int stall_test;
+    // staged delay gradients: the upstream gradient (kernel pixel order) and
+    // dL/dtautx (ntx, np), dL/dtaurx (nrx, np), either may be null
+    const float *gk;
+    float *gtx, *grx;
 };
 
 // gather kinds of the polynomial-record interpolators (records from poly.cu)
@@ -219,6 +223,9 @@ long long tabbed_plan_words(long long np, int ntx, int nrx);
 cudaError_t launch_tabbed_plan(const DasArgs &a, int interp, int dtype, int *plan, cudaStream_t s);
 cudaError_t launch_das_staged(const DasArgs &a, int interp, int sumtype, int dtype, const int *plan,
                               int *status, cudaStream_t s);
+// the delay gradients on the staging plan (cubic, float32 records, one frame)
+cudaError_t launch_das_staged_adj(const DasArgs &a, int sumtype, int dtype, const int *plan,
+                                  cudaStream_t s);
 
 // cubic upsampling for nearest with usf > 1: out (nch, ntu) float32 from the
 // spline records in a.data (time axis of the original channel data in a)
@@ -276,6 +283,7 @@ struct AdjArgs {
     float *partial;       // workspace: per-part sums of the spline-record adjoints
     unsigned char *live;  // workspace: live[r * tiles + tile] = receive r can contribute to the tile
     const float *gk;      // set by launch_adjoint: gk_buf, or grad_out without pixel_index
+    const int *plan;      // Tabbed: the forward's staging plan when its staged path applies, or NULL
 };
 // parts of the pixel range whose channel adjoints are summed separately, and
 // the workspace: [gathered gradient (nframes * nrx * np floats, 256-byte
@@ -286,7 +294,7 @@ size_t adjoint_grad_bytes(long long nframes, long long nrx, long long np);
 size_t adjoint_partial_bytes(long long nframes, long long ntx, long long nrx, long long np, int nt);
 size_t adjoint_workspace_bytes(long long nframes, long long ntx, long long nrx, long long np,
                                int nt);
-int adjoint_rows_warps(int nt);  // warps (private accumulation rows) per scatter CTA, 0 = nt too large
+int adjoint_rows_warps(int nt);  // warps per scatter CTA (they share its rows), 0 = nt too large
 cudaError_t launch_adjoint(const AdjArgs &a, int dtype, cudaStream_t s);
 cudaError_t launch_das_synth_slow(const DasArgs &a, int sumtype, int dtype, cudaStream_t s);
 

@@ -15,6 +15,7 @@ cudaError_t launch_plan_bf16(const DasArgs &, int, int *, cudaStream_t);
 cudaError_t launch_staged_f32(const DasArgs &, int, int, const int *, int *, cudaStream_t);
 cudaError_t launch_staged_f16(const DasArgs &, int, int, const int *, int *, cudaStream_t);
 cudaError_t launch_staged_bf16(const DasArgs &, int, int, const int *, int *, cudaStream_t);
+cudaError_t launch_staged_adj_f32(const DasArgs &, int, const int *, cudaStream_t);
 
 long long tabbed_plan_words(long long np, int ntx, int nrx) {
     return plan_layout(np, ntx, nrx).total;
@@ -71,6 +72,12 @@ cudaError_t launch_synth_rx_mask(const DasArgs &a, unsigned char *mask, cudaStre
     const long long bx = (a.np + 255) / 256;
     synth_rx_mask_kernel<<<(unsigned)bx, 256, 0, s>>>(a, mask);
     return cudaGetLastError();
+}
+
+cudaError_t launch_das_staged_adj(const DasArgs &a, int sumtype, int dtype, const int *plan,
+                                  cudaStream_t s) {
+    if (dtype != PYCBF_GB_F32) return cudaErrorInvalidValue;  // float32 records (F32, I16 data)
+    return launch_staged_adj_f32(a, sumtype, plan, s);
 }
 
 }  // namespace pgb

@@ -36,7 +36,8 @@ constexpr unsigned kWaitLimit = 1u << 30;  // polls; the ~1 s clock bound ends a
 //   [0] nlive, [1..3] pad, then per live receive k (in receive order) 16 words
 //   at 4 + 16 k: [0] code (receive index, | kUnstaged when its windows exceed
 //   a stage), [1] total staged elements, [2..3] pad, [4 + t] the window of
-//   transmit t: first element e0 | (element offset in the stage << 19)
+//   transmit t: first element e0 | (elements << 19) (staged receives; the
+//   stage holds the windows one after another in transmit order)
 // then the tile order (one int per tile, most live receives first), a
 // per-tile counter, the block items (int4 each: tile, first and one-past-last
 // position in the tile's live list, block ordinal << 16 | blocks of the
@@ -53,6 +54,7 @@ constexpr unsigned kWaitLimit = 1u << 30;  // polls; the ~1 s clock bound ends a
 constexpr int kRxBlock = kRxBlockSum;
 constexpr int kRxWords = 16;           // plan words per live receive
 constexpr int kUnstaged = 0x40000000;  // receive code flag: gathered from global memory
+constexpr int kCodeFlags = kUnstaged;
 constexpr int kWinBits = 19;           // window start bits (the staged path needs nt <= 2^19)
 constexpr int kStagedMaxNt = 1 << kWinBits;
 __host__ __device__ inline long long plan_tile_words(int nrx) {
@@ -298,7 +300,7 @@ __global__ void __launch_bounds__(kBlock) tabbed_plan_kernel(const __grid_consta
         }
         if (lane < kTxReg)
             rr[4 + lane] = (staged && lane < ntx)
-                               ? (int)((unsigned)my_e0 | ((unsigned)off << kWinBits))
+                               ? (int)((unsigned)my_e0 | ((unsigned)my_cnt << kWinBits))
                                : 0;
     }
 }
@@ -428,17 +430,43 @@ __device__ __forceinline__ float staged_group(const DasArgs &a, const float2 *tt
 
 // Cubic taps from float32 polynomial records in a stage: N <= kTapGroup
 // transmits of receive (trx, arx), their delays and weights as float32 pairs
-// tt2/at2 (the pair's second lane past N is padding).  The delay sums, weights
-// and quotients are formed two taps per instruction (each lane rounded as the
-// scalar operation).  The knot is floor(q) for the fast quotient q = fl(fl(x -
-// t0) * fl(1/dt)): q - 1/2 is exact for 0 <= q < 2^22, and adding 1.5 * 2^23
-// rounds it to an integer held in the low bits of the sum -- floor(q)
-// wherever q is not an integer -- so the sum's bit pattern minus that of 1.5 *
-// 2^23 is the index itself.  The fraction g = q - floor flags every tap whose
-// q lies within eps_fast of an integer: only there can q and the correctly
-// rounded quotient fl(fl(x - t0) / dt) have different floors, and the group
-// redoes those taps with the IEEE division.  Gathers are issued before that
-// rare branch and redone in it.
+// tt2/at2 (the pair's second lane past N is padding), sb[k] the element base
+// of transmit k's window in the stage.  The delay sums, weights and quotients
+// are formed two taps per instruction (each lane rounded as the scalar
+// operation).  The knot: for the fast quotient q = fl(fl(x - t0) * fl(1/dt)),
+// s = q - 1/2 is exact for 0 <= q < 2^22, and adding 1.5 * 2^23 rounds it to
+// an integer j held in the low bits of the sum, so h = s - j lies in
+// [-1/2, 1/2].  Where |h| <= 1/2 - eps_fast (eps_fast exceeds 1.5 |q| 2^-23,
+// the largest gap between q and the reference's correctly rounded quotient
+// fl(fl(x - t0) / dt), for every q below nt), both quotients lie strictly
+// between j and j + 1, so j is the reference's knot; the sum's bit pattern
+// minus that of 1.5 * 2^23 is j itself.  A group holding any other tap (q
+// within eps_fast of an integer; NaN and infinite delays too) takes
+// staged_cubic_exact instead, which decides every tap with the IEEE division.
+// The two paths share nothing after the branch but the running sum, so the
+// common one carries no merge of gathered records.
+template <int N>
+__device__ __forceinline__ float staged_cubic_exact(const DasArgs &a, const float2 *tt2,
+                                                 const float2 *at2, float trx, float arx,
+                                                 const int *sb, const float4 *stage, float accr) {
+    constexpr unsigned cap = kStageBytes / sizeof(float4);
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const float x = __fadd_rn(pair_lane(tt2, k), trx);
+        const float apod = __fmul_rn(pair_lane(at2, k), arx);
+        const float fl = floorf(__fdiv_rn(__fsub_rn(x, a.t0), a.dt));
+        const int j = (int)fminf(fmaxf(fl, -1.f), (float)a.nt);  // NaN: -1
+        const float4 c = stage[min((unsigned)(sb[k] + j), cap - 1u)];
+        const float xlo = __fadd_rn(a.t0, __fmul_rn(a.dt, fl));
+        const float b = __fmul_rn(__fsub_rn(x, xlo), a.inv_dt);
+        const float v = fmaf(fmaf(fmaf(c.w, b, c.z), b, c.y), b, c.x);
+        const bool ok = (x >= a.t0) && (x <= a.xmax) && (fabsf(apod) >= a.thresh);
+        const float r = fmaf(apod, v, accr);
+        accr = ok ? r : accr;
+    }
+    return accr;
+}
+
 template <int N>
 __device__ __forceinline__ float staged_cubic_group(const DasArgs &a, const float2 *tt2,
                                                     const float2 *at2, float trx, float arx,
@@ -449,6 +477,7 @@ __device__ __forceinline__ float staged_cubic_group(const DasArgs &a, const floa
     const float2 trx2 = make_float2(trx, trx), arx2 = make_float2(arx, arx);
     const float2 t02 = make_float2(a.t0, a.t0), inv2 = make_float2(a.inv_dt, a.inv_dt);
     const float2 half2 = make_float2(0.5f, 0.5f), mag2 = make_float2(12582912.f, 12582912.f);
+    const float hmax = 0.5f - a.eps_fast;
     float2 x2[NP], ap2[NP], fj2[NP];
     int e[2 * NP];
     bool nearb = false;
@@ -457,28 +486,19 @@ __device__ __forceinline__ float staged_cubic_group(const DasArgs &a, const floa
         x2[p] = add2_rn(tt2[p], trx2);
         ap2[p] = mul2_rn(at2[p], arx2);
         const float2 q2 = mul2_rn(sub2_rn(x2[p], t02), inv2);
-        const float2 r2 = add2_rn(sub2_rn(q2, half2), mag2);
+        const float2 s2 = sub2_rn(q2, half2);
+        const float2 r2 = add2_rn(s2, mag2);
         fj2[p] = sub2_rn(r2, mag2);
-        const float2 g2 = sub2_rn(q2, fj2[p]);
+        const float2 h2 = sub2_rn(s2, fj2[p]);
         e[2 * p] = sb[2 * p] + (__float_as_int(r2.x) - 0x4B400000);
         e[2 * p + 1] = sb[2 * p + 1] + (__float_as_int(r2.y) - 0x4B400000);
-        nearb |= !(g2.x >= a.eps_fast && g2.x <= 1.f - a.eps_fast);
-        if (2 * p + 1 < N) nearb |= !(g2.y >= a.eps_fast && g2.y <= 1.f - a.eps_fast);
+        nearb |= !(fabsf(h2.x) <= hmax);
+        if (2 * p + 1 < N) nearb |= !(fabsf(h2.y) <= hmax);
     }
+    if (nearb) return staged_cubic_exact<N>(a, tt2, at2, trx, arx, sb, stage, accr);
     float4 pv[N];
 #pragma unroll
     for (int k = 0; k < N; ++k) pv[k] = stage[min((unsigned)e[k], cap - 1u)];
-    if (nearb) {
-#pragma unroll
-        for (int k = 0; k < N; ++k) {
-            const float x = (k & 1) ? x2[k >> 1].y : x2[k >> 1].x;
-            const float fl = floorf(__fdiv_rn(__fsub_rn(x, a.t0), a.dt));
-            const int j = (int)fminf(fmaxf(fl, -1.f), (float)a.nt);  // NaN: 0
-            if (k & 1) fj2[k >> 1].y = fl;
-            else fj2[k >> 1].x = fl;
-            pv[k] = stage[min((unsigned)(sb[k] + j), cap - 1u)];
-        }
-    }
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
         // b = (x - xlo) / dt, xlo = fl(t0 + fl(dt j)) as the reference rounds the
@@ -503,6 +523,90 @@ __device__ __forceinline__ float staged_cubic_group(const DasArgs &a, const floa
     return accr;
 }
 
+// Delay gradients of N <= kTapGroup cubic taps of receive (trx, arx), the
+// adjoint of the delay-and-sum with respect to tautx and taurx: for every tap
+// the forward counts (the same decisions: range, threshold, knot), d = apod *
+// (gp * dS/dx) with dS/dx = (p1 + 2 p2 b + 3 p3 b^2) / dt from the interval's
+// polynomial record; d is added into gt[k] (this pixel's dL/dtautx of the
+// group's transmit k, over receives in order) and into the returned gr
+// (dL/dtaurx, over transmits in order).  Records come from the stage
+// (STAGED; sb the element bases of the windows in the stage) or from global memory
+// (grec: the record row of the group's first transmit, chs between
+// transmits).
+template <int N, bool STAGED>
+__device__ __forceinline__ float adj_cubic_group(const DasArgs &a, const float2 *tt2,
+                                                 const float2 *at2, float trx, float arx, float gp,
+                                                 const int *sb, const float4 *stage,
+                                                 const float4 *grec, long long chs, float *gt,
+                                                 float gr) {
+    constexpr unsigned cap = kStageBytes / sizeof(float4);
+    constexpr int NP = (N + 1) / 2;
+    const float2 trx2 = make_float2(trx, trx), arx2 = make_float2(arx, arx);
+    const float2 t02 = make_float2(a.t0, a.t0), inv2 = make_float2(a.inv_dt, a.inv_dt);
+    const float2 half2 = make_float2(0.5f, 0.5f), mag2 = make_float2(12582912.f, 12582912.f);
+    const float hmax = 0.5f - a.eps_fast;
+    float2 x2[NP], ap2[NP], fj2[NP];
+    int jj[2 * NP];
+    bool nearb = false;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        x2[p] = add2_rn(tt2[p], trx2);
+        ap2[p] = mul2_rn(at2[p], arx2);
+        const float2 s2 = sub2_rn(mul2_rn(sub2_rn(x2[p], t02), inv2), half2);
+        const float2 r2 = add2_rn(s2, mag2);
+        fj2[p] = sub2_rn(r2, mag2);
+        const float2 h2 = sub2_rn(s2, fj2[p]);
+        jj[2 * p] = __float_as_int(r2.x) - 0x4B400000;
+        jj[2 * p + 1] = __float_as_int(r2.y) - 0x4B400000;
+        nearb |= !(fabsf(h2.x) <= hmax);
+        if (2 * p + 1 < N) nearb |= !(fabsf(h2.y) <= hmax);
+    }
+    if (nearb) {  // rare: every tap of the group with the IEEE quotient
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const float x = (k & 1) ? x2[k >> 1].y : x2[k >> 1].x;
+            const float fl = floorf(__fdiv_rn(__fsub_rn(x, a.t0), a.dt));
+            jj[k] = (int)fminf(fmaxf(fl, -1.f), (float)a.nt);  // NaN: -1
+            if (k & 1) fj2[k >> 1].y = fl;
+            else fj2[k >> 1].x = fl;
+        }
+    }
+    float4 pv[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        if (STAGED) {
+            pv[k] = stage[min((unsigned)(sb[k] + jj[k]), cap - 1u)];
+        } else {
+            const int j = min(max(jj[k], 0), a.nt - 1);
+            pv[k] = __ldg(grec + k * chs + j);
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const float2 xlo2 = make_float2(__fadd_rn(a.t0, __fmul_rn(a.dt, fj2[p].x)),
+                                        __fadd_rn(a.t0, __fmul_rn(a.dt, fj2[p].y)));
+        const float2 b2 = mul2_rn(sub2_rn(x2[p], xlo2), inv2);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int k = 2 * p + h;
+            if (k < N) {
+                const float b = h ? b2.y : b2.x;
+                const float x = h ? x2[p].y : x2[p].x;
+                const float apod = h ? ap2[p].y : ap2[p].x;
+                const float slope =
+                    fmaf(fmaf(3.f * pv[k].w, b, 2.f * pv[k].z), b, pv[k].y) * a.inv_dt;
+                const float d = apod * (gp * slope);
+                const bool ok = (x >= a.t0) && (x <= a.xmax) && (fabsf(apod) >= a.thresh);
+                if (ok) {
+                    gt[k] += d;
+                    gr += d;
+                }
+            }
+        }
+    }
+    return gr;
+}
+
 // Persistent: a grid sized to the GPU takes work items from the plan's queue
 // head (plan[1], zeroed before the launch) in the plan's order, largest first,
 // so the slowest items start first and the last wave is short: (tile, block
@@ -518,7 +622,13 @@ __device__ __forceinline__ float staged_cubic_group(const DasArgs &a, const floa
 // it - 1 with receive it + 3 once every warp has left that slot.  Each warp
 // keeps the plan words of the next receive it will stage in registers,
 // loaded one turn ahead.
-template <int KIND, int SUM, typename T>
+//
+// ADJ: the delay gradients instead of the image (cubic, float32 records, one
+// frame): whole tiles as items, the upstream gradient a.gk (kernel pixel
+// order; per pixel for TX_AND_RX, per receive and pixel for TX_ONLY), dL/dtaurx
+// written per live receive into a.grx and dL/dtautx per item into a.gtx (the
+// rows of receives a tile cannot use stay as the caller zeroed them).
+template <int KIND, int SUM, typename T, bool ADJ = false>
 __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_constant__ DasArgs a,
                                                               int *__restrict__ plan) {
     using E = typename StagedElem<KIND, T>::E;
@@ -544,7 +654,7 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
     const long long tiles = L.tiles;
     const long long tile_words = L.tile_words;
     constexpr bool kBlockSum = SUM == PYCBF_GB_SUM_TX_AND_RX || SUM == PYCBF_GB_SUM_TX_ONLY;
-    const bool by_block = kBlockSum && a.nframes == 1;
+    const bool by_block = !ADJ && kBlockSum && a.nframes == 1;
     const long long nitems = by_block ? (long long)__ldg(plan + 2) : tiles * a.nframes;
     const int *order = plan + L.order;
     const int4 *bitems = reinterpret_cast<const int4 *>(plan + L.items);
@@ -604,12 +714,16 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             const int slot = gi & (kStages - 1);
             const int code = s_rx[it];
             const bool staged = !(code & kUnstaged);
-            const int r = code & (kUnstaged - 1);
+            const int r = code & ~kCodeFlags;
             const int e0 = wv & ((1 << kWinBits) - 1);
-            const int off = (int)((unsigned)wv >> kWinBits);
-            int nxt = __shfl_down_sync(kFull, off, 1);
-            if (lane == ntx - 1) nxt = tot;
-            const int cnt = (staged && lane < ntx) ? nxt - off : 0;
+            const int cnt = (staged && lane < ntx) ? (int)((unsigned)wv >> kWinBits) : 0;
+            // this transmit's offset in the stage: exclusive prefix of the lengths
+            int off = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(kFull, off, o);
+                if (lane >= o) off += v;
+            }
+            off -= cnt;
             if (lane < kTxReg) sbase[slot][lane] = (staged && lane < ntx) ? off - e0 : 0;
             // stall test: the item's first receive announces its bytes (at least 16)
             // and issues no copy, so its phase never completes and nothing is in flight
@@ -674,25 +788,32 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
         float bacc = 0.f;  // the current receive block's sequential sum (TX_AND_RX)
         int cur_block = -1;
         bool failed = false;
+        // ADJ: this pixel's dL/dtautx per transmit, and its upstream gradient
+        float gt[kTxReg];
+#pragma unroll
+        for (int k = 0; k < kTxReg; ++k) gt[k] = 0.f;
+        const float gpix = (ADJ && SUM == PYCBF_GB_SUM_TX_AND_RX && valid) ? __ldg(a.gk + i) : 0.f;
         // receive-side values, fetched two receives ahead
         const float *trp = a.taurx + i, *arp = a.apodrx + i;
-        auto rx_load = [&](int it, float &trx, float &arx) {
-            const long long ro = (long long)(s_rx[it] & (kUnstaged - 1)) * np;
+        auto rx_load = [&](int it, float &trx, float &arx, float &gpr) {
+            const long long ro = (long long)(s_rx[it] & ~kCodeFlags) * np;
             trx = valid ? __ldg(trp + ro) : 0.f;
             arx = valid ? __ldg(arp + ro) : 0.f;
+            gpr = (ADJ && SUM == PYCBF_GB_SUM_TX_ONLY && valid) ? __ldg(a.gk + ro + i) : gpix;
         };
-        float trx1 = 0.f, arx1 = 0.f, trx2 = 0.f, arx2 = 0.f;
-        if (nlive > 0) rx_load(0, trx1, arx1);
-        if (nlive > 1) rx_load(1, trx2, arx2);
+        float trx1 = 0.f, arx1 = 0.f, trx2 = 0.f, arx2 = 0.f, gp1 = 0.f, gp2 = 0.f;
+        if (nlive > 0) rx_load(0, trx1, arx1, gp1);
+        if (nlive > 1) rx_load(1, trx2, arx2, gp2);
 
         for (int it = 0; it < nlive; ++it) {
             const int gi = g0 + it;
             const int slot = gi & (kStages - 1);
-            const int r = s_rx[it] & (kUnstaged - 1);
-            const float trx = trx1, arx = arx1;
+            const int r = s_rx[it] & ~kCodeFlags;
+            const float trx = trx1, arx = arx1, gp = gp1;
             trx1 = trx2;
             arx1 = arx2;
-            if (it + 2 < nlive) rx_load(it + 2, trx2, arx2);
+            gp1 = gp2;
+            if (it + 2 < nlive) rx_load(it + 2, trx2, arx2, gp2);
             if (!mbar_try_wait(&full[slot], (unsigned)(gi >> 2) & 1u)) {
                 if (*(volatile int *)&s_failed ||
                     !mbar_wait_bounded(&full[slot], (unsigned)(gi >> 2) & 1u, wait_lim)) {
@@ -709,7 +830,49 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             }
             const bool live = valid && (__fmul_rn(amax, fabsf(arx)) >= a.thresh);
             float accr = 0.f;
-            if (live) {
+            if constexpr (ADJ) {
+                // delay gradients of this receive's taps (dL/dtaurx of a
+                // non-live pixel is 0: every tap of it fails the threshold)
+                float gr = 0.f;
+                if (live) {
+                    const long long chs = (long long)nrx * a.nt;
+                    const float4 *grow = static_cast<const float4 *>(a.data) + (frame_ch + r) * a.nt;
+                    const bool stg = sstaged[slot] != 0;
+                    const float4 *st4 =
+                        reinterpret_cast<const float4 *>(smem_raw + (size_t)slot * kStageBytes);
+                    int sb[kTxReg];
+#pragma unroll
+                    for (int g = 0; g < kTxReg; g += 4) {
+                        const int4 b = *reinterpret_cast<const int4 *>(&sbase[slot][g]);
+                        sb[g] = b.x;
+                        sb[g + 1] = b.y;
+                        sb[g + 2] = b.z;
+                        sb[g + 3] = b.w;
+                    }
+#pragma unroll
+                    for (int g = 0; g < kTxReg; g += kTapGroup) {
+                        if (g < ntx) {
+                            const int rem = ntx - g;
+#define PGB_AGROUP(n, st)                                                                         \
+    adj_cubic_group<n, st>(a, tt2 + g / 2, at2 + g / 2, trx, arx, gp, sb + g, st4,                \
+                           grow + (long long)g * chs, chs, gt + g, gr)
+                            if (stg) {
+                                if (rem >= 4) gr = PGB_AGROUP(4, true);
+                                else if (rem == 3) gr = PGB_AGROUP(3, true);
+                                else if (rem == 2) gr = PGB_AGROUP(2, true);
+                                else gr = PGB_AGROUP(1, true);
+                            } else {
+                                if (rem >= 4) gr = PGB_AGROUP(4, false);
+                                else if (rem == 3) gr = PGB_AGROUP(3, false);
+                                else if (rem == 2) gr = PGB_AGROUP(2, false);
+                                else gr = PGB_AGROUP(1, false);
+                            }
+#undef PGB_AGROUP
+                        }
+                    }
+                }
+                if (valid && a.grx) a.grx[(long long)r * np + i] = gr;
+            } else if (live) {
                 if (sstaged[slot]) {
                     const E *stage = reinterpret_cast<const E *>(smem_raw + (size_t)slot * kStageBytes);
                     int sb[kTxReg];
@@ -761,7 +924,8 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
                 }
             }
             if (SUM == PYCBF_GB_SUM_TX_AND_RX) bacc += accr;
-            if (SUM == PYCBF_GB_SUM_TX_ONLY && valid) a.out[((long long)f * nrx + r) * np + op] = accr;
+            if (!ADJ && SUM == PYCBF_GB_SUM_TX_ONLY && valid)
+                a.out[((long long)f * nrx + r) * np + op] = accr;
             if (SUM == PYCBF_GB_SUM_DMAS_SSR || SUM == PYCBF_GB_SUM_DMAS_POWER) {
                 const float sv = (SUM == PYCBF_GB_SUM_DMAS_SSR) ? copysignf(sqrtf(fabsf(accr)), accr) : accr;
                 acc = fmaf(sv, s1, acc);
@@ -784,6 +948,17 @@ __global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_cons
             }
         }
         __syncthreads();
+        if constexpr (ADJ) {
+            if (valid && a.gtx) {
+                const float nan = __int_as_float(0x7fc00000);
+#pragma unroll
+                for (int k = 0; k < kTxReg; ++k)
+                    if (k < ntx) a.gtx[(long long)k * np + i] = s_failed ? nan : gt[k];
+            }
+            if (s_failed) break;
+            g0 += nlive;
+            continue;
+        }
         if (s_failed) {
             if (valid) {
                 const float nan = __int_as_float(0x7fc00000);
@@ -881,7 +1056,7 @@ static __global__ void __launch_bounds__(1024) plan_order_kernel(int *plan, long
             return;
         }
         // the block of live receive k
-        auto blk = [&](int k) { return (rec[4 + kRxWords * k] & (kUnstaged - 1)) / kRxBlock; };
+        auto blk = [&](int k) { return (rec[4 + kRxWords * k] & ~kCodeFlags) / kRxBlock; };
         int nb = 0;
         for (int k = 0; k < nlive; ++k)
             if (k == 0 || blk(k) != blk(k - 1)) ++nb;
@@ -956,6 +1131,36 @@ cudaError_t launch_staged_one(const DasArgs &a, const int *plan, int *status, cu
         if (err != cudaSuccess) return err;
     }
     kern<<<(unsigned)grid, kBlock, smem, s>>>(a, const_cast<int *>(plan));
+    return cudaGetLastError();
+}
+
+// The delay gradients on the staging plan (ADJ mode; cubic, float32 records,
+// one frame, sumtype TX_AND_RX or TX_ONLY).  dL/dtaurx rows of receives a tile
+// cannot use are zeroed first.
+template <typename T>
+cudaError_t launch_staged_adj(const DasArgs &a, int sum, const int *plan, cudaStream_t s) {
+    if (!CoefRec<T>::kPoly || a.nframes != 1) return cudaErrorInvalidValue;
+    auto kern = sum == PYCBF_GB_SUM_TX_AND_RX
+                    ? das_staged_kernel<PYCBF_GB_INTERP_CUBIC, PYCBF_GB_SUM_TX_AND_RX, T, true>
+                    : das_staged_kernel<PYCBF_GB_INTERP_CUBIC, PYCBF_GB_SUM_TX_ONLY, T, true>;
+    const int smem = (int)staged_smem_bytes(a.nrx);
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (err != cudaSuccess) return err;
+    int dev = 0, nsm = 0, per_sm = 0;
+    if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
+    if ((err = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+        return err;
+    if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, smem)) !=
+        cudaSuccess)
+        return err;
+    const PlanLayout L = plan_layout(a.np, a.ntx, a.nrx);
+    const long long grid = std::min<long long>(L.tiles, (long long)std::max(1, per_sm) * nsm);
+    int *pl = const_cast<int *>(plan);
+    if ((err = cudaMemsetAsync(pl + 1, 0, sizeof(int), s)) != cudaSuccess) return err;
+    if (a.grx && (err = cudaMemsetAsync(a.grx, 0, sizeof(float) * (size_t)a.nrx * a.np, s)) !=
+                     cudaSuccess)
+        return err;
+    kern<<<(unsigned)grid, kBlock, smem, s>>>(a, pl);
     return cudaGetLastError();
 }
 

@@ -18,4 +18,8 @@ cudaError_t launch_staged_f32(const DasArgs &a, int interp, int sum, const int *
     return launch_staged_type<float>(a, interp, sum, plan, status, s);
 }
 
+cudaError_t launch_staged_adj_f32(const DasArgs &a, int sum, const int *plan, cudaStream_t s) {
+    return launch_staged_adj<float>(a, sum, plan, s);
+}
+
 }  // namespace pgb

@@ -185,6 +185,13 @@ def test_adjoint_entry_points_validate_first():
     assert tab(info=_info(nt=20000)) == _lib.ERANGE
     assert tab(grf=p) == _lib.EWORKSPACE                    # grad_rf needs the workspace
     assert tab(grf=p, ws=p, wsb=1) == _lib.EWORKSPACE
+    planned = lambda **kw: L.pycbf_gb_das_tabbed_adjoint_planned(
+        ct.byref(kw.get("info", info)), p, p, p, p, p, 10, None, 0.01, kw.get("sum", 3),
+        kw.get("plan", None), kw.get("gout", p), None, p, p, None, 0, None)
+    assert planned(plan=ct.c_void_p(8)) == _lib.EINVAL     # plans are 16-byte aligned
+    assert planned(sum=0) == _lib.EUNSUPPORTED
+    assert planned(gout=None) == _lib.EINVAL
+    assert planned(info=_info(ntx=129)) == _lib.ERANGE
     geo = _lib.SyntheticGeom()
     sinfo = _info(ndim=2)
     assert L.pycbf_gb_das_synthetic_adjoint(ct.byref(sinfo), p, ct.byref(geo), p, None, 3, p,

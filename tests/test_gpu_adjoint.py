@@ -248,3 +248,30 @@ def test_caller_delay_tables_in_any_pixel_order(tab):
     ref = TabbedBeamformer(tautx=tab.tautx, apodtx=tab.apodtx, taurx=tab.taurx, apodrx=tab.apodrx,
                            t0=tab.t0, dt=tab.dt, nt=tab.nt, interp={"kind": "cubic"})(rf, out_as_numpy=False)
     assert torch.equal(res[0][0], ref)
+
+
+@pytest.mark.parametrize("sumtype", ["tx_and_rx", "tx_only"])
+def test_planned_delay_gradients_equal_the_generic(tab, sumtype):
+    """With the forward's staging plan the delay gradients gather the spline
+    records from the plan's staged windows (the staged kernel in its adjoint
+    mode): the same taps, products and summation order as the generic kernel,
+    so the same bits; the image and the channel-data gradient are unchanged."""
+    bf = TabbedBeamformer(tautx=tab.tautx, apodtx=tab.apodtx, taurx=tab.taurx, apodrx=tab.apodrx,
+                          t0=tab.t0, dt=tab.dt, nt=tab.nt, interp={"kind": "cubic"})
+    assert bf._plan is not None and bf._pixel_index is not None
+    ktx, kap_tx, krx, kap_rx = bf._tables
+    rf = torch.as_tensor(tab.rf, device="cuda")
+    res = []
+    for plan in (None, bf._plan):
+        r = rf.clone().requires_grad_(True)
+        ttx, trx = ktx.clone().requires_grad_(True), krx.clone().requires_grad_(True)
+        out = adjoint.das_tabbed(r, ttx, trx, kap_tx, kap_rx, t0=tab.t0, dt=tab.dt,
+                                 thresh=bf.thresh, sumtype=sumtype, pixel_index=bf._pixel_index,
+                                 plan=plan)
+        g = torch.randn(out.shape, generator=torch.Generator().manual_seed(4)).cuda()
+        (out * g).sum().backward()
+        res.append((out.detach(), ttx.grad, trx.grad, r.grad))
+    assert torch.equal(res[0][0], res[1][0])
+    assert torch.equal(res[0][1], res[1][1]) and torch.equal(res[0][2], res[1][2])
+    assert torch.equal(res[0][3], res[1][3])
+    assert float(res[1][1].abs().sum()) > 0 and float(res[1][2].abs().sum()) > 0

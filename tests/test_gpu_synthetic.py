@@ -192,6 +192,33 @@ def test_slsc_vs_oracle(synthetic_small):
     assert err < 2e-4
 
 
+@pytest.mark.parametrize("nlag,nkern", [(16, 3), (20, 2), (6, 5)])
+def test_slsc_both_kernels_vs_oracle(synthetic_small, nlag, nkern):
+    """nlag <= 16 with nkern <= 3 runs the register-blocked kernel, larger
+    values the shared-memory ring kernel: both against the oracle, on a mask
+    with holes (every fifth element off in part of the image) so that the
+    kept elements are not contiguous."""
+    w = synthetic_small
+    nx, nz = w.grid
+    tables = oracle_tables(w)
+    nrx = tables[2].shape[0]
+    sep = oracle_image(w, tables, "cubic", "tx_only").reshape(nrx, nx, nz)
+    mask = (tables[3] != 0).reshape(nrx, nx, nz).copy()
+    mask[::5, : nx // 2, :] = False
+    L = _lib.load()
+    im = torch.as_tensor(sep, device="cuda")
+    m = torch.as_tensor(mask.astype(np.uint8), device="cuda")
+    out = torch.empty((nx, nz), device="cuda")
+    assert L.pycbf_gb_slsc(im.data_ptr(), m.data_ptr(), 1, nrx, nx, nz, nlag, nkern,
+                           out.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    out = out.cpu().numpy()
+    ref = oracle.slsc(sep, mask, nlag, nkern)
+    assert np.array_equal(np.isnan(out), np.isnan(ref))
+    ok = ~np.isnan(ref)
+    assert np.max(np.abs(out[ok] - ref[ok])) < 2e-4
+
+
 def test_slsc_kernel_vs_notebook_golden(golden):
     g = golden("coherence_small.npz")
     L = _lib.load()
