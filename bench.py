@@ -113,13 +113,23 @@ def fp64_columns(w, cols, dev):
     rf = torch.as_tensor(w.rf, device=dev, dtype=f64)
     ntx, nrx, nt = rf.shape
     y = rf.reshape(-1, nt).T                                        # (nt, nch)
-    # natural spline: 0.5 z_i-1 + 2 z_i + 0.5 z_i+1 = (y_i+1 - 2 y_i + y_i-1) / 2, z = y'' dt^2 / 6
+    # natural spline: 0.5 z_i-1 + 2 z_i + 0.5 z_i+1 = (y_i+1 - 2 y_i + y_i-1) / 2, z = y'' dt^2 / 6,
+    # solved on the host by the Thomas algorithm (all channels at once)
+    yh = np.asarray(w.rf, dtype=np.float64).reshape(-1, nt).T
+    d = 0.5 * (yh[2:] - 2.0 * yh[1:-1] + yh[:-2])
     n = nt - 2
-    A = (torch.diag(torch.full((n,), 2.0, dtype=f64, device=dev))
-         + torch.diag(torch.full((n - 1,), 0.5, dtype=f64, device=dev), 1)
-         + torch.diag(torch.full((n - 1,), 0.5, dtype=f64, device=dev), -1))
-    z = torch.zeros_like(y)
-    z[1:-1] = torch.linalg.solve(A, 0.5 * (y[2:] - 2.0 * y[1:-1] + y[:-2]))
+    cp = np.empty(n)
+    dp = np.empty_like(d)
+    cp[0], dp[0] = 0.25, d[0] / 2.0
+    for i in range(1, n):
+        m = 2.0 - 0.5 * cp[i - 1]
+        cp[i] = 0.5 / m
+        dp[i] = (d[i] - 0.5 * dp[i - 1]) / m
+    zh = np.zeros_like(yh)
+    zh[n] = dp[n - 1]
+    for i in range(n - 2, -1, -1):
+        zh[i + 1] = dp[i] - cp[i] * zh[i + 2]
+    z = torch.as_tensor(zh, device=dev)
     yz = torch.stack([y.T.reshape(ntx, nrx, nt), z.T.reshape(ntx, nrx, nt)])
     t32 = lambda a: torch.as_tensor(np.ascontiguousarray(a[:, cols]), device=dev)
     ttx, atx, trx, arx = t32(w.tautx), t32(w.apodtx), t32(w.taurx), t32(w.apodrx)
