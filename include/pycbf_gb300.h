@@ -351,6 +351,23 @@ int pycbf_gb_slsc(const float *im, const unsigned char *mask, long long nframes,
                   int nz, int nlag, int nkern, float *out, void *stream);
 
 /* ---------------------------------------------------------------------- */
+/* The same coherence with the kept-element sets computed once per mask    */
+/* (no counterpart in the reference, whose notebook loop re-derives them   */
+/* per pixel).  pycbf_gb_slsc_kept writes, for the axial kernel half-width */
+/* nkern, bit e % 32 of word e / 32 of each pixel (word q of pixel p at    */
+/* kept[q * nx * nz + p]) when element e's mask is on over the pixel's     */
+/* whole kernel; kept_bytes >= pycbf_gb_slsc_kept_bytes(nrx, nx, nz).      */
+/* pycbf_gb_slsc_with_kept then gives pycbf_gb_slsc's output bit for bit   */
+/* for the same nkern.  Both need nlag <= 16, nkern <= 3 and nrx <= 256    */
+/* (PYCBF_GB_ERANGE otherwise: use pycbf_gb_slsc).                          */
+/* ---------------------------------------------------------------------- */
+size_t pycbf_gb_slsc_kept_bytes(int nrx, int nx, int nz);
+int pycbf_gb_slsc_kept(const unsigned char *mask, int nrx, int nx, int nz, int nlag, int nkern,
+                       unsigned *kept, size_t kept_bytes, void *stream);
+int pycbf_gb_slsc_with_kept(const float *im, const unsigned *kept, long long nframes, int nrx,
+                            int nx, int nz, int nlag, int nkern, float *out, void *stream);
+
+/* ---------------------------------------------------------------------- */
 /* Cubic Tabbed delay-and-sum that allocates nothing (no counterpart in    */
 /* the reference).  For callers that cannot call cudaMalloc -- a language  */
 /* runtime reaching CUDA only through this C ABI, a service whose device   */

@@ -27,7 +27,8 @@ EXPORTS = (
     "pycbf_gb_workspace_bytes", "pycbf_gb_spline_coefficients", "pycbf_gb_das_tabbed",
     "pycbf_gb_das_tabbed_prefiltered", "pycbf_gb_tabbed_plan_bytes", "pycbf_gb_tabbed_plan",
     "pycbf_gb_das_synthetic", "pycbf_gb_tap_census_tabbed", "pycbf_gb_tap_census_synthetic",
-    "pycbf_gb_synthetic_rx_mask", "pycbf_gb_dmas", "pycbf_gb_slsc", "pycbf_gb_fp32_probe",
+    "pycbf_gb_synthetic_rx_mask", "pycbf_gb_dmas", "pycbf_gb_slsc", "pycbf_gb_slsc_kept_bytes",
+    "pycbf_gb_slsc_kept", "pycbf_gb_slsc_with_kept", "pycbf_gb_fp32_probe",
     "pycbf_gb_das_tabbed_cubic_noalloc", "pycbf_gb_das_synthetic_slowness",
     "pycbf_gb_adjoint_workspace_bytes", "pycbf_gb_das_tabbed_adjoint",
     "pycbf_gb_das_tabbed_adjoint_planned",
@@ -111,6 +112,10 @@ def load() -> ct.CDLL:
         L.pycbf_gb_synthetic_rx_mask.argtypes = [P(RFInfo), P(SyntheticGeom), vp, vp]
         L.pycbf_gb_dmas.argtypes = [vp, ll, ll, ll, vp, i, i, i, vp, vp]
         L.pycbf_gb_slsc.argtypes = [vp, vp, ll, i, i, i, i, i, vp, vp]
+        L.pycbf_gb_slsc_kept_bytes.argtypes = [i, i, i]
+        L.pycbf_gb_slsc_kept_bytes.restype = sz
+        L.pycbf_gb_slsc_kept.argtypes = [vp, i, i, i, i, i, vp, sz, vp]
+        L.pycbf_gb_slsc_with_kept.argtypes = [vp, vp, ll, i, i, i, i, i, vp, vp]
         L.pycbf_gb_fp32_probe.argtypes = [vp, i, i, vp]
         L.pycbf_gb_das_tabbed_cubic_noalloc.argtypes = [P(RFInfo), vp, vp, vp, vp, vp, ll, vp, f, i,
                                                         vp, vp]

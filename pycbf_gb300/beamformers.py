@@ -820,6 +820,16 @@ class _SLSCMixin:
         if not (1 <= int(self.nlag) <= 32) or not (0 <= int(self.nkern) <= 31):
             raise BeamformerException("nlag must be in 1..32 and nkern in 0..31")
         self._mask = self.rx_mask().contiguous()
+        # the kept-element bit sets depend on the mask and nkern only: once here
+        self._kept = None
+        nbytes = self._lib.pycbf_gb_slsc_kept_bytes(self.nrx, nx, nz)
+        kept = torch.empty(max(nbytes, 4), dtype=torch.uint8, device="cuda")
+        st = self._lib.pycbf_gb_slsc_kept(_ptr(self._mask), self.nrx, nx, nz, int(self.nlag),
+                                          int(self.nkern), _ptr(kept), nbytes, _stream_ptr())
+        if st == _lib.OK:
+            self._kept = kept
+        elif st != _lib.ERANGE:  # ERANGE: outside the register kernel's limits
+            _lib.check(st, "pycbf_gb_slsc_kept")
 
     def __call__(self, txrxt, out_as_numpy: bool = True, buffer=None):
         sep = self._beamform(txrxt, None, sumtype="tx_only")
@@ -827,9 +837,16 @@ class _SLSCMixin:
         nx, nz = (int(v) for v in self.grid_shape)
         shape = (nx, nz) if nframes is None else (nframes, nx, nz)
         out = self._output(shape, buffer)
-        st = self._lib.pycbf_gb_slsc(_ptr(sep), _ptr(self._mask), nframes or 1, self.nrx, nx, nz,
-                                     int(self.nlag), int(self.nkern), _ptr(out), _stream_ptr())
-        _lib.check(st, "pycbf_gb_slsc")
+        if self._kept is not None:
+            st = self._lib.pycbf_gb_slsc_with_kept(_ptr(sep), _ptr(self._kept), nframes or 1,
+                                                   self.nrx, nx, nz, int(self.nlag),
+                                                   int(self.nkern), _ptr(out), _stream_ptr())
+            _lib.check(st, "pycbf_gb_slsc_with_kept")
+        else:
+            st = self._lib.pycbf_gb_slsc(_ptr(sep), _ptr(self._mask), nframes or 1, self.nrx, nx,
+                                         nz, int(self.nlag), int(self.nkern), _ptr(out),
+                                         _stream_ptr())
+            _lib.check(st, "pycbf_gb_slsc")
         return _to_host(out) if out_as_numpy else out
 
 

@@ -458,7 +458,32 @@ int pycbf_gb_slsc(const float *im, const unsigned char *mask, long long nframes,
     if (nframes <= 0 || nrx <= 0 || nx <= 0 || nz <= 0 || nlag <= 0 || nkern < 0)
         return PYCBF_GB_EINVAL;
     if (nlag > 32 || 2 * nkern + 1 > 64 || nframes > 65535) return PYCBF_GB_ERANGE;
-    return cuda_status(launch_slsc(im, mask, nframes, nrx, nx, nz, nlag, nkern, out,
+    return cuda_status(launch_slsc(im, mask, nullptr, nframes, nrx, nx, nz, nlag, nkern, out,
+                                   static_cast<cudaStream_t>(stream)));
+}
+
+size_t pycbf_gb_slsc_kept_bytes(int nrx, int nx, int nz) {
+    if (nrx <= 0 || nx <= 0 || nz <= 0) return 0;
+    return sizeof(unsigned) * (size_t)((nrx + 31) / 32) * (size_t)nx * (size_t)nz;
+}
+
+int pycbf_gb_slsc_kept(const unsigned char *mask, int nrx, int nx, int nz, int nlag, int nkern,
+                       unsigned *kept, size_t kept_bytes, void *stream) {
+    if (!mask || !kept) return PYCBF_GB_EINVAL;
+    if (nrx <= 0 || nx <= 0 || nz <= 0 || nlag <= 0 || nkern < 0) return PYCBF_GB_EINVAL;
+    if (!slsc_kept_supported(nrx, nlag, nkern)) return PYCBF_GB_ERANGE;
+    if (kept_bytes < pycbf_gb_slsc_kept_bytes(nrx, nx, nz)) return PYCBF_GB_ERANGE;
+    return cuda_status(
+        launch_slsc_kept(mask, nrx, nx, nz, nkern, kept, static_cast<cudaStream_t>(stream)));
+}
+
+int pycbf_gb_slsc_with_kept(const float *im, const unsigned *kept, long long nframes, int nrx,
+                            int nx, int nz, int nlag, int nkern, float *out, void *stream) {
+    if (!im || !kept || !out) return PYCBF_GB_EINVAL;
+    if (nframes <= 0 || nrx <= 0 || nx <= 0 || nz <= 0 || nlag <= 0 || nkern < 0)
+        return PYCBF_GB_EINVAL;
+    if (!slsc_kept_supported(nrx, nlag, nkern) || nframes > 65535) return PYCBF_GB_ERANGE;
+    return cuda_status(launch_slsc(im, nullptr, kept, nframes, nrx, nx, nz, nlag, nkern, out,
                                    static_cast<cudaStream_t>(stream)));
 }
 

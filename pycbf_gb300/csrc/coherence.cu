@@ -155,24 +155,14 @@ constexpr int kSlscKern = 3;
 constexpr int kSlscWin = 2 * kSlscKern + 1;
 constexpr int kSlscWords = 8;  // kept-element bits: nrx <= 256
 
-__global__ void __launch_bounds__(128, 2)
-slsc_reg_kernel(const float *__restrict__ im, const unsigned char *__restrict__ mask, int nrx,
-                int nx, int nz, int nlag, int nkern, float *__restrict__ out) {
-    const long long pix = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long npix = (long long)nx * nz;
-    if (pix >= npix) return;
-    const int ix = (int)(pix / nz), iz = (int)(pix % nz);
-    const long long f = blockIdx.y;
-    const int z0 = max(0, iz - nkern), z1 = min(nz, iz + nkern + 1);
-    const int L = z1 - z0;
-    const float invL = 1.0f / (float)L;
-
-    // kept elements: receive mask on over the whole kernel
-    unsigned kept[kSlscWords];
+// Kept elements of pixel (ix, iz): bit e of kept[e / 32] is set when element
+// e's receive mask is on over the whole axial kernel [z0, z1) (the mask bytes
+// of one element are all in flight at once; positions past z1 read as on).
+__device__ __forceinline__ void slsc_kept_bits(const unsigned char *__restrict__ mask, int nrx,
+                                               int nx, int nz, int ix, int z0, int z1,
+                                               unsigned (&kept)[kSlscWords]) {
 #pragma unroll
     for (int q = 0; q < kSlscWords; ++q) kept[q] = 0u;
-    // the mask bytes of the kernel, all loads of an element in flight at once
-    // (out-of-kernel positions read as on)
     for (int e = 0; e < nrx; ++e) {
         const unsigned char *m = mask + ((long long)e * nx + ix) * nz;
         unsigned on = 1u;
@@ -184,6 +174,54 @@ slsc_reg_kernel(const float *__restrict__ im, const unsigned char *__restrict__ 
 #pragma unroll
         for (int q = 0; q < kSlscWords; ++q)
             if (q == (e >> 5)) kept[q] |= on << (e & 31);
+    }
+}
+
+// The kept-element bit sets of every pixel for one axial kernel half-width,
+// word q of pixel p at kept[q * npix + p] (q < ceil(nrx / 32)): they depend
+// on the receive mask only, so a beamformer computes them once and every
+// frame's coherence pass reads 4 bytes per 32 elements instead of the
+// kernel's mask bytes of every element.
+__global__ void __launch_bounds__(128)
+slsc_kept_kernel(const unsigned char *__restrict__ mask, int nrx, int nx, int nz, int nkern,
+                 unsigned *__restrict__ kept_out) {
+    const long long pix = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long npix = (long long)nx * nz;
+    if (pix >= npix) return;
+    const int ix = (int)(pix / nz), iz = (int)(pix % nz);
+    const int z0 = max(0, iz - nkern), z1 = min(nz, iz + nkern + 1);
+    unsigned kept[kSlscWords];
+    slsc_kept_bits(mask, nrx, nx, nz, ix, z0, z1, kept);
+    const int nw = (nrx + 31) >> 5;
+#pragma unroll
+    for (int q = 0; q < kSlscWords; ++q)
+        if (q < nw) kept_out[q * npix + pix] = kept[q];
+}
+
+// PRE: the kept bit sets come from slsc_kept_kernel's array (kept_in), else
+// from the mask bytes.
+template <bool PRE>
+__global__ void __launch_bounds__(128, 2)
+slsc_reg_kernel(const float *__restrict__ im, const unsigned char *__restrict__ mask,
+                const unsigned *__restrict__ kept_in, int nrx, int nx, int nz, int nlag, int nkern,
+                float *__restrict__ out) {
+    const long long pix = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long npix = (long long)nx * nz;
+    if (pix >= npix) return;
+    const int ix = (int)(pix / nz), iz = (int)(pix % nz);
+    const long long f = blockIdx.y;
+    const int z0 = max(0, iz - nkern), z1 = min(nz, iz + nkern + 1);
+    const int L = z1 - z0;
+    const float invL = 1.0f / (float)L;
+
+    // kept elements: receive mask on over the whole kernel
+    unsigned kept[kSlscWords];
+    if constexpr (PRE) {
+        const int nw = (nrx + 31) >> 5;
+#pragma unroll
+        for (int q = 0; q < kSlscWords; ++q) kept[q] = q < nw ? __ldg(kept_in + q * npix + pix) : 0u;
+    } else {
+        slsc_kept_bits(mask, nrx, nx, nz, ix, z0, z1, kept);
     }
     int nsel = 0;
 #pragma unroll
@@ -280,15 +318,34 @@ slsc_reg_kernel(const float *__restrict__ im, const unsigned char *__restrict__ 
     out[f * npix + pix] = res;
 }
 
-cudaError_t launch_slsc(const float *im, const unsigned char *mask, long long nframes, int nrx,
-                        int nx, int nz, int nlag, int nkern, float *out, cudaStream_t s) {
-    if (nlag <= kSlscLags && nkern <= kSlscKern && nrx <= 32 * kSlscWords) {
+bool slsc_kept_supported(int nrx, int nlag, int nkern) {
+    return nlag <= kSlscLags && nkern <= kSlscKern && nrx <= 32 * kSlscWords;
+}
+
+cudaError_t launch_slsc_kept(const unsigned char *mask, int nrx, int nx, int nz, int nkern,
+                             unsigned *kept, cudaStream_t s) {
+    const long long npix = (long long)nx * nz;
+    const long long bx = (npix + 127) / 128;
+    slsc_kept_kernel<<<(unsigned)bx, 128, 0, s>>>(mask, nrx, nx, nz, nkern, kept);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_slsc(const float *im, const unsigned char *mask, const unsigned *kept,
+                        long long nframes, int nrx, int nx, int nz, int nlag, int nkern, float *out,
+                        cudaStream_t s) {
+    if (slsc_kept_supported(nrx, nlag, nkern)) {
         const long long npix = (long long)nx * nz;
         const long long bx = (npix + 127) / 128;
-        slsc_reg_kernel<<<dim3((unsigned)bx, (unsigned)nframes), 128, 0, s>>>(im, mask, nrx, nx, nz,
-                                                                              nlag, nkern, out);
+        const dim3 grid((unsigned)bx, (unsigned)nframes);
+        if (kept)
+            slsc_reg_kernel<true><<<grid, 128, 0, s>>>(im, nullptr, kept, nrx, nx, nz, nlag, nkern,
+                                                       out);
+        else
+            slsc_reg_kernel<false><<<grid, 128, 0, s>>>(im, mask, nullptr, nrx, nx, nz, nlag,
+                                                        nkern, out);
         return cudaGetLastError();
     }
+    if (!mask) return cudaErrorInvalidValue;
     const int kmax = 2 * nkern + 1;
     const size_t per_thread = sizeof(float) * ((size_t)nlag * kmax + 2 * (size_t)nlag);
     int bs = (int)std::min<size_t>(128, (200 * 1024) / per_thread);

@@ -304,8 +304,14 @@ cudaError_t launch_das_synth_slow(const DasArgs &a, int sumtype, int dtype, cuda
 cudaError_t launch_dmas(const float *im, long long nframes, long long nsep, long long np,
                         const int *lags, int nlag, int power, int sumlags, float *out,
                         cudaStream_t s);
-cudaError_t launch_slsc(const float *im, const unsigned char *mask, long long nframes, int nrx,
-                        int nx, int nz, int nlag, int nkern, float *out, cudaStream_t s);
+// kept: the per-pixel kept-element bit sets of launch_slsc_kept, or null to
+// derive them from mask (which may then be null only when kept is given)
+cudaError_t launch_slsc(const float *im, const unsigned char *mask, const unsigned *kept,
+                        long long nframes, int nrx, int nx, int nz, int nlag, int nkern, float *out,
+                        cudaStream_t s);
+bool slsc_kept_supported(int nrx, int nlag, int nkern);
+cudaError_t launch_slsc_kept(const unsigned char *mask, int nrx, int nx, int nz, int nkern,
+                             unsigned *kept, cudaStream_t s);
 
 // argument checks of the cubic Tabbed delay-and-sum on prefiltered records (abi.cu)
 int check_tabbed_prefiltered(const pycbf_gb_rfinfo *rf, const void *coef, const float *tautx,

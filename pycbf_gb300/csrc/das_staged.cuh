@@ -26,8 +26,14 @@
 
 namespace pgb {
 
+// Four stages of 10.5 KB: with the receive codes a CTA holds ~43 KB of shared
+// memory, so five CTAs (20 warps) fit an SM -- the kernel waits on short
+// dependency chains and on loads, and 16 warps per SM measured 5 % slower
+// (12 warps: 15 % slower).  A receive whose windows exceed a stage (about 5 %
+// of the live receive-tiles of the 128-element plane-wave workload) is
+// gathered from global memory instead.
 constexpr int kStages = 4;
-constexpr int kStageBytes = 12 * 1024;
+constexpr int kStageBytes = 10752;
 constexpr unsigned kWaitLimit = 1u << 30;  // polls; the ~1 s clock bound ends a wait first
 
 // plan layout (int32 words): [0] status, [1] work-queue head of the staged
@@ -629,7 +635,7 @@ __device__ __forceinline__ float adj_cubic_group(const DasArgs &a, const float2 
 // written per live receive into a.grx and dL/dtautx per item into a.gtx (the
 // rows of receives a tile cannot use stay as the caller zeroed them).
 template <int KIND, int SUM, typename T, bool ADJ = false>
-__global__ void __launch_bounds__(kBlock, 4) das_staged_kernel(const __grid_constant__ DasArgs a,
+__global__ void __launch_bounds__(kBlock, ADJ ? 4 : 5) das_staged_kernel(const __grid_constant__ DasArgs a,
                                                               int *__restrict__ plan) {
     using E = typename StagedElem<KIND, T>::E;
     constexpr bool kPolyCubic = KIND == PYCBF_GB_INTERP_CUBIC && CoefRec<T>::kPoly;

@@ -232,3 +232,17 @@ def test_batch_plan_validates_jobs():
     bad.geom = 1  # synthetic without geometry
     assert plan((_lib.BatchJob * 2)(j, bad)) == _lib.EINVAL
     assert L.pycbf_gb_batch_run(p, ct.byref(info), 6, 10, None) == _lib.EINVAL
+
+
+def test_slsc_kept_limits():
+    """Host checks only: the kept-set entry points refuse what the register
+    kernel cannot run (ERANGE) and missing pointers (EINVAL)."""
+    L = _lib.load()
+    p = 256
+    assert L.pycbf_gb_slsc_kept(p, 257, 4, 4, 16, 3, p, 1 << 20, None) == _lib.ERANGE
+    assert L.pycbf_gb_slsc_kept(p, 64, 4, 4, 17, 3, p, 1 << 20, None) == _lib.ERANGE
+    assert L.pycbf_gb_slsc_kept(p, 64, 4, 4, 16, 4, p, 1 << 20, None) == _lib.ERANGE
+    assert L.pycbf_gb_slsc_kept(None, 64, 4, 4, 16, 3, p, 1 << 20, None) == _lib.EINVAL
+    assert L.pycbf_gb_slsc_with_kept(p, None, 1, 64, 4, 4, 16, 3, p, None) == _lib.EINVAL
+    assert L.pycbf_gb_slsc_with_kept(p, p, 1, 64, 4, 4, 17, 3, p, None) == _lib.ERANGE
+    assert L.pycbf_gb_slsc_kept_bytes(0, 4, 4) == 0

@@ -219,6 +219,47 @@ def test_slsc_both_kernels_vs_oracle(synthetic_small, nlag, nkern):
     assert np.max(np.abs(out[ok] - ref[ok])) < 2e-4
 
 
+@pytest.mark.parametrize("nrx,nlag,nkern,nframes", [(40, 16, 3, 2), (256, 5, 0, 1),
+                                                    (33, 1, 2, 1), (192, 16, 1, 3)])
+def test_slsc_kept_sets_equal_the_mask_path(nrx, nlag, nkern, nframes):
+    """The coherence from kept-element sets computed once per mask equals the
+    mask-byte path bit for bit (NaNs included), on ragged masks: random holes,
+    whole elements off, a grid whose z extent is not a multiple of the kernel."""
+    nx, nz = 9, 37
+    rng = np.random.default_rng(nrx + 7 * nkern)
+    im = rng.normal(size=(nframes, nrx, nx, nz)).astype(np.float32)
+    im[:, 3, 2, :] = 0.0  # a flat kernel: deviation below 1e-10
+    mask = (rng.random((nrx, nx, nz)) > 0.15).astype(np.uint8)
+    mask[::7] = 0
+    mask[:, 4, :] = 1
+    L = _lib.load()
+    dim = torch.as_tensor(im, device="cuda")
+    dm = torch.as_tensor(mask, device="cuda")
+    nbytes = L.pycbf_gb_slsc_kept_bytes(nrx, nx, nz)
+    assert nbytes == 4 * ((nrx + 31) // 32) * nx * nz
+    kept = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    assert L.pycbf_gb_slsc_kept(dm.data_ptr(), nrx, nx, nz, nlag, nkern, kept.data_ptr(),
+                                nbytes - 1, None) == _lib.ERANGE
+    assert L.pycbf_gb_slsc_kept(dm.data_ptr(), nrx, nx, nz, nlag, nkern, kept.data_ptr(),
+                                nbytes, None) == _lib.OK
+    a = torch.full((nframes, nx, nz), 7.0, device="cuda")
+    b = torch.full((nframes, nx, nz), 9.0, device="cuda")
+    assert L.pycbf_gb_slsc(dim.data_ptr(), dm.data_ptr(), nframes, nrx, nx, nz, nlag, nkern,
+                           a.data_ptr(), None) == _lib.OK
+    assert L.pycbf_gb_slsc_with_kept(dim.data_ptr(), kept.data_ptr(), nframes, nrx, nx, nz, nlag,
+                                     nkern, b.data_ptr(), None) == _lib.OK
+    torch.cuda.synchronize()
+    a, b = a.cpu().numpy(), b.cpu().numpy()
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    ref = oracle.slsc(im[0], mask.astype(bool), nlag, nkern)
+    assert np.array_equal(np.isnan(b[0]), np.isnan(ref))
+    ok = ~np.isnan(ref)
+    if nkern == 0:  # one-sample kernels have no deviation: every lag is NaN
+        assert not ok[ref != 0].any()
+    else:
+        assert ok.any() and np.max(np.abs(b[0][ok] - ref[ok])) < 2e-4
+
+
 def test_slsc_kernel_vs_notebook_golden(golden):
     g = golden("coherence_small.npz")
     L = _lib.load()

@@ -268,6 +268,39 @@ def test_staged_kernel_matches_generic(tabbed_small, kind, sumtype):
     assert staged.kernel_status() == 0
 
 
+@pytest.mark.parametrize("sumtype", ["tx_and_rx", "tx_only", "dmas_ssr"])
+def test_staged_mixed_decisions_match_generic(sumtype):
+    """Tiles whose taps all contribute next to tiles with delays past the
+    record, NaN delays and transmit weights straddling the threshold: the
+    staged image equals the exact-decision kernel's bit for bit, for one frame
+    (receive-block items) and for two (tile items)."""
+    rng = np.random.default_rng(17)
+    ntx, nrx, nt, npx = 5, 16, 1024, 4096
+    dt, t0 = np.float32(1 / 25e6), np.float32(2e-7)
+    base = rng.uniform(100, 900, npx) * dt
+    tautx = (base[None] + rng.uniform(0, 20, (ntx, npx)) * dt).astype(np.float32)
+    taurx = (base[None] * 0.1 + rng.uniform(0, 20, (nrx, npx)) * dt).astype(np.float32)
+    tautx[:, 1024:1100] += np.float32(nt * dt)      # past the record for one tile
+    tautx[2, 2048:2060] = np.nan                     # NaN delays in another
+    apodtx = np.ones((ntx, npx), np.float32)
+    apodtx[3, 3000:3300] = 0.004                     # one transmit below threshold / |apodrx|
+    apodrx = rng.choice(np.array([1.0, 0.5, 0.0], np.float32), size=(nrx, npx), p=[0.6, 0.3, 0.1])
+    case = dict(tautx=tautx, taurx=taurx, apodtx=apodtx, apodrx=apodrx, t0=t0, dt=dt, nt=nt)
+    rf = rng.normal(size=(2, ntx, nrx, nt)).astype(np.float32)
+    kw = dict(pixel_order="natural")
+    if sumtype == "dmas_ssr":
+        mk = lambda **k: pg.TabbedDMASBeamformer(
+            tautx=tautx, taurx=taurx, apodtx=apodtx, apodrx=apodrx, t0=float(t0), dt=float(dt),
+            nt=nt, lags=np.arange(1, nrx), lagaxis="rx", sumlags=True, dmastype="ssr", **kw, **k)
+    else:
+        mk = lambda **k: bf_for(case, "cubic", sumtype, **kw, **k)
+    staged, plain = mk(), mk(stage_channels=False)
+    assert staged._plan is not None and getattr(staged, "_fused", True)
+    for frames in (rf[0], rf):
+        np.testing.assert_array_equal(staged(frames), plain(frames))
+    assert staged.kernel_status() == 0
+
+
 def test_staged_frames_and_half_storage(tabbed_small):
     rng = np.random.default_rng(2)
     frames = np.stack([tabbed_small["rf"], rng.normal(size=tabbed_small["rf"].shape).astype(np.float32)])
