@@ -336,6 +336,82 @@ __device__ __forceinline__ float synth_rx_delay(const DasArgs &a, int r, const f
 // ---------------------------------------------------------------------------
 constexpr int kGroup = 6;  // taps whose gathers a thread keeps in flight together
 
+// Cubic taps of up to N transmits k0.. k0+nk-1 of one receive (trx, arx)
+// for the generic kernel, the decisions made as the staged kernel makes them:
+// delay sums, weights and fast quotients q = fl(fl(x - t0) * fl(1/dt)) two
+// taps per instruction; s = q - 1/2 plus 1.5 * 2^23 rounds to the knot j in
+// the sum's low bits, and where |s - j| <= 1/2 - eps_fast the fast quotient
+// and the reference's correctly rounded one floor to the same j.  A tap that
+// contributes (in range, weight past the threshold) with its quotient closer
+// to an integer is redone with the IEEE division.  Records are gathered from
+// global memory (rec: the receive's channel of transmit k0, chs elements
+// between transmits); values and the running sum are those of the generic
+// group (Kind::value, one fma per contributing tap, in transmit order), so
+// the image bits do not change.
+template <int GEOM, typename T, int N>
+__device__ __forceinline__ float generic_cubic_group(const DasArgs &a, const float *tt,
+                                                     const float *at, int nk, float trx, float arx,
+                                                     const typename CoefRec<T>::raw *rec,
+                                                     long long chs, float accr) {
+    using K = Kind<PYCBF_GB_INTERP_CUBIC, T>;
+    constexpr int NP = (N + 1) / 2;
+    const float2 trx2 = make_float2(trx, trx), arx2 = make_float2(arx, arx);
+    const float2 t02 = make_float2(a.t0, a.t0), inv2 = make_float2(a.inv_dt, a.inv_dt);
+    const float2 half2 = make_float2(0.5f, 0.5f), mag2 = make_float2(12582912.f, 12582912.f);
+    const float hmax = 0.5f - a.eps_fast;
+    float xs[N], ap[N], fj[N];
+    int jj[N];
+    unsigned hit = 0u, fix = 0u;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const int k1 = (2 * p + 1 < N) ? 2 * p + 1 : 2 * p;
+        const float2 x2 = add2_rn(make_float2(tt[2 * p], tt[k1]), trx2);
+        const float2 ap2 = (GEOM == GEOM_TABBED) ? mul2_rn(make_float2(at[2 * p], at[k1]), arx2)
+                                                 : make_float2(1.f, 1.f);
+        const float2 q2 = mul2_rn(sub2_rn(x2, t02), inv2);
+        const float2 s2 = sub2_rn(q2, half2);
+        const float2 r2 = add2_rn(s2, mag2);
+        const float2 f2 = sub2_rn(r2, mag2);
+        const float2 h2 = sub2_rn(s2, f2);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int k = 2 * p + h;
+            if (k < N) {
+                const float x = h ? x2.y : x2.x;
+                const float apod = h ? ap2.y : ap2.x;
+                const bool contrib = (k < nk) && (x >= a.t0) && (x <= a.xmax) &&
+                                     (GEOM != GEOM_TABBED || fabsf(apod) >= a.thresh);
+                const bool near = !(fabsf(h ? h2.y : h2.x) <= hmax);
+                xs[k] = x;
+                ap[k] = apod;
+                fj[k] = h ? f2.y : f2.x;
+                jj[k] = min(__float_as_int(h ? r2.y : r2.x) - 0x4B400000, a.nt - 1);
+                hit |= (unsigned)contrib << k;
+                fix |= (unsigned)(contrib && near) << k;
+            }
+        }
+    }
+    if (fix) {  // rare: a quotient next to a rounding boundary, redo it exactly
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            if ((fix >> k) & 1u) {
+                int idx;
+                K::index_exact(xs[k], a, idx);
+                jj[k] = idx;
+                fj[k] = (float)idx;
+            }
+        }
+    }
+    typename K::P pv[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+        if ((hit >> k) & 1u) pv[k] = CoefRec<T>::load(rec + (long long)k * chs + jj[k]);
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+        if ((hit >> k) & 1u) accr = fmaf(ap[k], K::value(pv[k], xs[k], fj[k], a), accr);
+    return accr;
+}
+
 // One pixel (table column i of frame f) of the generic delay-and-sum: the
 // body of das_kernel, also run by the batched kernel for each of its jobs.
 // sm: the CTA's dynamic shared memory (das_smem_bytes), a column per thread.
@@ -523,10 +599,24 @@ __device__ __forceinline__ void das_pixel(const DasArgs &a, long long i, int f, 
             }
         };
 
+        // cubic sums per receive: the fast-decision groups; the rest (census,
+        // per-tap outputs, other kinds) the general group
+        constexpr bool kFastCubic = KIND == PYCBF_GB_INTERP_CUBIC && !CENSUS &&
+                                    SUM != PYCBF_GB_SUM_NONE && SUM != PYCBF_GB_SUM_RX_ONLY;
+        using Rec = typename CoefRec<T>::raw;
+        const Rec *rec_r = static_cast<const Rec *>(a.data) + ch0;
         if (in_regs) {
 #pragma unroll
-            for (int g = 0; g < kTxReg; g += kGroup)
-                if (g < ntx) group(g, min(kGroup, ntx - g), rtau + g, rapod + g);
+            for (int g = 0; g < kTxReg; g += kGroup) {
+                if (g < ntx) {
+                    if constexpr (kFastCubic)
+                        accr = generic_cubic_group<GEOM, T, kGroup>(
+                            a, rtau + g, rapod + g, min(kGroup, ntx - g), trx, arx,
+                            rec_r + (long long)g * chs, chs, accr);
+                    else
+                        group(g, min(kGroup, ntx - g), rtau + g, rapod + g);
+                }
+            }
         } else {
             for (int g = 0; g < ntx; g += kGroup) {
                 const int nk = min(kGroup, ntx - g);
@@ -536,7 +626,11 @@ __device__ __forceinline__ void das_pixel(const DasArgs &a, long long i, int f, 
                     tt[k] = (k < nk) ? stau[(size_t)(g + k) * kBlock] : 0.f;
                     at[k] = (GEOM == GEOM_TABBED && k < nk) ? sapod[(size_t)(g + k) * kBlock] : 1.f;
                 }
-                group(g, nk, tt, at);
+                if constexpr (kFastCubic)
+                    accr = generic_cubic_group<GEOM, T, kGroup>(a, tt, at, nk, trx, arx,
+                                                                rec_r + (long long)g * chs, chs, accr);
+                else
+                    group(g, nk, tt, at);
             }
         }
 

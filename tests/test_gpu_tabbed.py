@@ -51,10 +51,11 @@ def test_block_items_deterministic_and_frame_consistent(tabbed_small):
 
 
 def test_staged_decisions_near_boundaries():
-    """The staged kernel's fast quotient and its boundary tolerance, against
-    the global-gather kernel's exact decisions, bit for bit, on delays within
-    a few ulp of every knot and half-knot (random channel data, so a tap at
-    the wrong sample changes the image)."""
+    """The fast quotients and their boundary tolerance (staged kernel; generic
+    kernel for cubic sums), on delays within a few ulp of every knot and
+    half-knot: staged against generic bit for bit, and both against the
+    oracle's exact decisions (random channel data, so a tap at the wrong
+    sample changes the image)."""
     rng = np.random.default_rng(43)
     nt, dt, t0 = 512, np.float32(1 / 31.25e6), np.float32(1.3e-6)
     npx = 8192
@@ -75,8 +76,14 @@ def test_staged_decisions_near_boundaries():
         staged = bf_for(case, kind, pixel_order="natural")
         plain = bf_for(case, kind, pixel_order="natural", stage_channels=False)
         assert staged._plan is not None
-        np.testing.assert_array_equal(staged(rf), plain(rf))
+        a = plain(rf)
+        np.testing.assert_array_equal(staged(rf), a)
         assert staged.kernel_status() == 0
+        # both take fast quotients for cubic sums: against the oracle's exact
+        # decisions a tap at the wrong knot would move its pixel by O(1)
+        ref = oracle.das_tabbed(rf, case["tautx"], case["apodtx"], case["taurx"],
+                                case["apodrx"], float(t0), float(dt), nt, interp=kind)
+        assert_image_close(a, ref, rel=1e-5, peak=1e-5, what=f"{kind} near boundaries")
 
 
 @pytest.mark.parametrize("name", CASES)
