@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(kBlock) adj_delay_kernel(const __grid_constant
     float pnt[3] = {0.f, 0.f, 0.f};
     float slow = 0.f;
     if (GEOM == GEOM_SYNTH_SLOW) {
-        for (int k = 0; k < a.ndim; ++k) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
+        for (int k = 0; k < 3; ++k) if (k < a.ndim) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
         slow = __ldg(a.slow + i);
     }
     float amax = 0.f;
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kBlock) adj_live_kernel(const __grid_constant_
             for (int t = 0; t < a.ntx; ++t)
                 amax = fmaxf(amax, fabsf(__ldg(a.apodtx + (long long)t * a.np + i)));
         else
-            for (int k = 0; k < a.ndim; ++k) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
+            for (int k = 0; k < 3; ++k) if (k < a.ndim) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
     }
     for (int r = 0; r < a.nrx; ++r) {
         bool v = false;
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(128) adj_scatter_kernel(const __grid_constant_
             in.v[2] = __ldg(a.tautx + (long long)t * np + i);
             in.v[3] = __ldg(a.taurx + (long long)r * np + i);
         } else {
-            for (int k = 0; k < a.ndim; ++k) in.v[k] = __ldg(a.geo.pnts + i * a.ndim + k);
+            for (int k = 0; k < 3; ++k) if (k < a.ndim) in.v[k] = __ldg(a.geo.pnts + i * a.ndim + k);
             in.v[3] = __ldg(a.slow + i);
         }
         in.gp = __ldg(grow + i);

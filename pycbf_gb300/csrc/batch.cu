@@ -31,7 +31,7 @@ __device__ __forceinline__ void batch_tile(const DasArgs &a, long long tile) {
     const long long chs = (long long)nrx * a.nt;
     float pnt[3] = {0.f, 0.f, 0.f};
     if (GEOM == GEOM_SYNTH)
-        for (int k = 0; k < a.ndim; ++k) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
+        for (int k = 0; k < 3; ++k) if (k < a.ndim) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
 
     float acc = 0.f;
     for (int t0 = 0; t0 < ntx; t0 += TXC) {

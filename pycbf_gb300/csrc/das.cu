@@ -63,7 +63,7 @@ __global__ void synth_rx_mask_kernel(const __grid_constant__ DasArgs a, unsigned
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.np) return;
     float pnt[3] = {0.f, 0.f, 0.f};
-    for (int k = 0; k < a.ndim; ++k) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
+    for (int k = 0; k < 3; ++k) if (k < a.ndim) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
     for (int r = 0; r < a.nrx; ++r)
         mask[(long long)r * a.np + i] = isinf(synth_rx_delay(a, r, pnt)) ? 0 : 1;
 }

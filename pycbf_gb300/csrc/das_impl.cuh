@@ -250,10 +250,13 @@ template <typename T> struct Kind<KIND_POLY_DELTA, T> : KindPoly<KIND_POLY_DELTA
 __device__ __forceinline__ void synth_dist(const float *o, const float *n, const float *p, int nd,
                                            float &mag, float &proj) {
     float m2 = 0.f, pr = 0.f;
-    for (int k = 0; k < nd; ++k) {
-        const float d = __fsub_rn(p[k], __ldg(o + k));
-        m2 = __fadd_rn(m2, __fmul_rn(d, d));
-        pr = __fadd_rn(pr, __fmul_rn(d, __ldg(n + k)));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {  // nd <= 3: constant indices keep p in registers
+        if (k < nd) {
+            const float d = __fsub_rn(p[k], __ldg(o + k));
+            m2 = __fadd_rn(m2, __fmul_rn(d, d));
+            pr = __fadd_rn(pr, __fmul_rn(d, __ldg(n + k)));
+        }
     }
     mag = __fsqrt_rn(m2);
     proj = pr;
@@ -385,7 +388,8 @@ __device__ __forceinline__ float generic_cubic_group(const DasArgs &a, const flo
                 xs[k] = x;
                 ap[k] = apod;
                 fj[k] = h ? f2.y : f2.x;
-                jj[k] = min(__float_as_int(h ? r2.y : r2.x) - 0x4B400000, a.nt - 1);
+                // a contributing tap has x <= xmax, so its fast knot is <= nt - 1
+                jj[k] = __float_as_int(h ? r2.y : r2.x) - 0x4B400000;
                 hit |= (unsigned)contrib << k;
                 fix |= (unsigned)(contrib && near) << k;
             }
@@ -412,10 +416,16 @@ __device__ __forceinline__ float generic_cubic_group(const DasArgs &a, const flo
     return accr;
 }
 
+// Where the transmit side of a pixel lives: decided per launch from ntx
+// (kTxAuto, one kernel for both), or fixed at compile time so that a kernel
+// carries the registers of one form only (kTxRegs: ntx <= kTxReg in
+// registers; kTxSmem: the thread's column of shared memory).
+constexpr int kTxAuto = 0, kTxRegs = 1, kTxSmem = 2;
+
 // One pixel (table column i of frame f) of the generic delay-and-sum: the
 // body of das_kernel, also run by the batched kernel for each of its jobs.
 // sm: the CTA's dynamic shared memory (das_smem_bytes), a column per thread.
-template <int GEOM, int KIND, int SUM, typename T, bool CENSUS>
+template <int GEOM, int KIND, int SUM, typename T, bool CENSUS, int TXM = kTxAuto>
 __device__ __forceinline__ void das_pixel(const DasArgs &a, long long i, int f, float *sm) {
     using K = Kind<KIND, T>;
     const int tid = threadIdx.x;
@@ -423,13 +433,13 @@ __device__ __forceinline__ void das_pixel(const DasArgs &a, long long i, int f, 
     const long long np = a.np;
     const int ntx = a.ntx, nrx = a.nrx;
     const long long op = a.pixel_index ? (long long)__ldg(a.pixel_index + i) : i;
-    const bool in_regs = ntx <= kTxReg;
+    const bool in_regs = TXM == kTxAuto ? ntx <= kTxReg : TXM == kTxRegs;
     const long long frame_ch = (long long)f * ntx * nrx;
     const long long chs = (long long)nrx * a.nt;  // channel stride between transmits
 
     float pnt[3] = {0.f, 0.f, 0.f};
     if (GEOM != GEOM_TABBED)
-        for (int k = 0; k < a.ndim; ++k) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
+        for (int k = 0; k < 3; ++k) if (k < a.ndim) pnt[k] = __ldg(a.geo.pnts + i * a.ndim + k);
     const float slow = (GEOM == GEOM_SYNTH_SLOW) ? __ldg(a.slow + i) : 0.f;
 
     // transmit side: registers (ntx <= kTxReg) or this thread's column of shared memory.
@@ -665,10 +675,12 @@ __device__ __forceinline__ void das_pixel(const DasArgs &a, long long i, int f, 
     }
 }
 
-template <int GEOM, int KIND, int SUM, typename T, bool CENSUS>
-__global__ void __launch_bounds__(kBlock, 4) das_kernel(const __grid_constant__ DasArgs a) {
+// Five CTAs per SM for the shared-memory form (its registers fit 96 per
+// thread; 3-D 25-transmit launches measured 5 % faster than at four).
+template <int GEOM, int KIND, int SUM, typename T, bool CENSUS, int TXM>
+__global__ void __launch_bounds__(kBlock, TXM == kTxSmem ? 5 : 4) das_kernel(const __grid_constant__ DasArgs a) {
     extern __shared__ float sm[];
-    das_pixel<GEOM, KIND, SUM, T, CENSUS>(a, (long long)blockIdx.x * kBlock + threadIdx.x,
+    das_pixel<GEOM, KIND, SUM, T, CENSUS, TXM>(a, (long long)blockIdx.x * kBlock + threadIdx.x,
                                           (int)blockIdx.y, sm);
 }
 
@@ -678,10 +690,10 @@ inline size_t das_smem_bytes(int geom, int sum, int ntx) {
     return per * (size_t)ntx * kBlock * sizeof(float);
 }
 
-template <int GEOM, int KIND, int SUM, typename T, bool CENSUS>
-cudaError_t launch_das_one(const DasArgs &a, cudaStream_t s) {
+template <int GEOM, int KIND, int SUM, typename T, bool CENSUS, int TXM>
+cudaError_t launch_das_txm(const DasArgs &a, cudaStream_t s) {
     const size_t smem = das_smem_bytes(GEOM, SUM, a.ntx);
-    auto kern = das_kernel<GEOM, KIND, SUM, T, CENSUS>;
+    auto kern = das_kernel<GEOM, KIND, SUM, T, CENSUS, TXM>;
     if (smem > 48 * 1024) {
         cudaError_t err =
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -691,6 +703,18 @@ cudaError_t launch_das_one(const DasArgs &a, cudaStream_t s) {
     dim3 grid((unsigned)bx, CENSUS ? 1u : (unsigned)a.nframes);
     kern<<<grid, kBlock, smem, s>>>(a);
     return cudaGetLastError();
+}
+
+// cubic images: a kernel per transmit-side form (fewer registers each);
+// census launches and the other kinds: one kernel for both
+template <int GEOM, int KIND, int SUM, typename T, bool CENSUS>
+cudaError_t launch_das_one(const DasArgs &a, cudaStream_t s) {
+    if constexpr (KIND == PYCBF_GB_INTERP_CUBIC && !CENSUS) {
+        if (a.ntx <= kTxReg) return launch_das_txm<GEOM, KIND, SUM, T, CENSUS, kTxRegs>(a, s);
+        return launch_das_txm<GEOM, KIND, SUM, T, CENSUS, kTxSmem>(a, s);
+    } else {
+        return launch_das_txm<GEOM, KIND, SUM, T, CENSUS, kTxAuto>(a, s);
+    }
 }
 
 template <int GEOM, int KIND, typename T>
