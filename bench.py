@@ -818,6 +818,11 @@ def run_batch_variants(a, dev, ctx):
                  "storage": storage, "taps_per_call": bb.taps,
                  "launches_per_call": bb.launches_per_replay(),
                  "config": bb.config.__dict__, "configs_timed": len(bb.timings),
+                 "best_ms_by_form": {
+                     "queue (one persistent launch)": min(
+                         (v for c, v in bb.timings.items() if c.branches == 0), default=float("nan")),
+                     "branches (every frame's own launches)": min(
+                         (v for c, v in bb.timings.items() if c.branches > 0), default=float("nan"))},
                  "setup_and_autotune_s": tune_s,
                  "roofline": roofline_of(t, nbytes, flops, ctx["hbm_peak"], ctx["fp32_peak"],
                                          "batch_spline_kernel + batch_das_kernel (queue form) or "

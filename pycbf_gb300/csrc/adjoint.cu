@@ -127,30 +127,31 @@ __global__ void __launch_bounds__(kBlock) adj_delay_kernel(const __grid_constant
         }
         float grx = 0.f;
         for (int t0 = 0; t0 < ntx; t0 += G) {
-            bool hit[G];
+            // the forward's decisions (fast knots, IEEE redo next to a boundary)
+            const int nk = min(G, ntx - t0);
+            float tt[G], ap[G], sum[G], xs[G], fj[G];
             int jj[G];
-            float am[G], bb[G], ap[G], sum[G], xs[G];
-            bool any = false;
 #pragma unroll
             for (int k = 0; k < G; ++k) {
-                const int t = t0 + k;
-                hit[k] = false;
-                jj[k] = 0;
-                am[k] = bb[k] = sum[k] = xs[k] = 0.f;
+                tt[k] = (k < nk) ? stau[(size_t)(t0 + k) * kBlock] : 0.f;
+                sum[k] = 0.f;
+            }
+            unsigned inr, near;
+            cubic_knots<G>(a, tt, trx, xs, jj, fj, inr, near);
+            unsigned hitm = inr & ((1u << nk) - 1u);
+#pragma unroll
+            for (int k = 0; k < G; ++k) {
                 ap[k] = 1.f;
-                if (t < ntx) {
-                    const float x = __fadd_rn(stau[(size_t)t * kBlock], trx);
-                    xs[k] = x;
-                    bool ok = true;
-                    if (GEOM == GEOM_TABBED) {
-                        ap[k] = __fmul_rn(sw[(size_t)t * kBlock], arx);
-                        ok = fabsf(ap[k]) >= a.thresh;
-                    }
-                    hit[k] = ok && cubic_tap(x, a, jj[k], am[k], bb[k]);
-                    any |= hit[k];
+                if (GEOM == GEOM_TABBED && k < nk) {
+                    ap[k] = __fmul_rn(sw[(size_t)(t0 + k) * kBlock], arx);
+                    if (!(fabsf(ap[k]) >= a.thresh)) hitm &= ~(1u << k);
                 }
             }
-            if (!any) continue;
+            if (!hitm) continue;
+            if (hitm & near) cubic_knots_exact<G>(a, xs, jj, fj, hitm & near);
+            bool hit[G];
+#pragma unroll
+            for (int k = 0; k < G; ++k) hit[k] = (hitm >> k) & 1u;
             for (int f = 0; f < nfr; ++f) {
                 const float gp = __ldg(g.gk + grad_row(SUM, f, r, nrx) * np + i);
                 float4 c[G];
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(kBlock) adj_delay_kernel(const __grid_constant
 #pragma unroll
                 for (int k = 0; k < G; ++k)
                     if (hit[k])
-                        sum[k] = fmaf(gp, Kind<PYCBF_GB_INTERP_CUBIC, T>::slope(c[k], xs[k], (float)jj[k], a),
+                        sum[k] = fmaf(gp, Kind<PYCBF_GB_INTERP_CUBIC, T>::slope(c[k], xs[k], fj[k], a),
                                       sum[k]);
             }
 #pragma unroll
