@@ -398,17 +398,17 @@ __device__ __forceinline__ void cubic_knots_exact(const DasArgs &a, const float 
 }
 
 // Cubic taps of up to N transmits k0.. k0+nk-1 of one receive (trx, arx)
-// for the generic kernel.  The knots are the fast ones of cubic_knots,
-// computed inline: a tap that contributes (in range, weight past the
-// threshold) with its quotient near an integer takes the IEEE division in a
-// branch of its own, which a warp rarely enters.  Every tap then gathers a
-// record -- knot clamped into the channel, padding taps reading the group's
-// last channel -- and a select keeps the contributing ones, so no load or
-// add is predicated on a bit mask.  Records come from global memory (rec:
-// the receive's channel of transmit k0, chs elements between transmits);
-// values and the running sum are those of the generic group (Kind::value,
-// one fma per contributing tap, in transmit order), so the image bits do
-// not depend on which kernel ran.
+// for the generic kernel, the decisions made as the staged kernel makes them:
+// delay sums, weights and fast quotients q = fl(fl(x - t0) * fl(1/dt)) two
+// taps per instruction; s = q - 1/2 plus 1.5 * 2^23 rounds to the knot j in
+// the sum's low bits, and where |s - j| <= 1/2 - eps_fast the fast quotient
+// and the reference's correctly rounded one floor to the same j.  A tap that
+// contributes (in range, weight past the threshold) with its quotient closer
+// to an integer is redone with the IEEE division.  Records are gathered from
+// global memory (rec: the receive's channel of transmit k0, chs elements
+// between transmits); values and the running sum are those of the generic
+// group (Kind::value, one fma per contributing tap, in transmit order), so
+// the image bits do not change.
 template <int GEOM, typename T, int N>
 __device__ __forceinline__ float generic_cubic_group(const DasArgs &a, const float *tt,
                                                      const float *at, int nk, float trx, float arx,
@@ -420,10 +420,9 @@ __device__ __forceinline__ float generic_cubic_group(const DasArgs &a, const flo
     const float2 t02 = make_float2(a.t0, a.t0), inv2 = make_float2(a.inv_dt, a.inv_dt);
     const float2 half2 = make_float2(0.5f, 0.5f), mag2 = make_float2(12582912.f, 12582912.f);
     const float hmax = 0.5f - a.eps_fast;
-    const unsigned jmax = (unsigned)(a.nt - 1);
     float xs[N], ap[N], fj[N];
-    unsigned jj[N];
-    bool ok[N];
+    int jj[N];
+    unsigned hit = 0u, fix = 0u;
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
         const int k1 = (2 * p + 1 < N) ? 2 * p + 1 : 2 * p;
@@ -441,31 +440,37 @@ __device__ __forceinline__ float generic_cubic_group(const DasArgs &a, const flo
             if (k < N) {
                 const float x = h ? x2.y : x2.x;
                 const float apod = h ? ap2.y : ap2.x;
-                const bool c = (k < nk) && (x >= a.t0) && (x <= a.xmax) &&
-                               (GEOM != GEOM_TABBED || fabsf(apod) >= a.thresh);
-                int j = __float_as_int(h ? r2.y : r2.x) - 0x4B400000;
-                float f = h ? f2.y : f2.x;
-                if (c && !(fabsf(h ? h2.y : h2.x) <= hmax)) {
-                    K::index_exact(x, a, j);  // next to a rounding boundary: the IEEE quotient
-                    f = (float)j;
-                }
+                const bool contrib = (k < nk) && (x >= a.t0) && (x <= a.xmax) &&
+                                     (GEOM != GEOM_TABBED || fabsf(apod) >= a.thresh);
+                const bool near = !(fabsf(h ? h2.y : h2.x) <= hmax);
                 xs[k] = x;
                 ap[k] = apod;
-                fj[k] = f;
-                jj[k] = min((unsigned)j, jmax);  // every gather inside the channel
-                ok[k] = c;
+                fj[k] = h ? f2.y : f2.x;
+                // a contributing tap has x <= xmax, so its fast knot is <= nt - 1
+                jj[k] = __float_as_int(h ? r2.y : r2.x) - 0x4B400000;
+                hit |= (unsigned)contrib << k;
+                fix |= (unsigned)(contrib && near) << k;
+            }
+        }
+    }
+    if (fix) {  // rare: a quotient next to a rounding boundary, redo it exactly
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            if ((fix >> k) & 1u) {
+                int idx;
+                K::index_exact(xs[k], a, idx);
+                jj[k] = idx;
+                fj[k] = (float)idx;
             }
         }
     }
     typename K::P pv[N];
 #pragma unroll
     for (int k = 0; k < N; ++k)
-        pv[k] = CoefRec<T>::load(rec + (long long)min(k, nk - 1) * chs + jj[k]);
+        if ((hit >> k) & 1u) pv[k] = CoefRec<T>::load(rec + (long long)k * chs + jj[k]);
 #pragma unroll
-    for (int k = 0; k < N; ++k) {
-        const float c = fmaf(ap[k], K::value(pv[k], xs[k], fj[k], a), accr);
-        accr = ok[k] ? c : accr;
-    }
+    for (int k = 0; k < N; ++k)
+        if ((hit >> k) & 1u) accr = fmaf(ap[k], K::value(pv[k], xs[k], fj[k], a), accr);
     return accr;
 }
 
