@@ -201,7 +201,7 @@ slsc_kept_kernel(const unsigned char *__restrict__ mask, int nrx, int nx, int nz
 // PRE: the kept bit sets come from slsc_kept_kernel's array (kept_in), else
 // from the mask bytes.
 template <bool PRE>
-__global__ void __launch_bounds__(128, 2)
+__global__ void __launch_bounds__(128, 3)  // 3 CTAs (168 registers): 1.09 ms against 1.30 at 2
 slsc_reg_kernel(const float *__restrict__ im, const unsigned char *__restrict__ mask,
                 const unsigned *__restrict__ kept_in, int nrx, int nx, int nz, int nlag, int nkern,
                 float *__restrict__ out) {

@@ -338,6 +338,11 @@ __device__ __forceinline__ float synth_rx_delay(const DasArgs &a, int r, const f
 // the kernel
 // ---------------------------------------------------------------------------
 constexpr int kGroup = 6;  // taps whose gathers a thread keeps in flight together
+// the same for the fast cubic group over transmits in shared memory: six
+// for float32 records; four for 16-bit records, whose (y, z) interpolation
+// needs more registers (groups of six cost the 3-D 25-transmit launch 11 %
+// in occupancy)
+template <typename T> constexpr int kGroupSmem = CoefRec<T>::kPoly ? 6 : 4;
 
 // Fast knots of N cubic taps x_k = fl(tt_k + trx), decided as the staged
 // kernel decides them: delay sums and quotients q = fl(fl(x - t0) * fl(1/dt))
@@ -686,19 +691,31 @@ __device__ __forceinline__ void das_pixel(const DasArgs &a, long long i, int f, 
                 }
             }
         } else {
-            for (int g = 0; g < ntx; g += kGroup) {
-                const int nk = min(kGroup, ntx - g);
-                float tt[kGroup], at[kGroup];
+            if constexpr (kFastCubic) {
+                for (int g = 0; g < ntx; g += kGroupSmem<T>) {
+                    const int nk = min(kGroupSmem<T>, ntx - g);
+                    float tt[kGroupSmem<T>], at[kGroupSmem<T>];
 #pragma unroll
-                for (int k = 0; k < kGroup; ++k) {
-                    tt[k] = (k < nk) ? stau[(size_t)(g + k) * kBlock] : 0.f;
-                    at[k] = (GEOM == GEOM_TABBED && k < nk) ? sapod[(size_t)(g + k) * kBlock] : 1.f;
+                    for (int k = 0; k < kGroupSmem<T>; ++k) {
+                        tt[k] = (k < nk) ? stau[(size_t)(g + k) * kBlock] : 0.f;
+                        at[k] = (GEOM == GEOM_TABBED && k < nk) ? sapod[(size_t)(g + k) * kBlock]
+                                                                : 1.f;
+                    }
+                    accr = generic_cubic_group<GEOM, T, kGroupSmem<T>>(
+                        a, tt, at, nk, trx, arx, rec_r + (long long)g * chs, chs, accr);
                 }
-                if constexpr (kFastCubic)
-                    accr = generic_cubic_group<GEOM, T, kGroup>(a, tt, at, nk, trx, arx,
-                                                                rec_r + (long long)g * chs, chs, accr);
-                else
+            } else {
+                for (int g = 0; g < ntx; g += kGroup) {
+                    const int nk = min(kGroup, ntx - g);
+                    float tt[kGroup], at[kGroup];
+#pragma unroll
+                    for (int k = 0; k < kGroup; ++k) {
+                        tt[k] = (k < nk) ? stau[(size_t)(g + k) * kBlock] : 0.f;
+                        at[k] = (GEOM == GEOM_TABBED && k < nk) ? sapod[(size_t)(g + k) * kBlock]
+                                                                : 1.f;
+                    }
                     group(g, nk, tt, at);
+                }
             }
         }
 

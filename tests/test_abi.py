@@ -162,7 +162,7 @@ def test_adjoint_workspace_bytes():
     grad = lambda np_: (2 * 3 * np_ * 4 + 255) // 256 * 256  # gathered upstream gradient
     live = lambda np_: (3 * ((np_ + 127) // 128) + 255) // 256 * 256  # receive x tile flags
     n = L.pycbf_gb_adjoint_workspace_bytes(ct.byref(info), 100000)
-    parts = min(48, (2048 + nch - 1) // nch)
+    parts = min(100000 // 2048, (11264 + nch - 1) // nch, 64)
     assert n == grad(100000) + parts * nch * 2 * lp * 4 + live(100000)
     assert L.pycbf_gb_adjoint_workspace_bytes(ct.byref(info), 100) == \
         grad(100) + nch * 2 * lp * 4 + live(100)
