@@ -92,9 +92,8 @@ typedef struct pycbf_gb_rfinfo {
  * call:
  *   ntx, nrx <= 2^20; nt < 2^22; nframes <= 65535; np < 2^31;
  *   cubic interpolation (the spline prefilter): nt <= 18000;
- *   delay-and-sum: ntx <= 227 for Tabbed (151 with PYCBF_GB_SUM_RX_ONLY),
- *   ntx <= 454 for Synthetic (227 with PYCBF_GB_SUM_RX_ONLY), the per-pixel
- *   transmit delays and weights living in shared memory. */
+ *   delay-and-sum: ntx <= 454 (227 with PYCBF_GB_SUM_RX_ONLY), the per-pixel
+ *   transmit delays living in shared memory. */
 
 /* Synthetic-point geometry, all device pointers (float32).  The fields follow
  * the Synthetic dataclass (pycbf/__bf_base_classes__.py:166-178).  The acos
@@ -498,6 +497,7 @@ typedef struct pycbf_gb_batch_info {
     int max_nt;
     int tiles_per_item;
     int max_ntx;
+    int dtypes;                     /* bit 1 << dtype for every storage type present  */
 } pycbf_gb_batch_info;
 
 size_t pycbf_gb_batch_plan_bytes(const pycbf_gb_batch_job *jobs, int njobs, int tiles_per_item);

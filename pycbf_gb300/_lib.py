@@ -68,7 +68,8 @@ class BatchJob(ct.Structure):
 class BatchInfo(ct.Structure):
     """pycbf_gb_batch_info: what pycbf_gb_batch_run needs from the plan."""
     _fields_ = [("nitems", ct.c_longlong), ("nchannels", ct.c_longlong), ("njobs", ct.c_int),
-                ("max_nt", ct.c_int), ("tiles_per_item", ct.c_int), ("max_ntx", ct.c_int)]
+                ("max_nt", ct.c_int), ("tiles_per_item", ct.c_int), ("max_ntx", ct.c_int),
+                ("dtypes", ct.c_int)]
 
 
 class GPUError(RuntimeError):

@@ -81,7 +81,8 @@ void fill_time_axis(DasArgs &a, const pycbf_gb_rfinfo *rf) {
 
 bool das_shape_ok(int geom, int sumtype, long long ntx) {
     if (ntx <= 16) return true;
-    const size_t per = (geom == GEOM_TABBED ? 2 : 1) + (sumtype == PYCBF_GB_SUM_RX_ONLY ? 1 : 0);
+    (void)geom;
+    const size_t per = 1 + (sumtype == PYCBF_GB_SUM_RX_ONLY ? 1 : 0);  // das_smem_bytes
     return per * (size_t)ntx * 128 * sizeof(float) <= 227 * 1024;
 }
 
@@ -705,10 +706,11 @@ int pycbf_gb_batch_plan(const pycbf_gb_batch_job *jobs, int njobs, int tiles_per
     std::vector<int2> items;
     std::vector<double> cost;
     long long ch0 = 0;
-    int max_nt = 1, max_ntx = 1;
+    int max_nt = 1, max_ntx = 1, dtypes = 0;
     for (int k = 0; k < njobs; ++k) {
         const pycbf_gb_batch_job &j = jobs[k];
         BatchJob &b = desc[(size_t)k];
+        dtypes |= 1 << j.rf.dtype;
         b = BatchJob{};
         fill_time_axis(b.a, &j.rf);
         b.a.data = j.coef;
@@ -768,6 +770,7 @@ int pycbf_gb_batch_plan(const pycbf_gb_batch_job *jobs, int njobs, int tiles_per
     info->max_nt = max_nt;
     info->tiles_per_item = tiles_per_item;
     info->max_ntx = max_ntx;
+    info->dtypes = dtypes;
     // shared-memory sizes of the batched prefilter and delay-and-sum, set outside any capture
     st = cuda_status(prepare_batch_das(max_ntx));
     if (st) return st;
@@ -794,7 +797,7 @@ int pycbf_gb_batch_run(const void *plan, const pycbf_gb_batch_info *info, int tx
                                              false));
     if (st) return st;
     return cuda_status(launch_batch_das(jobs, items, info->nitems, info->tiles_per_item, counter,
-                                        tx_chunk, ctas, s, info->max_ntx));
+                                        tx_chunk, ctas, s, info->max_ntx, info->dtypes));
 }
 
 }  // extern "C"

@@ -204,6 +204,51 @@ batch_das_full_kernel(const BatchJob *__restrict__ jobs, const int2 *__restrict_
     }
 }
 
+// The same for a batch of one storage type T: each pixel runs the single-frame
+// kernels' cubic body with its transmit-side form fixed per job (registers for
+// ntx <= kTxReg, the column of shared memory beyond), so the kernel carries the
+// paths of one storage type only (the mixed kernel above spills).
+// each form behind a call of its own, so the compiler allocates its registers
+// apart from the others' (one call per pixel, not per tap)
+template <int GEOM, typename T, int TXM>
+__device__ __noinline__ void batch_pixel(const DasArgs &a, long long i, float *sm) {
+    das_pixel<GEOM, PYCBF_GB_INTERP_CUBIC, PYCBF_GB_SUM_TX_AND_RX, T, false, TXM>(a, i, 0, sm);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock, 4)
+batch_das_typed_kernel(const BatchJob *__restrict__ jobs, const int2 *__restrict__ items,
+                       long long nitems, int tiles_per_item, unsigned long long *counter) {
+    extern __shared__ float sm[];
+    __shared__ __align__(16) BatchJob s_job;
+    __shared__ long long s_k;
+    constexpr int kWords = (int)(sizeof(BatchJob) / sizeof(int));
+    for (;;) {
+        if (threadIdx.x == 0) s_k = (long long)atomicAdd(counter, 1ULL);
+        __syncthreads();
+        const long long k = s_k;
+        if (k >= nitems) break;
+        const int2 it = __ldg(items + k);
+        const int *src = reinterpret_cast<const int *>(jobs + it.x);
+        int *dst = reinterpret_cast<int *>(&s_job);
+        for (int w = threadIdx.x; w < kWords; w += blockDim.x) dst[w] = __ldg(src + w);
+        __syncthreads();
+        const bool regs = s_job.a.ntx <= kTxReg;
+        const bool tabbed = s_job.geom == GEOM_TABBED;
+        for (int sub = 0; sub < tiles_per_item; ++sub) {
+            const long long i = ((long long)it.y * tiles_per_item + sub) * kBlock + threadIdx.x;
+            if (tabbed) {
+                if (regs) batch_pixel<GEOM_TABBED, T, kTxRegs>(s_job.a, i, sm);
+                else batch_pixel<GEOM_TABBED, T, kTxSmem>(s_job.a, i, sm);
+            } else {
+                if (regs) batch_pixel<GEOM_SYNTH, T, kTxRegs>(s_job.a, i, sm);
+                else batch_pixel<GEOM_SYNTH, T, kTxSmem>(s_job.a, i, sm);
+            }
+        }
+        __syncthreads();  // every thread is done with s_job and s_k
+    }
+}
+
 }  // namespace
 
 size_t batch_full_smem_bytes(int max_ntx) {
@@ -213,20 +258,42 @@ size_t batch_full_smem_bytes(int max_ntx) {
 cudaError_t prepare_batch_das(int max_ntx) {
     const size_t smem = batch_full_smem_bytes(max_ntx);
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
-    return cudaFuncSetAttribute(batch_das_full_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)std::max<size_t>(smem, 48 * 1024));
+    const int lim = (int)std::max<size_t>(smem, 48 * 1024);
+    cudaError_t err =
+        cudaFuncSetAttribute(batch_das_full_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(batch_das_typed_kernel<float>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(batch_das_typed_kernel<__half>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(batch_das_typed_kernel<__nv_bfloat16>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    return err;
 }
 
 cudaError_t launch_batch_das(const BatchJob *jobs, const int2 *items, long long nitems,
                              int tiles_per_item, unsigned long long *counter, int tx_chunk,
-                             int ctas, cudaStream_t s, int max_ntx) {
+                             int ctas, cudaStream_t s, int max_ntx, int dtypes) {
     cudaError_t err = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
     if (err != cudaSuccess) return err;
     if (nitems <= 0) return cudaSuccess;
     const unsigned grid = (unsigned)std::max(1, ctas);
     if (tx_chunk == 0) {  // shared-memory size set by prepare_batch_das, outside any capture
-        batch_das_full_kernel<<<grid, kBlock, batch_full_smem_bytes(max_ntx), s>>>(
-            jobs, items, nitems, tiles_per_item, counter);
+        const size_t smem = batch_full_smem_bytes(max_ntx);
+        if (dtypes == 1 << PYCBF_GB_F32)
+            batch_das_typed_kernel<float><<<grid, kBlock, smem, s>>>(jobs, items, nitems,
+                                                                     tiles_per_item, counter);
+        else if (dtypes == 1 << PYCBF_GB_F16)
+            batch_das_typed_kernel<__half><<<grid, kBlock, smem, s>>>(jobs, items, nitems,
+                                                                      tiles_per_item, counter);
+        else if (dtypes == 1 << PYCBF_GB_BF16)
+            batch_das_typed_kernel<__nv_bfloat16><<<grid, kBlock, smem, s>>>(
+                jobs, items, nitems, tiles_per_item, counter);
+        else
+            batch_das_full_kernel<<<grid, kBlock, smem, s>>>(jobs, items, nitems, tiles_per_item,
+                                                             counter);
         return cudaGetLastError();
     }
     switch (tx_chunk) {

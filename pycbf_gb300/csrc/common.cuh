@@ -261,10 +261,12 @@ cudaError_t launch_batch_spline(const BatchJob *jobs, int njobs, long long nch_t
 // items: (job, first tile / tiles_per_item) pairs in processing order; counter:
 // the work-queue head (zero before the launch)
 // tx_chunk 0: the single-frame kernel's per-pixel body (dynamic shared memory for
-// max_ntx transmits, its limit set by prepare_batch_das outside any capture)
+// max_ntx transmits, its limit set by prepare_batch_das outside any capture);
+// dtypes: bit 1 << dtype of each storage type in the batch (one type: a kernel
+// with that type's paths only)
 cudaError_t launch_batch_das(const BatchJob *jobs, const int2 *items, long long nitems,
                              int tiles_per_item, unsigned long long *counter, int tx_chunk,
-                             int ctas, cudaStream_t s, int max_ntx);
+                             int ctas, cudaStream_t s, int max_ntx, int dtypes);
 cudaError_t prepare_batch_das(int max_ntx);
 
 // ---------------------------------------------------------------------------

@@ -509,8 +509,10 @@ __device__ __forceinline__ void das_pixel(const DasArgs &a, long long i, int f, 
     // Synthetic masks travel as +inf delays, which the range test rejects.
     float rtau[kTxReg], rapod[kTxReg], racc[kTxReg];
     float *stau = sm + tid;
-    float *sapod = stau + (size_t)ntx * kBlock;
-    float *sacc = sapod + (GEOM == GEOM_TABBED ? (size_t)ntx * kBlock : 0);
+    // Tabbed transmit weights beyond kTxReg are read from the table per
+    // receive (L1-resident: a tile's rows), which halves the shared memory of
+    // the column form and so raises the CTAs per SM (two -> five at 75 transmits)
+    float *sacc = stau + (size_t)ntx * kBlock;
     float amax = 0.f;  // max |apodtx| of this pixel, for the exact receive-level reject
     auto tx_side = [&](int t, float &tau, float &apod) {
         if (GEOM == GEOM_TABBED) {
@@ -542,7 +544,6 @@ __device__ __forceinline__ void das_pixel(const DasArgs &a, long long i, int f, 
             float tau, apod;
             tx_side(k, tau, apod);
             stau[(size_t)k * kBlock] = tau;
-            if (GEOM == GEOM_TABBED) sapod[(size_t)k * kBlock] = apod;
             if (SUM == PYCBF_GB_SUM_RX_ONLY) sacc[(size_t)k * kBlock] = 0.f;
         }
     }
@@ -698,8 +699,9 @@ __device__ __forceinline__ void das_pixel(const DasArgs &a, long long i, int f, 
 #pragma unroll
                     for (int k = 0; k < kGroupSmem<T>; ++k) {
                         tt[k] = (k < nk) ? stau[(size_t)(g + k) * kBlock] : 0.f;
-                        at[k] = (GEOM == GEOM_TABBED && k < nk) ? sapod[(size_t)(g + k) * kBlock]
-                                                                : 1.f;
+                        at[k] = (GEOM == GEOM_TABBED && k < nk)
+                                    ? __ldg(a.apodtx + (long long)(g + k) * np + i)
+                                    : 1.f;
                     }
                     accr = generic_cubic_group<GEOM, T, kGroupSmem<T>>(
                         a, tt, at, nk, trx, arx, rec_r + (long long)g * chs, chs, accr);
@@ -711,8 +713,9 @@ __device__ __forceinline__ void das_pixel(const DasArgs &a, long long i, int f, 
 #pragma unroll
                     for (int k = 0; k < kGroup; ++k) {
                         tt[k] = (k < nk) ? stau[(size_t)(g + k) * kBlock] : 0.f;
-                        at[k] = (GEOM == GEOM_TABBED && k < nk) ? sapod[(size_t)(g + k) * kBlock]
-                                                                : 1.f;
+                        at[k] = (GEOM == GEOM_TABBED && k < nk)
+                                    ? __ldg(a.apodtx + (long long)(g + k) * np + i)
+                                    : 1.f;
                     }
                     group(g, nk, tt, at);
                 }
@@ -759,9 +762,11 @@ __global__ void __launch_bounds__(kBlock, TXM == kTxSmem ? 5 : 4) das_kernel(con
                                           (int)blockIdx.y, sm);
 }
 
+// the column form: per transmit the delay (and the RX_ONLY accumulator)
 inline size_t das_smem_bytes(int geom, int sum, int ntx) {
+    (void)geom;
     if (ntx <= kTxReg) return 0;
-    size_t per = (geom == GEOM_TABBED ? 2 : 1) + (sum == PYCBF_GB_SUM_RX_ONLY ? 1 : 0);
+    const size_t per = 1 + (sum == PYCBF_GB_SUM_RX_ONLY ? 1 : 0);
     return per * (size_t)ntx * kBlock * sizeof(float);
 }
 

@@ -84,8 +84,8 @@ def test_size_limits_return_erange():
 
     assert tabbed(_info(ntx=(1 << 20) + 1)) == _lib.ERANGE
     assert tabbed(_info(nrx=(1 << 20) + 1)) == _lib.ERANGE
-    assert tabbed(_info(ntx=228)) == _lib.ERANGE
-    assert tabbed(_info(ntx=152), sumtype=2) == _lib.ERANGE
+    assert tabbed(_info(ntx=455)) == _lib.ERANGE
+    assert tabbed(_info(ntx=228), sumtype=2) == _lib.ERANGE
     cubic = _info(nt=18001)
     need = L.pycbf_gb_workspace_bytes(ct.byref(cubic), _lib.INTERP["cubic"])
     assert tabbed(cubic, interp=_lib.INTERP["cubic"], ws=p, wsb=need) == _lib.ERANGE

@@ -317,6 +317,34 @@ def test_staged_frames_and_half_storage(tabbed_small):
         np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("sumtype", ["tx_and_rx", "tx_only", "rx_only", "none"])
+def test_many_transmits_column_form_vs_oracle(sumtype):
+    """ntx > 12: the generic kernel's transmit delays in shared memory and the
+    transmit weights read from the table per receive; weights straddling the
+    threshold and delays past the record.  Tap census bit-exact, images within
+    the parity bar."""
+    rng = np.random.default_rng(29)
+    ntx, nrx, nt, npx = 23, 10, 1024, 3000
+    dt = np.float32(1 / 25e6)
+    base = rng.uniform(50, 900, npx) * dt
+    case = dict(tautx=(base[None] + rng.uniform(0, 60, (ntx, npx)) * dt).astype(np.float32),
+                taurx=(base[None] * 0.2 + rng.uniform(0, 40, (nrx, npx)) * dt).astype(np.float32),
+                apodtx=rng.choice(np.array([1.0, 0.3, 0.02, 0.004], np.float32), size=(ntx, npx)),
+                apodrx=rng.choice(np.array([1.0, 0.6, 0.0], np.float32), size=(nrx, npx)),
+                t0=np.float32(1e-7), dt=dt, nt=nt)
+    case["tautx"][:, :40] += np.float32(nt * dt)
+    case["rf"] = rng.normal(size=(ntx, nrx, nt)).astype(np.float32)
+    bf = bf_for(case, "cubic", sumtype, pixel_order="natural")
+    assert bf._plan is None  # ntx > 12: the generic kernel
+    assert_image_close(bf(case["rf"]), oracle_for(case, "cubic", sumtype, threads=NCPU),
+                       what=f"ntx {ntx} {sumtype}")
+    cnt, isum = bf.tap_census()
+    ok_cnt, ok_isum = oracle.tap_census(case["tautx"], case["apodtx"], case["taurx"],
+                                        case["apodrx"], float(case["t0"]), float(dt), nt)
+    np.testing.assert_array_equal(cnt.cpu().numpy(), ok_cnt)
+    np.testing.assert_array_equal(isum.cpu().numpy(), ok_isum)
+
+
 def test_staged_kernel_unstaged_receives():
     """Delays spread over the whole record: no window fits a stage, so every
     receive takes the kernel's global-gather path (with padded transmits)."""
