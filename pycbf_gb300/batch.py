@@ -47,7 +47,7 @@ class BatchConfig:
 # the queue form's own fields first, the branch counts last, so that both forms
 # are searched before one of them wins the coordinate search
 SEARCH_SPACE = dict(tx_chunk=(12, 0, 8, 4), tiles_per_item=(1, 2, 4), order=(1, 0),
-                    ctas_per_sm=(4, 3, 2), branches=(0, 4, 8, 16))
+                    ctas_per_sm=(4, 5, 3, 2), branches=(0, 4, 8, 16))
 _TUNED: dict = {}
 
 
