@@ -205,54 +205,61 @@ batch_das_full_kernel(const BatchJob *__restrict__ jobs, const int2 *__restrict_
 }
 
 // The same for a batch of one storage type T: each pixel runs the single-frame
-// kernels' cubic body with its transmit-side form fixed per job (registers for
-// ntx <= kTxReg, the column of shared memory beyond), so the kernel carries the
-// paths of one storage type only (the mixed kernel above spills).
-// each form behind a call of its own, so the compiler allocates its registers
-// apart from the others' (one call per pixel, not per tap)
-template <int GEOM, typename T, int TXM>
+// kernels' cubic body in its shared-memory column form, whatever the job's
+// ntx (the column is sized for the batch's largest ntx; per-receive sums are
+// sequential over transmits either way, so the images are those of the
+// single-frame calls bit for bit).  The kernel carries the paths of one
+// storage type only -- the mixed kernel above spills -- and each geometry's
+// body sits behind a call of its own, so the compiler allocates its registers
+// apart from the other's (one call per pixel, not per tap).  A CTA copies a
+// job's descriptor only when its next item belongs to another job.  Measured
+// on the 64-frame batch: with the register form as well for ntx <= 12 the
+// float32 kernel took 43 ms, without it 38 ms.
+template <int GEOM, typename T>
 __device__ __noinline__ void batch_pixel(const DasArgs &a, long long i, float *sm) {
-    das_pixel<GEOM, PYCBF_GB_INTERP_CUBIC, PYCBF_GB_SUM_TX_AND_RX, T, false, TXM>(a, i, 0, sm);
+    das_pixel<GEOM, PYCBF_GB_INTERP_CUBIC, PYCBF_GB_SUM_TX_AND_RX, T, false, kTxSmem>(a, i, 0, sm);
 }
 
+// five CTAs per SM for 16-bit records (42 against 43 ms), four for float32
+// records, whose body spills under five's register cap (47 against 38 ms)
 template <typename T>
-__global__ void __launch_bounds__(kBlock, 4)
+__global__ void __launch_bounds__(kBlock, CoefRec<T>::kPoly ? 4 : 5)
 batch_das_typed_kernel(const BatchJob *__restrict__ jobs, const int2 *__restrict__ items,
                        long long nitems, int tiles_per_item, unsigned long long *counter) {
     extern __shared__ float sm[];
     __shared__ __align__(16) BatchJob s_job;
     __shared__ long long s_k;
     constexpr int kWords = (int)(sizeof(BatchJob) / sizeof(int));
+    int cur = -1;  // the job whose descriptor s_job holds
     for (;;) {
         if (threadIdx.x == 0) s_k = (long long)atomicAdd(counter, 1ULL);
         __syncthreads();
         const long long k = s_k;
         if (k >= nitems) break;
         const int2 it = __ldg(items + k);
-        const int *src = reinterpret_cast<const int *>(jobs + it.x);
-        int *dst = reinterpret_cast<int *>(&s_job);
-        for (int w = threadIdx.x; w < kWords; w += blockDim.x) dst[w] = __ldg(src + w);
-        __syncthreads();
-        const bool regs = s_job.a.ntx <= kTxReg;
+        if (it.x != cur) {  // the same in every thread: the barrier below is uniform
+            const int *src = reinterpret_cast<const int *>(jobs + it.x);
+            int *dst = reinterpret_cast<int *>(&s_job);
+            for (int w = threadIdx.x; w < kWords; w += blockDim.x) dst[w] = __ldg(src + w);
+            __syncthreads();
+            cur = it.x;
+        }
         const bool tabbed = s_job.geom == GEOM_TABBED;
         for (int sub = 0; sub < tiles_per_item; ++sub) {
             const long long i = ((long long)it.y * tiles_per_item + sub) * kBlock + threadIdx.x;
-            if (tabbed) {
-                if (regs) batch_pixel<GEOM_TABBED, T, kTxRegs>(s_job.a, i, sm);
-                else batch_pixel<GEOM_TABBED, T, kTxSmem>(s_job.a, i, sm);
-            } else {
-                if (regs) batch_pixel<GEOM_SYNTH, T, kTxRegs>(s_job.a, i, sm);
-                else batch_pixel<GEOM_SYNTH, T, kTxSmem>(s_job.a, i, sm);
-            }
+            if (tabbed) batch_pixel<GEOM_TABBED, T>(s_job.a, i, sm);
+            else batch_pixel<GEOM_SYNTH, T>(s_job.a, i, sm);
         }
-        __syncthreads();  // every thread is done with s_job and s_k
+        __syncthreads();  // every thread is done with s_k (and, before a new job, s_job)
     }
 }
 
 }  // namespace
 
+// the column of every job's transmit delays (the typed kernel uses the column
+// form for every ntx, so this holds even when max_ntx <= kTxReg)
 size_t batch_full_smem_bytes(int max_ntx) {
-    return das_smem_bytes(GEOM_TABBED, PYCBF_GB_SUM_TX_AND_RX, max_ntx);
+    return (size_t)std::max(max_ntx, 1) * kBlock * sizeof(float);
 }
 
 cudaError_t prepare_batch_das(int max_ntx) {

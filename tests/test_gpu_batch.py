@@ -61,6 +61,36 @@ def test_batch_matches_single_frames(batch, cfg):
             assert _rel(o, s) <= 1e-6, (k, _rel(o, s))
 
 
+@pytest.mark.parametrize("storage", ["float32", "float16", "bfloat16"])
+@pytest.mark.parametrize("big", [False, True])
+def test_one_storage_type_queue_matches_single_frames(batch, storage, big):
+    """A batch of one storage type runs the queue kernel compiled for that type
+    alone (the shared-memory column form for every ntx), with all jobs at
+    ntx <= 12 (big=False: a column of at most 12 transmits) or with larger
+    ones: bitwise the single-frame images."""
+    small = dict(xlim=(-3e-3, 3e-3), zlim=(4e-3, 14e-3), n_speckle=150, n_points=3)
+    wa = phantom.linear_pw_tabbed(nele=16, nsteer=3, nt=512, nx=24, nz=40, device="cuda", **small)
+    wc = phantom.linear_pw_synthetic(nele=24, nsteer=5, nt=1024, nx=20, nz=32, device="cuda",
+                                     **small)
+    entries = [(_tabbed(wa, storage), wa), (_synth(wc, storage), wc),
+               (_tabbed(wa, storage, order="natural"), wa)]
+    if big:
+        wb = phantom.linear_pw_tabbed(nele=24, nsteer=13, nt=1024, nx=16, nz=24, device="cuda",
+                                      **small)
+        wd = phantom.linear_pw_synthetic(nele=32, nsteer=15, nt=2048, nx=12, nz=20, device="cuda",
+                                         **small)
+        entries += [(_tabbed(wb, storage), wb), (_synth(wd, storage), wd)]
+    dt = {"float32": torch.float32, "float16": torch.float16, "bfloat16": torch.bfloat16}[storage]
+    frames = [torch.as_tensor(w.rf, device="cuda").to(dt) for _, w in entries]
+    singles = [bf(f, out_as_numpy=False).clone() for (bf, _), f in zip(entries, frames)]
+    bfs = [bf for bf, _ in entries]
+    assert (max(b.ntx for b in bfs) > 12) == big
+    for cfg in (BatchConfig(1, 1, 0, 4), BatchConfig(2, 0, 0, 3)):
+        outs = BatchBeamformer(bfs, config=cfg)(frames)
+        for k, (o, s) in enumerate(zip(outs, singles)):
+            assert torch.equal(o, s), (storage, big, cfg, k, _rel(o, s))
+
+
 def test_graph_replay_follows_the_inputs(batch):
     bfs, frames, singles = batch
     bb = BatchBeamformer(bfs, config=BatchConfig())
