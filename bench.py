@@ -491,7 +491,7 @@ def main_ours(a):
         if v:
             tg[key] = {"value": v["value"], "vs_plain": v["value"] / value,
                        "fp64_rel_l2": v.get("fp64_rel_l2")}
-    line["north_star_targets"] = tg
+    line["target_summary"] = tg
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
