@@ -4,9 +4,10 @@
 // host may store the tables in a locality-friendly pixel order and pass
 // pixel_index to scatter the results back).  Loop order: receive outer,
 // transmit inner.  The transmit-side delays and weights of a pixel are loaded
-// (Tabbed) or computed (Synthetic) once, into registers when ntx <= kTxReg,
-// else into this thread's column of shared memory; receive-side values are
-// loaded or computed once per receive.  Each tap gathers one coefficient
+// (Tabbed) or computed (Synthetic) once, into registers when ntx <= kTxReg;
+// beyond, the delays go to this thread's column of shared memory and the
+// Tabbed weights are read from the table per receive (L1-resident rows);
+// receive-side values are loaded or computed once per receive.  Each tap gathers one coefficient
 // record of its channel (cubic) or one/two samples (nearest/linear) through
 // the read-only path and accumulates in registers: no atomics, one store per
 // output element.
