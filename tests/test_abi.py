@@ -229,6 +229,9 @@ def test_batch_plan_validates_jobs():
     bad.coef = 8
     assert plan((_lib.BatchJob * 2)(j, bad)) == _lib.EINVAL
     bad = _lib.BatchJob.from_buffer_copy(j)
+    bad.rf.dtype = _lib.I16  # int16 counts: not a storage type of the batch
+    assert plan((_lib.BatchJob * 2)(j, bad)) == _lib.EINVAL
+    bad = _lib.BatchJob.from_buffer_copy(j)
     bad.geom = 1  # synthetic without geometry
     assert plan((_lib.BatchJob * 2)(j, bad)) == _lib.EINVAL
     assert L.pycbf_gb_batch_run(p, ct.byref(info), 6, 10, None) == _lib.EINVAL
