@@ -455,7 +455,7 @@ int pycbf_gb_das_synthetic_adjoint(const pycbf_gb_rfinfo *rf, const void *coef,
 /* batch can be captured in one CUDA graph.                                */
 /*                                                                        */
 /* Each job is one frame: rf.nframes = 1, rfdata (ntx, nrx, nt) stored as  */
-/* float32, float16 or bfloat16 (PYCBF_GB_I16: PYCBF_GB_EINVAL); coef its  */
+/* float32, float16 or bfloat16 (PYCBF_GB_I16: PYCBF_GB_EUNSUPPORTED); coef its */
 /* own pycbf_gb_workspace_bytes(&rf, PYCBF_GB_INTERP_CUBIC) bytes          */
 /* (16-byte aligned); out (np) float32.  Tabbed jobs give the tables, np   */
 /* and thresh (geo NULL); Synthetic jobs give geo (np from geo->np; delays */

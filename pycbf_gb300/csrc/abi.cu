@@ -666,7 +666,6 @@ int check_batch_job(const pycbf_gb_batch_job &j) {
     int st = check_rf(&j.rf, j.geom == 1);
     if (st) return st;
     if (j.rf.nframes != 1) return PYCBF_GB_EINVAL;
-    if (j.rf.dtype == PYCBF_GB_I16) return PYCBF_GB_EINVAL;  // storage types only
     if (!j.rfdata || !j.coef || !j.out) return PYCBF_GB_EINVAL;
     if (reinterpret_cast<uintptr_t>(j.coef) % 16) return PYCBF_GB_EINVAL;
     if (j.rf.nt > kMaxNtSpline) return PYCBF_GB_ERANGE;

@@ -230,7 +230,7 @@ def test_batch_plan_validates_jobs():
     assert plan((_lib.BatchJob * 2)(j, bad)) == _lib.EINVAL
     bad = _lib.BatchJob.from_buffer_copy(j)
     bad.rf.dtype = _lib.I16  # int16 counts: not a storage type of the batch
-    assert plan((_lib.BatchJob * 2)(j, bad)) == _lib.EINVAL
+    assert plan((_lib.BatchJob * 2)(j, bad)) == _lib.EUNSUPPORTED
     bad = _lib.BatchJob.from_buffer_copy(j)
     bad.geom = 1  # synthetic without geometry
     assert plan((_lib.BatchJob * 2)(j, bad)) == _lib.EINVAL
