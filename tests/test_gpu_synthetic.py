@@ -150,6 +150,41 @@ def test_synthetic_delay_branches(ndim, dof, behind):
     np.testing.assert_array_equal(isum.cpu().numpy(), ok_isum)
 
 
+@pytest.fixture(scope="module")
+def synthetic_wide():
+    """21 plane waves (> 12: the shared-memory column form) over a field
+    wider than the aperture, so that most warps of pixels see only part of
+    the transmits, some none, and the last warp is partial (37 x 45
+    pixels)."""
+    return phantom.linear_pw_synthetic(nele=32, nsteer=21, nt=1024, nx=37, nz=45, n_speckle=800,
+                                       xlim=(-14e-3, 14e-3), zlim=(4e-3, 24e-3), device="cuda")
+
+
+@pytest.mark.parametrize("sumtype", ["tx_and_rx", "tx_only"])
+def test_synthetic_column_form_masked_field(synthetic_wide, sumtype):
+    """The column form on transmit masks that differ between and within
+    warps: images against the oracle, and (tx_and_rx) bit for bit the image
+    of the batched queue kernel, which runs the same pixel body."""
+    from pycbf_gb300.batch import BatchBeamformer, BatchConfig
+    w = synthetic_wide
+    tables = oracle_tables(w)
+    live = (tables[1] != 0).reshape(21, -1)  # transmit masks, pixels in table order
+    nwarp = -(-live.shape[1] // 32)
+    pad = np.zeros((21, nwarp * 32 - live.shape[1]), bool)
+    anyl = np.concatenate([live, pad], 1).reshape(21, nwarp, 32).any(-1)
+    runs = anyl.sum(0)
+    assert (runs < 21).sum() >= nwarp // 4 and (runs == 0).any() and (runs == 21).any()
+    bf = synth_bf(w, interp={"kind": "cubic"}, sumtype=sumtype)
+    out = bf(w.rf, out_as_numpy=False)
+    ref = oracle_image(w, tables, "cubic", sumtype)
+    r, m = assert_image_close(out.cpu().numpy(), ref, what=sumtype)
+    report(f"synthetic_wide_column_{sumtype}", rel_l2=r, max_abs_peak=m)
+    if sumtype == "tx_and_rx":
+        rf = torch.as_tensor(w.rf, device="cuda")
+        (b,) = BatchBeamformer([bf], config=BatchConfig(1, 1, 0, 4))([rf])
+        assert torch.equal(b, bf(rf, out_as_numpy=False))
+
+
 @pytest.mark.parametrize("dmastype", ["ssr", "power"])
 def test_fused_dmas_all_pairs(synthetic_small, dmastype):
     w = synthetic_small
